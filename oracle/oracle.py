@@ -1,0 +1,153 @@
+"""ORACLE — test infrastructure, not product code.
+
+ctypes front end of ``oracle/gsph_oracle.cpp``, the CPU restatement of GANDALF's grad-h
+SPH + KD-tree gravity step.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's
+CPU-baseline leg import this module, and only as the checker.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "gsph_oracle.cpp")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "libgsph_oracle.so")
+
+PARTICLE_FIELDS = ["h", "rho", "invomega", "zeta", "hfactor", "pressure", "sound", "u",
+                   "div_v", "dudt", "ax", "ay", "az", "agx", "agy", "agz", "gpot",
+                   "gpot_hydro", "hrangesqd", "levelneib"]
+CELL_FIELDS = ["N", "level", "m", "rmax", "hmax", "cdistsqd", "bbmin0", "bbmin1", "bbmin2",
+               "bbmax0", "bbmax1", "bbmax2", "hbmin0", "hbmin1", "hbmin2", "hbmax0", "hbmax1",
+               "hbmax2", "rcell0", "rcell1", "rcell2", "r0", "r1", "r2", "q0", "q1", "q2", "q3",
+               "q4", "first", "pad"]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("self_gravity", ctypes.c_int32), ("eos", ctypes.c_int32),
+                ("periodic", ctypes.c_int32), ("nleafmax", ctypes.c_int32),
+                ("multipole", ctypes.c_int32), ("hydro_forces", ctypes.c_int32),
+                ("pad0", ctypes.c_int32), ("pad1", ctypes.c_int32),
+                ("h_fac", ctypes.c_double), ("h_converge", ctypes.c_double),
+                ("alpha_visc", ctypes.c_double), ("beta_visc", ctypes.c_double),
+                ("gamma_eos", ctypes.c_double), ("thetamaxsqd", ctypes.c_double),
+                ("temp0", ctypes.c_double), ("mu_bar", ctypes.c_double),
+                ("boxmin", ctypes.c_double * 3), ("boxmax", ctypes.c_double * 3)]
+
+
+DEFAULTS = dict(self_gravity=0, eos=0, periodic=0, nleafmax=8, multipole=1, h_fac=1.2,
+                h_converge=0.01, alpha_visc=1.0, beta_visc=2.0, gamma_eos=5.0 / 3.0,
+                thetamaxsqd=0.25, temp0=1.0, mu_bar=1.0, boxmin=(0.0, 0.0, 0.0),
+                boxmax=(1.0, 1.0, 1.0))
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement (g++, OpenMP, no FP contraction) into oracle/_build."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = LIB + ".tmp"
+    cmd = ["g++", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17",
+           SRC, "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = ctypes.CDLL(LIB)
+        vp, i64, i32, dp = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+        lib.gsph_oracle_create.restype = vp
+        lib.gsph_oracle_create.argtypes = [ctypes.POINTER(Params)]
+        lib.gsph_oracle_destroy.argtypes = [vp]
+        lib.gsph_oracle_run.restype = i32
+        lib.gsph_oracle_run.argtypes = [vp, i64] + [dp] * 9 + [i32, i32]
+        lib.gsph_oracle_particles.argtypes = [vp, dp]
+        lib.gsph_oracle_ncell.restype = i32
+        lib.gsph_oracle_ncell.argtypes = [vp]
+        lib.gsph_oracle_ltot.restype = i32
+        lib.gsph_oracle_ltot.argtypes = [vp]
+        lib.gsph_oracle_cells.argtypes = [vp, dp]
+        lib.gsph_oracle_order.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
+        lib.gsph_oracle_list.restype = i64
+        lib.gsph_oracle_list.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32)]
+        lib.gsph_oracle_counts.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+        _lib = lib
+    return _lib
+
+
+def make_params(params: dict) -> Params:
+    p = dict(DEFAULTS)
+    p.update({k: v for k, v in params.items() if k in DEFAULTS})
+    s = Params()
+    for k in ("self_gravity", "eos", "periodic", "nleafmax", "multipole"):
+        setattr(s, k, int(p[k]))
+    s.hydro_forces = 1
+    for k in ("h_fac", "h_converge", "alpha_visc", "beta_visc", "gamma_eos", "thetamaxsqd",
+              "temp0", "mu_bar"):
+        setattr(s, k, float(p[k]))
+    for k in range(3):
+        s.boxmin[k] = float(p["boxmin"][k])
+        s.boxmax[k] = float(p["boxmax"][k])
+    return s
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0) -> dict:
+    """One step of the restated algorithm; same result layout as oracle/refio.run."""
+    lib = _load()
+    prm = make_params(params)
+    h = lib.gsph_oracle_create(ctypes.byref(prm))
+    try:
+        arrs = [np.ascontiguousarray(ics[k], dtype=np.float64)
+                for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")]
+        n = len(arrs[0])
+        st = lib.gsph_oracle_run(h, n, *[_ptr(a) for a in arrs], int(lists), int(nthreads))
+        if st != 0:
+            raise RuntimeError(f"oracle step failed with status {st}")
+        out = np.empty((n, len(PARTICLE_FIELDS)))
+        lib.gsph_oracle_particles(h, _ptr(out))
+        nc = lib.gsph_oracle_ncell(h)
+        cells = np.empty((nc, len(CELL_FIELDS)))
+        lib.gsph_oracle_cells(h, _ptr(cells))
+        order = np.empty(n, dtype=np.int32)
+        lib.gsph_oracle_order(h, order.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        counts = (ctypes.c_int64 * 4)()
+        lib.gsph_oracle_counts(h, counts)
+        res = {
+            "particles": {k: out[:, i].copy() for i, k in enumerate(PARTICLE_FIELDS)},
+            "cells": {k: cells[:, i].copy() for i, k in enumerate(CELL_FIELDS)},
+            "order": order, "ltot": lib.gsph_oracle_ltot(h),
+            "counts": dict(density_pairs=counts[0], hydro_pairs=counts[1],
+                           direct_pairs=counts[2], cell_pairs=counts[3]),
+        }
+        if lists:
+            names = {0: "hydro_neib", 1: "grav_direct", 2: "gcell_lists"}
+            for which, name in names.items():
+                cnt = n if which < 2 else lib.gsph_oracle_list(h, 3, None, None)
+                tot = lib.gsph_oracle_list(h, which, None, None)
+                off = np.zeros(cnt + 1, dtype=np.int32)
+                ids = np.zeros(max(tot, 1), dtype=np.int32)
+                lib.gsph_oracle_list(h, which, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                     ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+                res[name] = [ids[off[i]:off[i + 1]] for i in range(cnt)]
+            nl = lib.gsph_oracle_list(h, 3, None, None)
+            leaf = np.zeros(max(nl, 1), dtype=np.int32)
+            lib.gsph_oracle_list(h, 3, None, leaf.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+            res["gcell_leaf"] = leaf[:nl]
+        return res
+    finally:
+        lib.gsph_oracle_destroy(h)
