@@ -1,0 +1,384 @@
+"""Benchmark: particle updates/s of the grad-h SPH + KD-tree gravity step on one GB300.
+
+Workload (default): the self-gravitating Plummer sphere, N = 262,144 gas particles,
+geometric opening angle theta = 0.5 (thetamaxsqd = 0.25), quadrupole cells, Nleafmax = 8,
+seeded synthetic particles (gandalf_gb300.ics.plummer_sphere).  One step = KD-tree build
++ grad-h h-rho solve + tree hmax update + hydro + self-gravity forces for every particle;
+one particle update = one particle through that step.
+
+Arms:
+  --impl gsph (default)  the CUDA library; `value` is device-resident throughput, `e2e`
+                         goes through the array-of-structures C ABI with host records
+                         copied in and out every step.
+  --impl reference       the CPU restatement of the reference algorithm (oracle/) on all
+                         host cores (the upstream binary is compiled only where its sources
+                         are available).
+Under torchrun each rank runs an independent replica on its own GPU (the step has no
+exchange between simulations); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle updates/s (SPH+tree gravity), mixed vs FP64 GPU at ≤1e-4 RMS rel error"
+UNIT = "particle updates/s"
+
+# Algorithmic floating-point operations per interaction, counted from the reference
+# formulas (add/sub/mul = 1, fused multiply-add = 2, sqrt and division = 1 each):
+#   density pair, per h iteration       GradhSph.cpp:197-204          42
+#   hydro pair                          GradhSph.cpp:384-447          80
+#   hydro + softened-gravity pair       GradhSph.cpp:498-571         145
+#   Newtonian direct term               GradhSph.cpp:671-686          24
+#   quadrupole cell term                NeighbourSearch.h:423-449     82
+#   monopole cell term                  NeighbourSearch.h:359-373     24
+FLOPS = dict(density=42, hydro=80, hydro_grav=145, direct=24, quad=82, mono=24)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gsph", choices=["gsph", "reference"])
+    ap.add_argument("--workload", default="plummer_sphere")
+    ap.add_argument("--n", type=int, default=0)
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name, n):
+    from gandalf_gb300 import ics
+    if name == "plummer_sphere":
+        return ics.plummer_sphere(n or 262144, seed=4321)
+    if name == "periodic_cube":
+        return ics.periodic_cube(n or 32768, seed=1234)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def workload_config(name, c):
+    p = c["params"]
+    cfg = {"workload": name, "n": len(c["x"]), "nleafmax": 8, "h_fac": 1.2, "h_converge": 0.01,
+           "kernel": "m4", "alpha_visc": 1.0, "beta_visc": 2.0}
+    if p.get("self_gravity"):
+        cfg.update(thetamaxsqd=p["thetamaxsqd"], multipole="quadrupole", gravity_mac="geometric")
+    else:
+        cfg.update(boundaries="periodic")
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def gradh_records(c):
+    """Host records laid out like GradhSphParticle<3> (src/Headers/Particle.h:133-368)."""
+    import torch
+    fields = [("flags", "<u4"), ("ptype", "<i4"), ("iorig", "<i4"), ("sinkid", "<i4"),
+              ("levelneib", "<i4"), ("nstep", "<i4"), ("nlast", "<i4"), ("level", "<i4"),
+              ("r", "<f8", 3), ("v", "<f8", 3), ("a", "<f8", 3), ("atree", "<f8", 3),
+              ("r0", "<f8", 3), ("v0", "<f8", 3), ("a0", "<f8", 3), ("m", "<f8"), ("h", "<f8"),
+              ("h_dust", "<f8"), ("hrangesqd", "<f8"), ("hfactor", "<f8"), ("sound", "<f8"),
+              ("rho", "<f8"), ("pressure", "<f8"), ("u", "<f8"), ("u0", "<f8"), ("dudt0", "<f8"),
+              ("dudt", "<f8"), ("gpot", "<f8"), ("gpot_hydro", "<f8"), ("dt", "<f8"),
+              ("dt_next", "<f8"), ("tlast", "<f8"), ("ionfrac", "<f8"), ("Xion", "<f8"),
+              ("ueq", "<f8"), ("dt_therm", "<f8"), ("vsig_max", "<f8"), ("rad_pres", "<f8", 3),
+              ("ionstate", "<i4"), ("pad", "<i4"), ("div_v", "<f8"), ("alpha", "<f8"),
+              ("dalphadt", "<f8"), ("invomega", "<f8"), ("zeta", "<f8")]
+    dt = np.dtype(fields)
+    n = len(c["x"])
+    buf = torch.empty(n * dt.itemsize, dtype=torch.uint8, pin_memory=True)
+    rec = buf.numpy().view(dt)
+    rec[:] = np.zeros(1, dtype=dt)
+    rec["r"] = np.stack([c["x"], c["y"], c["z"]], 1)
+    rec["v"] = np.stack([c["vx"], c["vy"], c["vz"]], 1)
+    rec["m"], rec["u"], rec["h"] = c["m"], c["u"], c["h"]
+    rec["iorig"] = np.arange(n)
+    rec["alpha"] = 1.0
+    off = {k: dt.fields[k][1] for k in ("r", "v", "m", "h", "u", "rho", "invomega", "zeta", "hfactor",
+                                         "hrangesqd", "pressure", "sound", "div_v", "dudt", "a",
+                                         "atree", "gpot", "gpot_hydro")}
+    return buf, rec, off
+
+
+def algorithmic_flops(st, gravity, quad=True):
+    """(flops of the force kernel, flops of the density kernel) from the interaction counts."""
+    if gravity:
+        fk = (st["hydro_pairs"] * FLOPS["hydro_grav"] + st["direct_pairs"] * FLOPS["direct"] +
+              st["cell_pairs"] * (FLOPS["quad"] if quad else FLOPS["mono"]))
+    else:
+        fk = st["hydro_pairs"] * FLOPS["hydro"]
+    return fk, st["density_pairs"] * FLOPS["density"]
+
+
+def run_form(c, params, precision, steps, warmup, flush):
+    import torch
+    from gandalf_gb300.sph import GradhSphTree
+
+    dev = {k: torch.from_numpy(np.ascontiguousarray(c[k])).cuda() for k in
+           ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")}
+    t = GradhSphTree(params, precision=precision, device=torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    t.set_stream(stream.cuda_stream)
+    for _ in range(warmup):
+        t.set_particles(dev)
+        t.step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    per = {"ms_build": 0.0, "ms_density": 0.0, "ms_hmax": 0.0, "ms_forces": 0.0}
+    launches = 0
+    st = None
+    for k in range(steps):
+        flush.zero_()                      # L2 flush, outside the timed pair
+        ev[k][0].record(stream)
+        t.set_particles(dev)
+        t.step()
+        ev[k][1].record(stream)
+        st = t.stats()
+        for key in per:
+            per[key] += st[key]
+        launches += st["launches"]
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    out = t.results()
+    t.close()
+    return {"ms_total": ms, "per": {k: v / steps for k, v in per.items()}, "stats": st,
+            "launches": launches, "results": out}
+
+
+def run_e2e(c, params, precision, steps, warmup):
+    from gandalf_gb300.sph import GradhSphTree
+    import torch
+    buf, rec, off = gradh_records(c)
+    t = GradhSphTree(params, precision=precision, device=torch.cuda.current_device())
+    for _ in range(max(1, warmup)):
+        t.set_particles_aos(rec, off)
+        t.step()
+        t.get_particles_aos(rec, off)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t.set_particles_aos(rec, off)
+        t.step()
+        t.get_particles_aos(rec, off)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    t.close()
+    n = len(rec)
+    return {"wall": wall, "bytes": n * rec.dtype.itemsize}
+
+
+def cpu_baseline(c, params, budget_s=40.0):
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.run(c, params, nthreads=cores)
+    wall = time.perf_counter() - t0
+    return {"value": len(c["x"]) / wall, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"one full step of the {len(c['x'])}-particle workload "
+                      f"(tree build + h solve + forces), {wall:.2f} s wall"}
+
+
+def reference_arm(args):
+    from oracle import oracle
+    c = workload(args.workload, args.n)
+    params = dict(c["params"])
+    cores = os.cpu_count() or 1
+    n = len(c["x"])
+    t0 = time.perf_counter()
+    oracle.run(c, params, nthreads=cores)          # first warm-up step sizes the run
+    t_one = time.perf_counter() - t0
+    budget = 150.0
+    warm = min(max(args.warmup - 1, 0), int(budget / 3 / max(t_one, 1e-3)))
+    for _ in range(warm):
+        oracle.run(c, params, nthreads=cores)
+    k = max(1, min(args.steps, int(budget / max(t_one, 1e-3))))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        oracle.run(c, params, nthreads=cores)
+    wall = time.perf_counter() - t0
+    value = n * k / wall
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / k, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args.workload, c), "impl": "reference",
+            "steps_executed": k,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{k} full steps of the {n}-particle workload on {cores} host threads "
+                                       "(oracle/gsph_oracle.cpp, the C++ restatement of the reference path)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from gandalf_gb300 import _native
+    from gandalf_gb300 import build as gbuild
+    gbuild.build()
+    lib = _native.load()
+    c = workload(args.workload, args.n)
+    params = dict(c["params"])
+    gravity = bool(params.get("self_gravity"))
+    n = len(c["x"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    forms = ["fp64", "mixed"] if args.precision == "auto" else [args.precision]
+    results = {}
+    with ClockSampler(local) as clk:
+        for form in forms:
+            try:
+                if world > 1:
+                    dist.barrier()
+                torch.cuda.synchronize()
+                results[form] = run_form(c, params, form, args.steps, args.warmup, flush)
+                if world > 1:
+                    dist.barrier()
+                torch.cuda.synchronize()
+            except RuntimeError as e:
+                if args.precision != "auto":
+                    raise
+                results[form] = {"error": str(e)}
+    clocks = clk.summary()
+    ok = [f for f in forms if "error" not in results[f]]
+    head = "mixed" if "mixed" in ok else ok[0]
+    R = results[head]
+    ms = R["ms_total"]
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * n * args.steps / (ms * 1e-3)
+    e2e = None
+    if not args.no_e2e:
+        E = run_e2e(c, params, head, max(1, min(args.steps, 5)), 1)
+        k = max(1, min(args.steps, 5))
+        e2e = {"value": n * k / E["wall"] * world, "unit": UNIT, "h2d_bytes_per_step": E["bytes"],
+               "d2h_bytes_per_step": E["bytes"], "path": "gsph_set_particles_aos + gsph_step + "
+                                                         "gsph_get_particles_aos, pinned host records"}
+    st = R["stats"]
+    f_force, f_dens = algorithmic_flops(st, gravity)
+    fp64 = head == "fp64"
+    peak_gf = lib.gsph_fma_peak_gflops(local, 1 if fp64 else 0)
+    achieved = f_force / (R["per"]["ms_forces"] * 1e-3) / 1e12
+    roof = {"bound": "fp64" if fp64 else "fp32", "kernel": "all-forces" if gravity else "hydro-forces",
+            "achieved": achieved, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
+            "frac": achieved / (peak_gf / 1e3) if peak_gf > 0 else None, "traffic": None,
+            "peak_source": "measured FMA-loop throughput of this GPU (gsph_fma_peak_gflops); "
+                           "MEASURED_PEAKS.json holds HBM and bf16 figures only",
+            "flops_per_launch": f_force, "ms_per_launch": R["per"]["ms_forces"]}
+    forms_out = {}
+    for f in forms:
+        if "error" in results[f]:
+            forms_out[f] = {"error": results[f]["error"][:200]}
+            continue
+        Rf = results[f]
+        forms_out[f] = {"value": n * args.steps / (Rf["ms_total"] * 1e-3),
+                        "ms_per_step": Rf["ms_total"] / args.steps,
+                        "phases_ms": {k: round(v, 4) for k, v in Rf["per"].items()}}
+    if "fp64" in ok and "mixed" in ok:
+        a, b = results["mixed"]["results"], results["fp64"]["results"]
+        errs = {}
+        for k in ("rho", "h"):
+            e = np.abs(a[k] - b[k]) / np.abs(b[k])
+            errs[k] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
+        A = np.stack([a["ax"], a["ay"], a["az"]], 1)
+        B = np.stack([b["ax"], b["ay"], b["az"]], 1)
+        nb = np.linalg.norm(B, axis=1)
+        e = np.linalg.norm(A - B, axis=1) / nb
+        errs["a"] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
+        forms_out["mixed_vs_fp64_rel_err"] = errs
+        forms_out["speedup_mixed_over_fp64"] = results["fp64"]["ms_total"] / results["mixed"]["ms_total"]
+    cfg = workload_config(args.workload, c)
+    cfg.update(precision=head, l2="flushed between timed steps (256 MiB write, outside the timed span)",
+               parallelism=f"replicas{world}")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if fp64 else "f32 pairs / f64 positions",
+            "data": "synthetic", "config": cfg, "e2e": e2e, "gpu_launches": R["launches"],
+            "roofline": roof, "forms": forms_out, "clocks": clocks}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(c, params)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

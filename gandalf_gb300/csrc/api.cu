@@ -1,0 +1,853 @@
+// C ABI of the GB300 grad-h SPH + KD-tree gravity step (declared in include/gsph_gb300.h).
+//
+// Host orchestration of one step, following HydroTree/GradhSphTree
+// (src/Tree/HydroTree.cpp:309-441, src/GradhSph/GradhSphTree.cpp:82-657):
+//   build tree -> h-rho solve -> hmax update -> hydro or hydro + gravity forces.
+// Device memory is owned by the context and sized for the largest N seen.  Every launch
+// goes to the context's stream; a step synchronises once at its end to read the
+// kernels' status word.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gsph_gb300.h"
+#include "gsph_state.cuh"
+#include "kernels.cuh"
+#include "tree.cuh"
+
+using namespace gsph;
+
+namespace {
+
+thread_local int g_create_error = GSPH_OK;
+
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct gsph_ctx {
+  gsph_config cfg;
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream all work is launched on
+  cudaStream_t own_stream = nullptr;  // the context's own stream
+  unsigned launches = 0;              // kernels launched since the step began
+  std::string err;
+  std::vector<Buf> bufs;     // everything allocated for the current capacity
+  int cap = 0;               // particle capacity of the allocations
+  int cap_ncell = 0;
+  int n = 0;                 // particles of the current set
+  bool have_particles = false, have_tree = false, have_props = false, have_forces = false;
+  // topology of the current n
+  int ltot = 0, ncell = 0, nleaf = 0, P = 0, lpg = 4;
+  // device arrays
+  double* in[9] = {};        // x y z vx vy vz m u h (input order)
+  double* f[26] = {};        // leaf-order fields (see kF* below)
+  int* id = nullptr;
+  int *cell_first = nullptr, *cell_n = nullptr, *cell_parent = nullptr, *leaf_cell = nullptr;
+  unsigned char* cell_level = nullptr;
+  int *heap_first = nullptr, *heap_n = nullptr, *heap_ones = nullptr;
+  CellGeom* geom = nullptr;
+  CellBox *bb = nullptr, *hbox = nullptr;
+  CellMoment* mom = nullptr;
+  unsigned* climb = nullptr;
+  unsigned long long* key[3] = {};
+  int* idx[3] = {};
+  int* listb[3] = {};
+  unsigned char *side = nullptr, *seg_axis = nullptr;
+  int* blocksum = nullptr;
+  unsigned long long* rootkey = nullptr;
+  double* ibox = nullptr;
+  unsigned long long* counters = nullptr;    // [0] status, [1..5] counts
+  double* scratch_out = nullptr;             // n doubles for field scatter
+  // array-of-structures staging
+  void* aos = nullptr;
+  size_t aos_bytes = 0;
+  int64_t aos_stride = 0;
+  // recording
+  int record = 0, rec_max = 0;
+  int* rec_sph_cnt = nullptr;
+  int* rec_sph_ids = nullptr;
+  unsigned long long *rec_dir_cnt = nullptr, *rec_dir_hash = nullptr, *rec_cell_cnt = nullptr,
+                     *rec_cell_hash = nullptr;
+  size_t rec_bytes = 0;
+  // timing
+  cudaEvent_t ev[5] = {};
+  gsph_stats last{};
+};
+
+namespace {
+
+enum {
+  kFX = 0, kFY, kFZ, kFVX, kFVY, kFVZ, kFM, kFU, kFH, kFH0, kFRho, kFInvOmega, kFZeta, kFHfactor,
+  kFHrangesqd, kFPressure, kFSound, kFAX, kFAY, kFAZ, kFAGX, kFAGY, kFAGZ, kFGpot, kFDudt, kFDivV,
+  kNumFields
+};
+
+int fail(gsph_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(gsph_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, GSPH_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define GSPH_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+  } while (0)
+
+void free_all(gsph_ctx* c) {
+  for (Buf& b : c->bufs) if (b.p) cudaFree(b.p);
+  c->bufs.clear();
+  c->cap = 0;
+  c->cap_ncell = 0;
+}
+
+template <class T>
+int alloc(gsph_ctx* c, T*& ptr, size_t count) {
+  void* p = nullptr;
+  const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+  c->bufs.push_back({p, bytes});
+  ptr = static_cast<T*>(p);
+  return GSPH_OK;
+}
+
+int tree_levels(int n, int nleafmax) {
+  int l = 0;
+  while ((double) nleafmax * std::pow(2.0, l) < (double) n) l++;
+  return l;
+}
+
+// Host tables of the tree shape for n particles (KDTree::CreateTreeStructure layout).
+struct Shape {
+  std::vector<int> cell_first, cell_n, cell_parent, leaf_cell, heap_first, heap_n, heap_ones;
+  std::vector<unsigned char> cell_level;
+};
+
+void make_shape(int n, int ltot, Shape& s) {
+  const int ncell = 2 * (1 << ltot) - 1;
+  s.cell_first.assign(ncell, 0); s.cell_n.assign(ncell, 0); s.cell_parent.assign(ncell, -1);
+  s.cell_level.assign(ncell, 0); s.leaf_cell.assign(1 << ltot, 0);
+  s.heap_first.assign(ncell, 0); s.heap_n.assign(ncell, 0); s.heap_ones.assign(ncell, 0);
+  struct Item { int c, h, level, first, cnt, parent; };
+  std::vector<Item> st;
+  st.push_back({0, 0, 0, 0, n, -1});
+  while (!st.empty()) {
+    Item it = st.back();
+    st.pop_back();
+    s.cell_first[it.c] = it.first; s.cell_n[it.c] = it.cnt; s.cell_parent[it.c] = it.parent;
+    s.cell_level[it.c] = (unsigned char) it.level;
+    s.heap_first[it.h] = it.first; s.heap_n[it.h] = it.cnt;
+    if (it.level == ltot) {
+      s.leaf_cell[it.h - ((1 << ltot) - 1)] = it.c;
+      continue;
+    }
+    const int half = it.cnt / 2;
+    const int c2 = it.c + (1 << (ltot - it.level));
+    st.push_back({c2, 2 * it.h + 2, it.level + 1, it.first + half, it.cnt - half, it.c});
+    st.push_back({it.c + 1, 2 * it.h + 1, it.level + 1, it.first, half, it.c});
+  }
+  for (int l = 0; l <= ltot; l++) {
+    int acc = 0;
+    for (int q = 0; q < (1 << l); q++) {
+      const int h = (1 << l) - 1 + q;
+      s.heap_ones[h] = acc;
+      acc += s.heap_n[h] - s.heap_n[h] / 2;
+    }
+  }
+}
+
+int ensure_capacity(gsph_ctx* c, int n) {
+  const int ltot = tree_levels(n, c->cfg.nleafmax);
+  if (ltot > 23) return fail(c, GSPH_ERR_UNSUPPORTED, "tree deeper than 23 levels");
+  const int ncell = 2 * (1 << ltot) - 1;
+  const int P = sort_padded_size(n);
+  bool fresh = false;
+  if (n > c->cap || ncell > c->cap_ncell || P > sort_padded_size(std::max(c->cap, 1))) {
+    fresh = true;
+    free_all(c);
+    const int capn = n, capc = ncell, capP = P;
+    int rc = GSPH_OK;
+    for (int q = 0; q < 9 && rc == GSPH_OK; q++) rc = alloc(c, c->in[q], capn);
+    for (int q = 0; q < kNumFields && rc == GSPH_OK; q++) rc = alloc(c, c->f[q], capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->id, capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->cell_first, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->cell_n, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->cell_parent, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->cell_level, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->leaf_cell, (capc + 1) / 2);
+    if (rc == GSPH_OK) rc = alloc(c, c->heap_first, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->heap_n, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->heap_ones, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->geom, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->bb, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->hbox, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->mom, capc);
+    if (rc == GSPH_OK) rc = alloc(c, c->climb, capc);
+    for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->key[q], capP);
+    for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->idx[q], capP);
+    for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->listb[q], capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->side, capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->seg_axis, (capc + 1) / 2);
+    if (rc == GSPH_OK) rc = alloc(c, c->blocksum, 3 * (size_t) partition_blocks(capn) + 3);
+    if (rc == GSPH_OK) rc = alloc(c, c->rootkey, 8);
+    if (rc == GSPH_OK) rc = alloc(c, c->ibox, 6 * ((size_t) 2 * capc + 3));
+    if (rc == GSPH_OK) rc = alloc(c, c->counters, 16);
+    if (rc == GSPH_OK) rc = alloc(c, c->scratch_out, capn);
+    if (rc != GSPH_OK) { free_all(c); return rc; }
+    c->cap = capn;
+    c->cap_ncell = capc;
+    c->rec_bytes = 0;   // recording buffers were freed with the rest
+    c->rec_sph_cnt = nullptr;
+  }
+  if (fresh || n != c->n || ltot != c->ltot || !c->have_particles) {
+    Shape s;
+    make_shape(n, ltot, s);
+    cudaStream_t st = c->stream;
+    GSPH_CUDA(cudaMemcpyAsync(c->cell_first, s.cell_first.data(), sizeof(int) * ncell, cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaMemcpyAsync(c->cell_n, s.cell_n.data(), sizeof(int) * ncell, cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaMemcpyAsync(c->cell_parent, s.cell_parent.data(), sizeof(int) * ncell, cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaMemcpyAsync(c->cell_level, s.cell_level.data(), ncell, cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaMemcpyAsync(c->leaf_cell, s.leaf_cell.data(), sizeof(int) * (1 << ltot), cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaMemcpyAsync(c->heap_first, s.heap_first.data(), sizeof(int) * ncell, cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaMemcpyAsync(c->heap_n, s.heap_n.data(), sizeof(int) * ncell, cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaMemcpyAsync(c->heap_ones, s.heap_ones.data(), sizeof(int) * ncell, cudaMemcpyHostToDevice, st));
+    GSPH_CUDA(cudaStreamSynchronize(st));   // host tables go out of scope
+    int maxleaf = 0;
+    for (int q = 0; q < (1 << ltot); q++) maxleaf = std::max(maxleaf, s.cell_n[s.leaf_cell[q]]);
+    int p2 = 1;
+    while (p2 < maxleaf) p2 <<= 1;
+    if (p2 > 32) return fail(c, GSPH_ERR_UNSUPPORTED, "leaf cells hold more than 32 particles");
+    c->lpg = 32 / p2;
+  }
+  c->n = n;
+  c->ltot = ltot;
+  c->ncell = ncell;
+  c->nleaf = 1 << ltot;
+  c->P = P;
+  return GSPH_OK;
+}
+
+SphParams make_params(const gsph_config& cfg) {
+  SphParams p{};
+  p.h_fac = cfg.h_fac; p.h_converge = cfg.h_converge; p.alpha_visc = cfg.alpha_visc;
+  p.beta_visc = cfg.beta_visc; p.gamma_eos = cfg.gamma_eos; p.temp0 = cfg.temp0; p.mu_bar = cfg.mu_bar;
+  p.thetamaxsqd = cfg.thetamaxsqd;
+  for (int k = 0; k < 3; k++) {
+    p.boxmin[k] = cfg.boxmin[k]; p.boxmax[k] = cfg.boxmax[k];
+    p.boxsize[k] = cfg.boxmax[k] - cfg.boxmin[k];
+    p.boxhalf[k] = 0.5 * p.boxsize[k];
+  }
+  p.eos = cfg.eos; p.periodic = cfg.periodic; p.multipole = cfg.multipole; p.self_gravity = cfg.self_gravity;
+  return p;
+}
+
+Particles make_particles(gsph_ctx* c) {
+  Particles p{};
+  p.n = c->n;
+  p.id = c->id;
+  double** f = c->f;
+  p.x = f[kFX]; p.y = f[kFY]; p.z = f[kFZ]; p.vx = f[kFVX]; p.vy = f[kFVY]; p.vz = f[kFVZ];
+  p.m = f[kFM]; p.u = f[kFU]; p.h = f[kFH]; p.h0 = f[kFH0];
+  p.rho = f[kFRho]; p.invomega = f[kFInvOmega]; p.zeta = f[kFZeta]; p.hfactor = f[kFHfactor];
+  p.hrangesqd = f[kFHrangesqd]; p.pressure = f[kFPressure]; p.sound = f[kFSound];
+  p.ax = f[kFAX]; p.ay = f[kFAY]; p.az = f[kFAZ]; p.agx = f[kFAGX]; p.agy = f[kFAGY]; p.agz = f[kFAGZ];
+  p.gpot = f[kFGpot]; p.dudt = f[kFDudt]; p.div_v = f[kFDivV];
+  return p;
+}
+
+Tree make_tree(gsph_ctx* c) {
+  Tree t{};
+  t.n = c->n; t.ltot = c->ltot; t.ncell = c->ncell; t.nleaf = c->nleaf;
+  t.cell_first = c->cell_first; t.cell_n = c->cell_n; t.cell_level = c->cell_level;
+  t.cell_parent = c->cell_parent; t.leaf_cell = c->leaf_cell;
+  t.geom = c->geom; t.bb = c->bb; t.hbox = c->hbox; t.mom = c->mom; t.climb = c->climb;
+  return t;
+}
+
+DeviceCounters make_counters(gsph_ctx* c) {
+  DeviceCounters d{};
+  d.status = reinterpret_cast<unsigned*>(c->counters);
+  d.density_pairs = c->counters + 1;
+  d.hydro_pairs = c->counters + 2;
+  d.direct_pairs = c->counters + 3;
+  d.cell_pairs = c->counters + 4;
+  d.exact_checks = c->counters + 5;
+  d.record = c->record && c->rec_sph_cnt != nullptr;
+  d.rec_max = c->rec_max;
+  d.rec_sph_cnt = c->rec_sph_cnt; d.rec_sph_ids = c->rec_sph_ids;
+  d.rec_dir_cnt = c->rec_dir_cnt; d.rec_dir_hash = c->rec_dir_hash;
+  d.rec_cell_cnt = c->rec_cell_cnt; d.rec_cell_hash = c->rec_cell_hash;
+  return d;
+}
+
+int check_config(const gsph_config* cfg, std::string& why) {
+  if (!cfg) { why = "config is NULL"; return GSPH_ERR_INVALID; }
+  if (cfg->ndim != 3) { why = "only ndim = 3 is implemented"; return GSPH_ERR_UNSUPPORTED; }
+  if (cfg->nleafmax < 1 || cfg->nleafmax > 32) { why = "Nleafmax must be 1..32"; return GSPH_ERR_INVALID; }
+  if (cfg->eos != GSPH_EOS_ENERGY_EQN && cfg->eos != GSPH_EOS_ISOTHERMAL) { why = "unknown gas_eos"; return GSPH_ERR_UNSUPPORTED; }
+  if (cfg->multipole != GSPH_MONOPOLE && cfg->multipole != GSPH_QUADRUPOLE) { why = "unknown multipole"; return GSPH_ERR_UNSUPPORTED; }
+  if (cfg->precision != GSPH_PRECISION_FP64 && cfg->precision != GSPH_PRECISION_MIXED) { why = "unknown precision"; return GSPH_ERR_INVALID; }
+  if (cfg->precision == GSPH_PRECISION_MIXED) { why = "the mixed-precision form is not built into this library"; return GSPH_ERR_UNSUPPORTED; }
+  if (cfg->self_gravity && cfg->periodic) { why = "periodic self-gravity needs Ewald sums (not implemented)"; return GSPH_ERR_UNSUPPORTED; }
+  if (!cfg->hydro_forces) { why = "hydro_forces = 0 is not implemented"; return GSPH_ERR_UNSUPPORTED; }
+  if (!(cfg->h_fac > 0.0) || !(cfg->h_converge > 0.0) || !(cfg->gamma_eos > 1.0) || !(cfg->thetamaxsqd > 0.0)) {
+    why = "h_fac, h_converge, thetamaxsqd must be > 0 and gamma_eos > 1"; return GSPH_ERR_INVALID;
+  }
+  if (cfg->periodic)
+    for (int k = 0; k < 3; k++)
+      if (!(cfg->boxmax[k] > cfg->boxmin[k])) { why = "periodic box has non-positive size"; return GSPH_ERR_INVALID; }
+  return GSPH_OK;
+}
+
+int validate_host(gsph_ctx* c, int64_t n, const double* const* a) {
+  for (int q = 0; q < 9; q++) if (!a[q]) return fail(c, GSPH_ERR_INVALID, "particle array is NULL");
+  for (int64_t i = 0; i < n; i++) {
+    for (int q = 0; q < 9; q++)
+      if (!std::isfinite(a[q][i])) return fail(c, GSPH_ERR_INVALID, "non-finite particle data");
+    if (!(a[6][i] > 0.0)) return fail(c, GSPH_ERR_INVALID, "particle mass must be > 0");
+    if (!(a[8][i] > 0.0)) return fail(c, GSPH_ERR_INVALID, "smoothing length must be > 0");
+    if (c->cfg.periodic)
+      for (int k = 0; k < 3; k++)
+        if (a[k][i] < c->cfg.boxmin[k] || a[k][i] >= c->cfg.boxmax[k])
+          return fail(c, GSPH_ERR_INVALID, "particle outside the periodic box");
+  }
+  return GSPH_OK;
+}
+
+struct OutPtrs { double* p[9]; };
+
+__global__ void k_unpack_aos(const unsigned char* base, int n, int64_t stride, gsph_field_offsets off, OutPtrs o) {
+  double* const* dst = o.p;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned char* r = base + (size_t) i * stride;
+    const double* pr = reinterpret_cast<const double*>(r + off.r);
+    const double* pv = reinterpret_cast<const double*>(r + off.v);
+    dst[0][i] = pr[0]; dst[1][i] = pr[1]; dst[2][i] = pr[2];
+    dst[3][i] = pv[0]; dst[4][i] = pv[1]; dst[5][i] = pv[2];
+    dst[6][i] = *reinterpret_cast<const double*>(r + off.m);
+    dst[7][i] = *reinterpret_cast<const double*>(r + off.u);
+    dst[8][i] = *reinterpret_cast<const double*>(r + off.h);
+  }
+}
+
+struct FieldPtrs { const double* f[kNumFields]; };
+
+__global__ void k_pack_aos(unsigned char* base, int n, int64_t stride, gsph_field_offsets off, FieldPtrs fp,
+                           const int* __restrict__ id) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    unsigned char* r = base + (size_t) id[s] * stride;
+    auto put = [&](int64_t o, int fld) { if (o >= 0) *reinterpret_cast<double*>(r + o) = fp.f[fld][s]; };
+    put(off.h, kFH); put(off.u, kFU); put(off.rho, kFRho); put(off.invomega, kFInvOmega);
+    put(off.zeta, kFZeta); put(off.hfactor, kFHfactor); put(off.hrangesqd, kFHrangesqd);
+    put(off.pressure, kFPressure); put(off.sound, kFSound); put(off.div_v, kFDivV); put(off.dudt, kFDudt);
+    put(off.gpot, kFGpot); put(off.gpot_hydro, kFGpot);
+    if (off.a >= 0) { put(off.a, kFAX); put(off.a + 8, kFAY); put(off.a + 16, kFAZ); }
+    if (off.atree >= 0) { put(off.atree, kFAGX); put(off.atree + 8, kFAGY); put(off.atree + 16, kFAGZ); }
+  }
+}
+
+__global__ void k_scatter_field(const double* __restrict__ src, const int* __restrict__ id, int n, double* dst) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) dst[id[s]] = src[s];
+}
+
+int field_index(int field) {
+  switch (field) {
+    case GSPH_FIELD_H: return kFH;
+    case GSPH_FIELD_RHO: return kFRho;
+    case GSPH_FIELD_INVOMEGA: return kFInvOmega;
+    case GSPH_FIELD_ZETA: return kFZeta;
+    case GSPH_FIELD_HFACTOR: return kFHfactor;
+    case GSPH_FIELD_PRESSURE: return kFPressure;
+    case GSPH_FIELD_SOUND: return kFSound;
+    case GSPH_FIELD_U: return kFU;
+    case GSPH_FIELD_DIV_V: return kFDivV;
+    case GSPH_FIELD_DUDT: return kFDudt;
+    case GSPH_FIELD_AX: return kFAX;
+    case GSPH_FIELD_AY: return kFAY;
+    case GSPH_FIELD_AZ: return kFAZ;
+    case GSPH_FIELD_AGX: return kFAGX;
+    case GSPH_FIELD_AGY: return kFAGY;
+    case GSPH_FIELD_AGZ: return kFAGZ;
+    case GSPH_FIELD_GPOT: return kFGpot;
+    case GSPH_FIELD_HRANGESQD: return kFHrangesqd;
+    default: return -1;
+  }
+}
+
+int grid1(int n) { return std::max(1, std::min((n + 255) / 256, 152 * 8)); }
+
+int check_launch(gsph_ctx* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  return GSPH_OK;
+}
+
+int read_status(gsph_ctx* c) {
+  unsigned long long h[6];
+  GSPH_CUDA(cudaMemcpyAsync(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  c->last.status = (uint32_t) h[0];
+  c->last.launches = c->launches;
+  c->last.density_pairs = (int64_t) h[1];
+  c->last.hydro_pairs = (int64_t) h[2];
+  c->last.direct_pairs = (int64_t) h[3];
+  c->last.cell_pairs = (int64_t) h[4];
+  c->last.exact_checks = (int64_t) h[5];
+  const unsigned st = (unsigned) h[0];
+  if (st & kStatusHNotConverged) return fail(c, GSPH_ERR_NOT_CONVERGED, "Problem with convergence of h-rho iteration");
+  if (st & kStatusStackOverflow) return fail(c, GSPH_ERR_CAPACITY, "tree walk stack overflow");
+  if (st & kStatusRetryLimit) return fail(c, GSPH_ERR_CAPACITY, "hmax retry limit reached");
+  return GSPH_OK;
+}
+
+int do_build(gsph_ctx* c) {
+  if (!c->have_particles) return fail(c, GSPH_ERR_STATE, "no particles imported");
+  BuildArgs a{};
+  a.n = c->n; a.ltot = c->ltot; a.P = c->P;
+  a.in = InputArrays{c->in[0], c->in[1], c->in[2], c->in[3], c->in[4], c->in[5], c->in[6], c->in[7], c->in[8]};
+  for (int q = 0; q < 3; q++) { a.sort.key[q] = c->key[q]; a.sort.idx[q] = c->idx[q]; a.lists_b[q] = c->listb[q]; }
+  a.side = c->side; a.seg_axis = c->seg_axis; a.blocksum = c->blocksum; a.rootkey = c->rootkey; a.ibox = c->ibox;
+  a.heap_first = c->heap_first; a.heap_n = c->heap_n; a.heap_ones_before = c->heap_ones;
+  a.p = make_particles(c);
+  a.id_out = c->id;
+  a.tree = make_tree(c);
+  a.thetamaxsqd = c->cfg.thetamaxsqd;
+  c->launches += (unsigned) launch_build_tree(a, c->stream);
+  c->have_tree = true;
+  c->have_props = c->have_forces = false;
+  return check_launch(c, "build tree");
+}
+
+int do_props(gsph_ctx* c) {
+  if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "tree not built");
+  const Tree t = make_tree(c);
+  const Particles p = make_particles(c);
+  launch_density(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+  int rc = check_launch(c, "density");
+  if (rc) return rc;
+  cudaEventRecord(c->ev[2], c->stream);
+  launch_update_hmax(t, p, c->stream);
+  c->launches += 2;
+  c->have_props = true;
+  return check_launch(c, "update hmax");
+}
+
+int do_forces(gsph_ctx* c, bool gravity) {
+  if (!c->have_props) return fail(c, GSPH_ERR_STATE, "smoothing lengths not solved");
+  const Tree t = make_tree(c);
+  const Particles p = make_particles(c);
+  if (c->record && c->rec_sph_cnt) {
+    GSPH_CUDA(cudaMemsetAsync(c->rec_sph_cnt, 0, sizeof(int) * (size_t) c->n, c->stream));
+    GSPH_CUDA(cudaMemsetAsync(c->rec_dir_cnt, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));
+    GSPH_CUDA(cudaMemsetAsync(c->rec_dir_hash, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));
+    GSPH_CUDA(cudaMemsetAsync(c->rec_cell_cnt, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
+    GSPH_CUDA(cudaMemsetAsync(c->rec_cell_hash, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
+  }
+  if (gravity) launch_all_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+  else launch_hydro_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+  c->launches += 1;
+  c->have_forces = true;
+  return check_launch(c, "forces");
+}
+
+int begin_counters(gsph_ctx* c) {
+  c->launches = 0;
+  GSPH_CUDA(cudaMemsetAsync(c->counters, 0, 16 * sizeof(unsigned long long), c->stream));
+  return GSPH_OK;
+}
+
+int ensure_recording(gsph_ctx* c) {
+  if (!c->record) return GSPH_OK;
+  const size_t need = (size_t) c->n * (sizeof(int) * (1 + c->rec_max) + 2 * sizeof(unsigned long long)) +
+                      (size_t) c->nleaf * 2 * sizeof(unsigned long long);
+  if (c->rec_sph_cnt && c->rec_bytes >= need) return GSPH_OK;
+  int rc = alloc(c, c->rec_sph_cnt, c->n);
+  if (!rc) rc = alloc(c, c->rec_sph_ids, (size_t) c->n * c->rec_max);
+  if (!rc) rc = alloc(c, c->rec_dir_cnt, c->n);
+  if (!rc) rc = alloc(c, c->rec_dir_hash, c->n);
+  if (!rc) rc = alloc(c, c->rec_cell_cnt, c->nleaf);
+  if (!rc) rc = alloc(c, c->rec_cell_hash, c->nleaf);
+  if (rc) return rc;
+  c->rec_bytes = need;
+  return GSPH_OK;
+}
+
+}  // namespace
+
+// ======================================================================================
+extern "C" {
+
+int32_t gsph_abi_version(void) { return GSPH_ABI_VERSION; }
+
+void gsph_config_defaults(gsph_config* cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->ndim = 3;
+  cfg->nleafmax = 8;
+  cfg->hydro_forces = 1;
+  cfg->self_gravity = 0;
+  cfg->eos = GSPH_EOS_ENERGY_EQN;
+  cfg->multipole = GSPH_QUADRUPOLE;
+  cfg->periodic = 0;
+  cfg->precision = GSPH_PRECISION_FP64;
+  cfg->h_fac = 1.2;
+  cfg->h_converge = 0.01;
+  cfg->alpha_visc = 1.0;
+  cfg->beta_visc = 2.0;
+  cfg->gamma_eos = 1.66666666666666;
+  cfg->temp0 = 1.0;
+  cfg->mu_bar = 1.0;
+  cfg->thetamaxsqd = 0.1;
+  for (int k = 0; k < 3; k++) { cfg->boxmin[k] = 0.0; cfg->boxmax[k] = 1.0; }
+}
+
+int32_t gsph_create_error(void) { return g_create_error; }
+
+gsph_ctx* gsph_create(const gsph_config* cfg, int32_t device) {
+  std::string why;
+  const int rc = check_config(cfg, why);
+  if (rc != GSPH_OK) { g_create_error = rc; return nullptr; }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    g_create_error = GSPH_ERR_CUDA;
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) { g_create_error = GSPH_ERR_CUDA; return nullptr; }
+  gsph_ctx* c = new gsph_ctx();
+  c->cfg = *cfg;
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    g_create_error = GSPH_ERR_CUDA;
+    return nullptr;
+  }
+  c->stream = c->own_stream;
+  for (int q = 0; q < 5; q++) cudaEventCreate(&c->ev[q]);
+  g_create_error = GSPH_OK;
+  return c;
+}
+
+void gsph_destroy(gsph_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_all(c);
+  if (c->aos) cudaFree(c->aos);
+  for (int q = 0; q < 5; q++) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+int32_t gsph_set_stream(gsph_ctx* c, void* stream) {
+  if (!c) return GSPH_ERR_INVALID;
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  return GSPH_OK;
+}
+
+const char* gsph_last_error(const gsph_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int32_t gsph_set_particles(gsph_ctx* c, int64_t n, const double* x, const double* y, const double* z,
+                           const double* vx, const double* vy, const double* vz, const double* m,
+                           const double* u, const double* h) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (n < 1 || n > (int64_t) 1 << 30) return fail(c, GSPH_ERR_INVALID, "particle count out of range");
+  cudaSetDevice(c->device);
+  const double* a[9] = {x, y, z, vx, vy, vz, m, u, h};
+  int rc = validate_host(c, n, a);
+  if (rc) return rc;
+  rc = ensure_capacity(c, (int) n);
+  if (rc) return rc;
+  for (int q = 0; q < 9; q++)
+    GSPH_CUDA(cudaMemcpyAsync(c->in[q], a[q], sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, c->stream));
+  c->have_particles = true;
+  c->have_tree = c->have_props = c->have_forces = false;
+  return GSPH_OK;
+}
+
+int32_t gsph_set_particles_device(gsph_ctx* c, int64_t n, const double* x, const double* y, const double* z,
+                                  const double* vx, const double* vy, const double* vz, const double* m,
+                                  const double* u, const double* h) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (n < 1 || n > (int64_t) 1 << 30) return fail(c, GSPH_ERR_INVALID, "particle count out of range");
+  const double* a[9] = {x, y, z, vx, vy, vz, m, u, h};
+  for (int q = 0; q < 9; q++) if (!a[q]) return fail(c, GSPH_ERR_INVALID, "particle array is NULL");
+  cudaSetDevice(c->device);
+  int rc = ensure_capacity(c, (int) n);
+  if (rc) return rc;
+  for (int q = 0; q < 9; q++)
+    GSPH_CUDA(cudaMemcpyAsync(c->in[q], a[q], sizeof(double) * (size_t) n, cudaMemcpyDeviceToDevice, c->stream));
+  c->have_particles = true;
+  c->have_tree = c->have_props = c->have_forces = false;
+  return GSPH_OK;
+}
+
+int32_t gsph_set_particles_aos(gsph_ctx* c, const void* base, int64_t n, int64_t stride, const gsph_field_offsets* off) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!base || !off || n < 1 || n > (int64_t) 1 << 30 || stride < 8 || (stride % 8) != 0)
+    return fail(c, GSPH_ERR_INVALID, "bad array-of-structures description");
+  const int64_t ins[5] = {off->r, off->v, off->m, off->h, off->u};
+  for (int q = 0; q < 5; q++)
+    if (ins[q] < 0 || ins[q] % 8 != 0 || ins[q] + (q < 2 ? 24 : 8) > stride)
+      return fail(c, GSPH_ERR_INVALID, "input field offset outside the record or misaligned");
+  cudaSetDevice(c->device);
+  int rc = ensure_capacity(c, (int) n);
+  if (rc) return rc;
+  const size_t bytes = (size_t) n * (size_t) stride;
+  if (bytes > c->aos_bytes) {
+    if (c->aos) cudaFree(c->aos);
+    c->aos = nullptr;
+    c->aos_bytes = 0;
+    GSPH_CUDA(cudaMalloc(&c->aos, bytes));
+    c->aos_bytes = bytes;
+  }
+  c->aos_stride = stride;
+  GSPH_CUDA(cudaMemcpyAsync(c->aos, base, bytes, cudaMemcpyHostToDevice, c->stream));
+  OutPtrs o;
+  for (int q = 0; q < 9; q++) o.p[q] = c->in[q];
+  k_unpack_aos<<<grid1((int) n), 256, 0, c->stream>>>(static_cast<const unsigned char*>(c->aos), (int) n, stride,
+                                                      *off, o);
+  rc = check_launch(c, "unpack");
+  if (rc) return rc;
+  c->have_particles = true;
+  c->have_tree = c->have_props = c->have_forces = false;
+  return GSPH_OK;
+}
+
+int32_t gsph_build_tree(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  cudaSetDevice(c->device);
+  int rc = begin_counters(c);
+  if (rc) return rc;
+  rc = do_build(c);
+  if (rc) return rc;
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  return GSPH_OK;
+}
+
+int32_t gsph_update_all_sph_properties(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  cudaSetDevice(c->device);
+  int rc = begin_counters(c);
+  if (rc) return rc;
+  rc = do_props(c);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int32_t gsph_update_all_sph_hydro_forces(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  cudaSetDevice(c->device);
+  int rc = ensure_recording(c);
+  if (rc) return rc;
+  rc = begin_counters(c);
+  if (rc) return rc;
+  rc = do_forces(c, false);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int32_t gsph_update_all_sph_forces(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->cfg.self_gravity) return fail(c, GSPH_ERR_STATE, "self_gravity is off in this context");
+  cudaSetDevice(c->device);
+  int rc = ensure_recording(c);
+  if (rc) return rc;
+  rc = begin_counters(c);
+  if (rc) return rc;
+  rc = do_forces(c, true);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int32_t gsph_step(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  cudaSetDevice(c->device);
+  int rc = ensure_recording(c);
+  if (rc) return rc;
+  rc = begin_counters(c);
+  if (rc) return rc;
+  cudaEventRecord(c->ev[0], c->stream);
+  rc = do_build(c);
+  if (rc) return rc;
+  cudaEventRecord(c->ev[1], c->stream);
+  rc = do_props(c);
+  if (rc) return rc;
+  cudaEventRecord(c->ev[3], c->stream);
+  rc = do_forces(c, c->cfg.self_gravity != 0);
+  if (rc) return rc;
+  cudaEventRecord(c->ev[4], c->stream);
+  rc = read_status(c);
+  float ms[4] = {0, 0, 0, 0};
+  cudaEventElapsedTime(&ms[0], c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&ms[1], c->ev[1], c->ev[2]);
+  cudaEventElapsedTime(&ms[2], c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&ms[3], c->ev[3], c->ev[4]);
+  c->last.ms_build = ms[0]; c->last.ms_density = ms[1]; c->last.ms_hmax = ms[2]; c->last.ms_forces = ms[3];
+  c->last.ms_total = ms[0] + ms[1] + ms[2] + ms[3];
+  return rc;
+}
+
+int32_t gsph_get_field_device(gsph_ctx* c, int32_t field, double* out) {
+  if (!c || !out) return GSPH_ERR_INVALID;
+  const int fi = field_index(field);
+  if (fi < 0) return fail(c, GSPH_ERR_INVALID, "unknown field");
+  if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "no results yet");
+  cudaSetDevice(c->device);
+  k_scatter_field<<<grid1(c->n), 256, 0, c->stream>>>(c->f[fi], c->id, c->n, out);
+  return check_launch(c, "scatter field");
+}
+
+int32_t gsph_get_field(gsph_ctx* c, int32_t field, double* out) {
+  if (!c || !out) return GSPH_ERR_INVALID;
+  int rc = gsph_get_field_device(c, field, c->scratch_out);
+  if (rc) return rc;
+  GSPH_CUDA(cudaMemcpyAsync(out, c->scratch_out, sizeof(double) * (size_t) c->n, cudaMemcpyDeviceToHost, c->stream));
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  return GSPH_OK;
+}
+
+int32_t gsph_get_particles_aos(gsph_ctx* c, void* base, int64_t n, int64_t stride, const gsph_field_offsets* off) {
+  if (!c || !base || !off) return GSPH_ERR_INVALID;
+  if (!c->aos || n != c->n || stride != c->aos_stride)
+    return fail(c, GSPH_ERR_STATE, "records were not imported with gsph_set_particles_aos");
+  if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "no results yet");
+  const int64_t outs[] = {off->rho, off->invomega, off->zeta, off->hfactor, off->hrangesqd, off->pressure,
+                          off->sound, off->div_v, off->dudt, off->gpot, off->gpot_hydro, off->h, off->u};
+  for (int64_t o : outs)
+    if (o >= 0 && (o % 8 != 0 || o + 8 > stride)) return fail(c, GSPH_ERR_INVALID, "output offset outside the record");
+  for (int64_t o : {off->a, off->atree})
+    if (o >= 0 && (o % 8 != 0 || o + 24 > stride)) return fail(c, GSPH_ERR_INVALID, "output offset outside the record");
+  cudaSetDevice(c->device);
+  FieldPtrs fp;
+  for (int q = 0; q < kNumFields; q++) fp.f[q] = c->f[q];
+  k_pack_aos<<<grid1(c->n), 256, 0, c->stream>>>(static_cast<unsigned char*>(c->aos), c->n, stride, *off, fp, c->id);
+  int rc = check_launch(c, "pack");
+  if (rc) return rc;
+  GSPH_CUDA(cudaMemcpyAsync(base, c->aos, (size_t) n * (size_t) stride, cudaMemcpyDeviceToHost, c->stream));
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  return GSPH_OK;
+}
+
+int32_t gsph_get_stats(gsph_ctx* c, gsph_stats* out) {
+  if (!c || !out) return GSPH_ERR_INVALID;
+  *out = c->last;
+  out->n = c->n; out->ncell = c->ncell; out->nleaf = c->nleaf; out->ltot = c->ltot;
+  return GSPH_OK;
+}
+
+int32_t gsph_set_recording(gsph_ctx* c, int32_t enable, int32_t max_sph) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (enable && (max_sph < 1 || max_sph > 4096)) return fail(c, GSPH_ERR_INVALID, "max_sph must be 1..4096");
+  c->record = enable ? 1 : 0;
+  if (enable && max_sph != c->rec_max) { c->rec_sph_cnt = nullptr; c->rec_bytes = 0; }
+  c->rec_max = enable ? max_sph : 0;
+  return GSPH_OK;
+}
+
+int64_t gsph_get_sph_neighbours(gsph_ctx* c, int64_t* offsets, int32_t* ids) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->record || !c->rec_sph_cnt || !c->have_forces) return fail(c, GSPH_ERR_STATE, "no recorded force pass");
+  cudaSetDevice(c->device);
+  const int n = c->n;
+  std::vector<int> cntv(n), idv(n);
+  std::vector<int> sids((size_t) n * c->rec_max);
+  GSPH_CUDA(cudaMemcpy(cntv.data(), c->rec_sph_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(idv.data(), c->id, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(sids.data(), c->rec_sph_ids, sizeof(int) * sids.size(), cudaMemcpyDeviceToHost));
+  std::vector<int64_t> cnt_in(n);
+  int64_t total = 0;
+  for (int s = 0; s < n; s++) {
+    if (cntv[s] > c->rec_max) return fail(c, GSPH_ERR_CAPACITY, "recorded SPH list exceeded max_sph");
+    cnt_in[idv[s]] = cntv[s];
+    total += cntv[s];
+  }
+  if (!ids) return total;
+  if (!offsets) return GSPH_ERR_INVALID;
+  offsets[0] = 0;
+  for (int i = 0; i < n; i++) offsets[i + 1] = offsets[i] + cnt_in[i];
+  for (int s = 0; s < n; s++) {
+    const int i = idv[s];
+    for (int k = 0; k < cntv[s]; k++) ids[offsets[i] + k] = idv[sids[(size_t) s * c->rec_max + k]];
+  }
+  return total;
+}
+
+int32_t gsph_get_direct_summary(gsph_ctx* c, int64_t* counts, uint64_t* hashes) {
+  if (!c || !counts || !hashes) return GSPH_ERR_INVALID;
+  if (!c->record || !c->rec_sph_cnt || !c->have_forces) return fail(c, GSPH_ERR_STATE, "no recorded force pass");
+  cudaSetDevice(c->device);
+  const int n = c->n;
+  std::vector<unsigned long long> dc(n), dh(n);
+  std::vector<int> idv(n);
+  GSPH_CUDA(cudaMemcpy(dc.data(), c->rec_dir_cnt, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(dh.data(), c->rec_dir_hash, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(idv.data(), c->id, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  for (int s = 0; s < n; s++) { counts[idv[s]] = (int64_t) dc[s]; hashes[idv[s]] = dh[s]; }
+  return GSPH_OK;
+}
+
+int32_t gsph_get_cell_summary(gsph_ctx* c, int32_t* leaf_cells, int64_t* counts, uint64_t* hashes) {
+  if (!c || !leaf_cells || !counts || !hashes) return GSPH_ERR_INVALID;
+  if (!c->record || !c->rec_sph_cnt || !c->have_forces) return fail(c, GSPH_ERR_STATE, "no recorded force pass");
+  cudaSetDevice(c->device);
+  const int nl = c->nleaf;
+  std::vector<unsigned long long> cc(nl), ch(nl);
+  GSPH_CUDA(cudaMemcpy(leaf_cells, c->leaf_cell, sizeof(int) * nl, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(cc.data(), c->rec_cell_cnt, sizeof(unsigned long long) * nl, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(ch.data(), c->rec_cell_hash, sizeof(unsigned long long) * nl, cudaMemcpyDeviceToHost));
+  for (int q = 0; q < nl; q++) { counts[q] = (int64_t) cc[q]; hashes[q] = ch[q]; }
+  return GSPH_OK;
+}
+
+int32_t gsph_get_tree(gsph_ctx* c, int32_t* cell_n, int32_t* cell_first, int32_t* order, double* cell_data) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "tree not built");
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  const int nc = c->ncell;
+  if (cell_n) GSPH_CUDA(cudaMemcpy(cell_n, c->cell_n, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+  if (cell_first) GSPH_CUDA(cudaMemcpy(cell_first, c->cell_first, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+  if (order) GSPH_CUDA(cudaMemcpy(order, c->id, sizeof(int) * c->n, cudaMemcpyDeviceToHost));
+  if (cell_data) {
+    std::vector<CellGeom> g(nc);
+    std::vector<CellBox> b(nc), hb(nc);
+    std::vector<CellMoment> mo(nc);
+    std::vector<int> cn(nc), cf(nc);
+    std::vector<unsigned char> lv(nc);
+    GSPH_CUDA(cudaMemcpy(g.data(), c->geom, sizeof(CellGeom) * nc, cudaMemcpyDeviceToHost));
+    GSPH_CUDA(cudaMemcpy(b.data(), c->bb, sizeof(CellBox) * nc, cudaMemcpyDeviceToHost));
+    GSPH_CUDA(cudaMemcpy(hb.data(), c->hbox, sizeof(CellBox) * nc, cudaMemcpyDeviceToHost));
+    GSPH_CUDA(cudaMemcpy(mo.data(), c->mom, sizeof(CellMoment) * nc, cudaMemcpyDeviceToHost));
+    GSPH_CUDA(cudaMemcpy(cn.data(), c->cell_n, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    GSPH_CUDA(cudaMemcpy(cf.data(), c->cell_first, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    GSPH_CUDA(cudaMemcpy(lv.data(), c->cell_level, nc, cudaMemcpyDeviceToHost));
+    for (int q = 0; q < nc; q++) {
+      double* r = cell_data + (size_t) q * 31;
+      r[0] = cn[q]; r[1] = lv[q]; r[2] = mo[q].m; r[3] = g[q].rmax; r[4] = g[q].hmax; r[5] = g[q].cdistsqd;
+      for (int k = 0; k < 3; k++) {
+        r[6 + k] = b[q].bbmin[k]; r[9 + k] = b[q].bbmax[k]; r[12 + k] = hb[q].bbmin[k]; r[15 + k] = hb[q].bbmax[k];
+        r[18 + k] = g[q].rcell[k]; r[21 + k] = mo[q].r[k];
+      }
+      for (int k = 0; k < 5; k++) r[24 + k] = mo[q].q[k];
+      r[29] = cf[q]; r[30] = 0;
+    }
+  }
+  return GSPH_OK;
+}
+
+}  // extern "C"

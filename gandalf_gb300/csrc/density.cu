@@ -1,0 +1,246 @@
+// Grad-h density and smoothing-length solve, one warp per leaf cell.
+//
+// Reference: GradhSphTree::UpdateAllSphProperties (src/GradhSph/GradhSphTree.cpp:82-271)
+// drives, per active leaf cell, the gather walk Tree::ComputeGatherNeighbourList
+// (src/Tree/Tree.cpp:290-381) and GradhSph::ComputeH (src/GradhSph/GradhSph.cpp:141-326).
+//
+// Mapping: lane = LPG * g + s.  Group g (LPG lanes) owns particle g of the leaf; the LPG
+// lanes of a group split the candidate particles and reduce their sums with xor
+// shuffles, so every lane of a group holds the same totals and runs the reference's
+// scalar iteration logic in lock step.  The gather list (leaf cells overlapping the
+// gather box, tagged with a periodic-image code) is staged in shared memory; if it does
+// not fit, every iteration re-walks the tree and consumes the list in chunks instead.
+//
+// The reference's retry protocol is kept: when any particle's h exceeds the cell's
+// hmax (times 1.05 per attempt) the whole cell restarts from the input h with a 5 %
+// larger hmax (GradhSphTree.cpp:154-240).
+#include "gsph_state.cuh"
+#include "gsph_walk.cuh"
+#include "kernels.cuh"
+
+namespace gsph {
+
+namespace {
+
+constexpr int kDensWarps = 4;          // warps per block
+constexpr int kDensStack = 1024;       // walk stack entries per warp
+constexpr int kDensList = 1024;        // gather-list entries per warp
+constexpr int kMaxAttempts = 96;       // 1.05^96 ~ 108x growth of hmax
+constexpr int kNodeBits = 25;          // depth-first ids < 2^25 (ltot <= 23)
+constexpr int kNoShift = 13;           // periodic image code for (0,0,0)
+
+__device__ __forceinline__ double shift_of(int code, int k, const SphParams& prm) {
+  const int d = (k == 0 ? code % 3 : (k == 1 ? (code / 3) % 3 : code / 9)) - 1;
+  return d == 0 ? 0.0 : (d > 0 ? prm.boxsize[k] : -prm.boxsize[k]);
+}
+
+template <int LPG>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int o = 1; o < LPG; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(kDensWarps * 32)
+k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
+  __shared__ int s_stack[kDensWarps][kDensStack];
+  __shared__ int s_list[kDensWarps][kDensList];
+  const int wib = threadIdx.x >> 5;
+  const int leaf = blockIdx.x * kDensWarps + wib;
+  if (leaf >= t.nleaf) return;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / LPG, sl = lane % LPG;
+  const int c = t.leaf_cell[leaf];
+  const int first = t.cell_first[c], ncell = t.cell_n[c];
+  const bool mine = g < ncell;
+  const int slot = first + (mine ? g : 0);
+  const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
+  const double h_start = p.h[slot];
+  const CellBox bb = t.bb[c];
+  double hmax = t.geom[c].hmax;
+  int* stack = s_stack[wib];
+  int* list = s_list[wib];
+  unsigned long long pairs = 0;
+
+  // final per-particle results
+  double h_out = h_start, rho_out = 0.0, om_out = 0.0, zeta_out = 0.0;
+  bool fail = false, solved = false;
+
+  for (int attempt = 0; attempt < kMaxAttempts; attempt++) {
+    hmax = __dmul_rn(1.05, hmax);
+    const double hr = __dmul_rn(kKernRange, hmax);
+    double gmin[3], gmax[3];
+    for (int k = 0; k < 3; k++) { gmin[k] = __dsub_rn(bb.bbmin[k], hr); gmax[k] = __dadd_rn(bb.bbmax[k], hr); }
+    // periodic image codes needed by this gather box (ghost semantics)
+    int nsh[3] = {1, 1, 1}, sh[3][3];
+    for (int k = 0; k < 3; k++) {
+      sh[k][0] = 1;
+      if (prm.periodic) {
+        if (gmax[k] > prm.boxmax[k]) sh[k][nsh[k]++] = 2;   // images r + L of lhs particles
+        if (gmin[k] < prm.boxmin[k]) sh[k][nsh[k]++] = 0;   // images r - L of rhs particles
+      }
+    }
+
+    // ---- gather walk into the cached list (or detect that it does not fit) ----------
+    WarpLists L{list, list, list, 0, 0, 0, kDensList};
+    bool overflow = false, stack_ok = true;
+    auto walk_all = [&](auto&& flush) {
+      for (int a0 = 0; a0 < nsh[0]; a0++)
+        for (int a1 = 0; a1 < nsh[1]; a1++)
+          for (int a2 = 0; a2 < nsh[2]; a2++) {
+            const int code = sh[0][a0] + 3 * sh[1][a1] + 9 * sh[2][a2];
+            double bmin[3], bmax[3];
+            for (int k = 0; k < 3; k++) {
+              const double s = shift_of(code, k, prm);
+              bmin[k] = gmin[k] - s;
+              bmax[k] = gmax[k] - s;
+            }
+            auto decide = [&](int node, int level) -> int {
+              const CellBox ob = t.bb[node];
+              if (t.cell_n[node] == 0) return kSkip;
+              if (!box_overlap(bmin, bmax, ob.bbmin, ob.bbmax)) return kSkip;
+              return level == t.ltot ? kEmitA : kOpen;
+            };
+            auto tag = [&](int node, int) { return node | (code << kNodeBits); };
+            stack_ok = stack_ok && warp_walk(0, t.ltot, t.cell_level, stack, kDensStack, L, decide, tag, flush);
+          }
+    };
+    walk_all([&]() { overflow = true; });
+    const int ncached = L.na;
+
+    // ---- h-rho iteration, reference semantics (GradhSph::ComputeH) -------------------
+    double hi = h_start, h_lower = 0.0, h_upper = hmax;
+    double rho = 0.0, om = 0.0, zeta = 0.0;
+    int iteration = 0;
+    bool done = !mine, abort_cell = false;
+    while (__any_sync(kFull, !done)) {
+      iteration++;
+      const double invh = 1.0 / hi;
+      const double invhsqd = invh * invh;
+      double srho = 0.0, som = 0.0, sze = 0.0;
+      auto consume = [&](int count) {
+        if (done) return;
+        for (int e = 0; e < count; e++) {
+          const int tagv = list[e];
+          const int node = tagv & ((1 << kNodeBits) - 1);
+          const int code = tagv >> kNodeBits;
+          const int f = t.cell_first[node], nn = t.cell_n[node];
+          const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+          for (int q = sl; q < nn; q += LPG) {
+            const int j = f + q;
+            double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+            if (code != kNoShift) {
+              const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+              bool ok = true;
+              if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
+              if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
+              if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
+              if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
+              if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
+              if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
+              if (!ok) continue;
+              xj = __dadd_rn(xj, sx); yj = __dadd_rn(yj, sy); zj = __dadd_rn(zj, sz);
+            }
+            const double dx = xj - xi, dy = yj - yi, dz = zj - zi;
+            const double ssqd = invhsqd * dot3_rn(dx, dy, dz);
+            if (ssqd < kKernRangeSqd) {
+              const double s = sqrt(ssqd);
+              const double mj = p.m[j];
+              srho = fma(mj, m4_w0(s), srho);
+              som = fma(mj * invh, m4_womega(s), som);
+              sze = fma(mj, m4_wzeta(s), sze);
+              pairs++;
+            }
+          }
+        }
+      };
+      if (!overflow) {
+        consume(ncached);
+      } else {
+        WarpLists L2{list, list, list, 0, 0, 0, kDensList};
+        L = L2;
+        walk_all([&]() { consume(L.na); });
+        consume(L.na);
+      }
+      srho = group_sum<LPG>(srho);
+      som = group_sum<LPG>(som);
+      sze = group_sum<LPG>(sze);
+      if (!done) {
+        const double hfac3 = invh * invh * invh;
+        rho = srho * hfac3;
+        om = som * hfac3;
+        zeta = sze * invhsqd;
+        const double hrho = prm.h_fac * pow(mi / rho, 1.0 / 3.0);
+        if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
+          done = true;
+        } else {
+          if (iteration < 30) hi = hrho;
+          else if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
+          else if (iteration < 150) {
+            if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
+            hi = 0.5 * (h_lower + h_upper);
+          } else {
+            fail = true;
+            done = true;
+          }
+          if (!done) {
+            if (hi > hmax) { abort_cell = true; done = true; }
+            else if (!(hi > h_lower && hi < h_upper)) done = true;
+          }
+        }
+      }
+    }
+    if (__any_sync(kFull, abort_cell)) continue;   // retry the whole cell with larger hmax
+    if (mine) {
+      const double hrho = prm.h_fac * pow(mi / rho, 1.0 / 3.0);
+      h_out = fmax(hrho, h_lower);
+      rho_out = rho; om_out = om; zeta_out = zeta;
+    }
+    if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
+    if (__any_sync(kFull, fail) && lane == 0) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
+    solved = true;
+    break;
+  }
+  if (!solved && lane == 0) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
+  {
+    unsigned long long tot = pairs;
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
+    if (lane == 0) atomicAdd(cnt.density_pairs, tot);
+  }
+  if (mine && sl == 0) {
+    const double hfin = h_out;
+    const double invh = 1.0 / hfin;
+    p.h[slot] = hfin;
+    p.rho[slot] = rho_out;
+    p.hfactor[slot] = invh * invh * invh * invh;
+    p.hrangesqd[slot] = __dmul_rn(__dmul_rn(kKernRangeSqd, hfin), hfin);
+    p.div_v[slot] = 0.0;
+    const double drho = -(1.0 / 3.0) * hfin / rho_out;   // h_rho_deriv, src/Headers/Sph.h:264-268
+    const double io = 1.0 / (1.0 - drho * om_out);
+    p.invomega[slot] = io;
+    p.zeta[slot] = drho * zeta_out * io;
+    double u = p.u[slot];
+    const double gm1 = prm.gamma_eos - 1.0;
+    if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
+    p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
+    p.pressure[slot] = gm1 * rho_out * u;
+  }
+}
+
+}  // namespace
+
+void launch_density(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
+                    int lanes_per_particle, cudaStream_t st) {
+  const int blocks = (t.nleaf + kDensWarps - 1) / kDensWarps;
+  switch (lanes_per_particle) {
+    case 32: k_density_fp64<32><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
+    case 16: k_density_fp64<16><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
+    case 8: k_density_fp64<8><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
+    case 4: k_density_fp64<4><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
+    case 2: k_density_fp64<2><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
+    default: k_density_fp64<1><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
+  }
+}
+
+}  // namespace gsph

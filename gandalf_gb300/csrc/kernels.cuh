@@ -1,0 +1,40 @@
+// Launchers of the per-leaf-cell kernels (density.cu, forces.cu).
+#pragma once
+#include "gsph_state.cuh"
+
+namespace gsph {
+
+// Device-side counters and status word, zeroed by the host before a step.
+struct DeviceCounters {
+  unsigned* status;                    // StatusBits, or-ed by kernels
+  unsigned long long* density_pairs;   // pair evaluations inside the kernel support
+  unsigned long long* hydro_pairs;     // SPH pairs (hydro or hydro + softened gravity)
+  unsigned long long* direct_pairs;    // Newtonian particle-particle terms
+  unsigned long long* cell_pairs;      // particle-cell multipole terms
+  unsigned long long* exact_checks;    // mixed form: membership tests resolved in fp64
+  // optional recording of interaction lists (verification only; record == 0 skips it)
+  int record;
+  int rec_max;                         // SPH ids kept per particle
+  int* rec_sph_cnt;                    // per slot
+  int* rec_sph_ids;                    // slot * rec_max
+  unsigned long long* rec_dir_cnt;     // per slot
+  unsigned long long* rec_dir_hash;    // per slot: sum of mix64(input id)
+  unsigned long long* rec_cell_cnt;    // per leaf index
+  unsigned long long* rec_cell_hash;   // per leaf index: sum of mix64(cell id)
+};
+
+__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+void launch_density(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
+                    int lanes_per_particle, cudaStream_t st);
+void launch_hydro_forces(const Tree& t, const Particles& p, const SphParams& prm,
+                         const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st);
+void launch_all_forces(const Tree& t, const Particles& p, const SphParams& prm,
+                       const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st);
+
+}  // namespace gsph

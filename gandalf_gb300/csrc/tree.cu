@@ -1,0 +1,537 @@
+// KD-tree build, stock and hmax update on the GPU, reproducing the reference tree exactly.
+//
+// Reference algorithm (src/Tree/KDTree.cpp):
+//   * ltot = smallest l with Nleafmax * 2^l >= N; all leaves on level ltot (:321-352)
+//   * root box = particle extent +- kernrange*h (:269-280)
+//   * a cell splits along the longest side of its inherited (loose) box (:492-498), at the
+//     (N/2)-th smallest coordinate: child 1 receives the N/2 smallest (:505-533)
+//   * cells are stocked bottom-up; cdistsqd = max(rmax^2, hmax^2) / theta^2 (:807-1083)
+//
+// GB300 design: the recursion becomes ltot level-synchronous passes over position lists.
+// Each particle's index is presorted once per axis (bitonic sort on (coordinate, index)),
+// so every segment's median along its split axis sits at position first + n/2 of that
+// axis list.  A pass then marks each particle's side and stable-partitions all three lists
+// with one global scan, which keeps each child's lists sorted.  Particles are never moved
+// until the final gather into leaf order.  Stocking is one launch: each leaf thread stocks
+// its leaf and climbs while it is the second child to arrive at a parent.
+#include "gsph_state.cuh"
+#include "tree.cuh"
+
+namespace gsph {
+
+namespace {
+
+constexpr int kSortBlock = 2048;       // elements per shared-memory bitonic block
+constexpr int kScanBlock = 2048;       // positions per partition block (1024 threads x 2)
+
+__device__ __forceinline__ bool key_gt(unsigned long long ka, int ia, unsigned long long kb, int ib) {
+  return ka > kb || (ka == kb && ia > ib);
+}
+
+__global__ void k_root_box_init(unsigned long long* rootkey) {
+  const int t = threadIdx.x;
+  if (t < 3) rootkey[t] = ~0ull;       // minima
+  else if (t < 6) rootkey[t] = 0ull;   // maxima
+}
+
+// Root box: min(r - 2h), max(r + 2h) per axis (order-independent, exact).
+__global__ void k_root_box(const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ z, const double* __restrict__ h, int n,
+                           unsigned long long* rootkey) {
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double hh = __dmul_rn(kKernRange, h[i]);
+    const double c[3] = {x[i], y[i], z[i]};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      lo[k] = min(lo[k], dkey(__dsub_rn(c[k], hh)));
+      hi[k] = max(hi[k], dkey(__dadd_rn(c[k], hh)));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = min(lo[k], __shfl_xor_sync(kFull, lo[k], o));
+      hi[k] = max(hi[k], __shfl_xor_sync(kFull, hi[k], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int k = 0; k < 3; k++) {
+      atomicMin(&rootkey[k], lo[k]);
+      atomicMax(&rootkey[3 + k], hi[k]);
+    }
+  }
+}
+
+__global__ void k_root_box_store(const unsigned long long* rootkey, double* ibox) {
+  const int t = threadIdx.x;
+  if (t < 6) ibox[t] = dkey_inv(rootkey[t]);   // ibox[0..2] = min, [3..5] = max
+}
+
+__global__ void k_sort_init(const double* __restrict__ x, const double* __restrict__ y,
+                            const double* __restrict__ z, int n, int P, SortArrays s) {
+  const int a = blockIdx.y;
+  const double* c = a == 0 ? x : (a == 1 ? y : z);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+    s.key[a][i] = i < n ? dkey(c[i]) : ~0ull;
+    s.idx[a][i] = i;
+  }
+}
+
+// Bitonic stages with strides <= kSortBlock/2 inside shared memory.
+__global__ void __launch_bounds__(kSortBlock / 2) k_bitonic_smem(SortArrays s, int kmin, int kmax, int jmax) {
+  __shared__ unsigned long long sk[kSortBlock];
+  __shared__ int si[kSortBlock];
+  const int a = blockIdx.y;
+  const int base = blockIdx.x * kSortBlock;
+  unsigned long long* key = s.key[a];
+  int* idx = s.idx[a];
+  for (int t = threadIdx.x; t < kSortBlock; t += blockDim.x) { sk[t] = key[base + t]; si[t] = idx[base + t]; }
+  for (int k = kmin; k <= kmax; k <<= 1) {
+    for (int j = min(k >> 1, jmax); j > 0; j >>= 1) {
+      __syncthreads();
+      const int t = threadIdx.x;
+      const int i = 2 * j * (t / j) + (t % j);
+      const int l = i + j;
+      const bool asc = ((base + i) & k) == 0;
+      const unsigned long long ki = sk[i], kl = sk[l];
+      const int ii = si[i], il = si[l];
+      if (key_gt(ki, ii, kl, il) == asc) { sk[i] = kl; sk[l] = ki; si[i] = il; si[l] = ii; }
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kSortBlock; t += blockDim.x) { key[base + t] = sk[t]; idx[base + t] = si[t]; }
+}
+
+__global__ void k_bitonic_global(SortArrays s, int P, int k, int j) {
+  const int a = blockIdx.y;
+  unsigned long long* key = s.key[a];
+  int* idx = s.idx[a];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P / 2; t += gridDim.x * blockDim.x) {
+    const int i = 2 * j * (t / j) + (t % j);
+    const int l = i + j;
+    const bool asc = (i & k) == 0;
+    const unsigned long long ki = key[i], kl = key[l];
+    const int ii = idx[i], il = idx[l];
+    if (key_gt(ki, ii, kl, il) == asc) { key[i] = kl; key[l] = ki; idx[i] = il; idx[l] = ii; }
+  }
+}
+
+// Segment containing position j on level l (recursive halving of [0, n)).
+__device__ __forceinline__ int seg_of(int j, int n, int l, int& first, int& cnt) {
+  int s = 0, f = 0, c = n;
+  for (int lev = 0; lev < l; lev++) {
+    const int half = c >> 1;
+    if (j < f + half) { s = 2 * s; c = half; }
+    else { s = 2 * s + 1; f += half; c -= half; }
+  }
+  first = f; cnt = c;
+  return s;
+}
+
+// One thread per segment of level l: split axis, median coordinate, child boxes.
+__global__ void k_split_prepare(int l, BuildLists cur, const double* __restrict__ x,
+                                const double* __restrict__ y, const double* __restrict__ z,
+                                const int* __restrict__ heap_first, const int* __restrict__ heap_n,
+                                double* ibox, unsigned char* seg_axis) {
+  const int nseg = 1 << l;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const int hidx = nseg - 1 + s;
+  const int first = heap_first[hidx], cnt = heap_n[hidx];
+  double bmin[3], bmax[3];
+  for (int k = 0; k < 3; k++) { bmin[k] = ibox[6 * hidx + k]; bmax[k] = ibox[6 * hidx + 3 + k]; }
+  int kd = 0;
+  double rkmax = 0.0;
+  for (int k = 0; k < 3; k++) {
+    const double ext = __dsub_rn(bmax[k], bmin[k]);
+    if (ext > rkmax) { rkmax = ext; kd = k; }
+  }
+  seg_axis[s] = (unsigned char) kd;
+  double rdiv = 0.0;
+  if (cnt > 0) {
+    const int id = cur.l[kd][first + cnt / 2];
+    rdiv = kd == 0 ? x[id] : (kd == 1 ? y[id] : z[id]);
+  }
+  const int c1 = 2 * hidx + 1, c2 = 2 * hidx + 2;
+  for (int k = 0; k < 3; k++) {
+    ibox[6 * c1 + k] = bmin[k]; ibox[6 * c1 + 3 + k] = bmax[k];
+    ibox[6 * c2 + k] = bmin[k]; ibox[6 * c2 + 3 + k] = bmax[k];
+  }
+  ibox[6 * c1 + 3 + kd] = rdiv;
+  ibox[6 * c2 + kd] = rdiv;
+}
+
+__global__ void k_mark_side(int l, int n, BuildLists cur, const unsigned char* __restrict__ seg_axis,
+                            unsigned char* side) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    int first, cnt;
+    const int s = seg_of(j, n, l, first, cnt);
+    const int kd = seg_axis[s];
+    side[cur.l[kd][j]] = (unsigned char) (j - first >= (cnt >> 1));
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_part_count(int n, BuildLists cur, const unsigned char* __restrict__ side,
+                                                     int* blocksum, int nb) {
+  const int a = blockIdx.y;
+  const int base = blockIdx.x * kScanBlock;
+  int c = 0;
+  for (int t = threadIdx.x; t < kScanBlock; t += blockDim.x) {
+    const int j = base + t;
+    if (j < n) c += side[cur.l[a][j]];
+  }
+  c = __reduce_add_sync(kFull, c);
+  __shared__ int ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0;
+    v = __reduce_add_sync(kFull, v);
+    if (threadIdx.x == 0) blocksum[a * nb + blockIdx.x] = v;
+  }
+}
+
+// Block-wide exclusive scan of one int per thread (1024 threads).
+__device__ __forceinline__ int block_exscan(int v, int* ws, int& total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) ws[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < (int) (blockDim.x >> 5) ? ws[lane] : 0;
+    int si = s;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, si, o);
+      if (lane >= o) si += y;
+    }
+    ws[lane] = si - s;
+    if (lane == 31) ws[32] = si;
+  }
+  __syncthreads();
+  total = ws[32];
+  const int r = ws[w] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(1024) k_part_scan(int* blocksum, int nb) {
+  __shared__ int ws[33];
+  const int a = blockIdx.y;
+  int* b = blocksum + a * nb;
+  int carry = 0;
+  for (int base = 0; base < nb; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int v = i < nb ? b[i] : 0;
+    int total;
+    const int ex = block_exscan(v, ws, total);
+    if (i < nb) b[i] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_part_scatter(int l, int n, BuildLists cur, BuildLists nxt,
+                                                       const unsigned char* __restrict__ side,
+                                                       const int* __restrict__ blocksum, int nb,
+                                                       const int* __restrict__ heap_ones_before) {
+  __shared__ int ws[33];
+  const int a = blockIdx.y;
+  const int base = blockIdx.x * kScanBlock;
+  const int j0 = base + 2 * threadIdx.x, j1 = j0 + 1;
+  const int id0 = j0 < n ? cur.l[a][j0] : -1;
+  const int id1 = j1 < n ? cur.l[a][j1] : -1;
+  const int f0 = id0 >= 0 ? side[id0] : 0;
+  const int f1 = id1 >= 0 ? side[id1] : 0;
+  int total;
+  const int ex = block_exscan(f0 + f1, ws, total) + blocksum[a * nb + blockIdx.x];
+  const int nseg = 1 << l;
+  int jj[2] = {j0, j1}, ids[2] = {id0, id1}, ff[2] = {f0, f1}, ee[2] = {ex, ex + f0};
+  for (int q = 0; q < 2; q++) {
+    if (ids[q] < 0) continue;
+    int first, cnt;
+    const int s = seg_of(jj[q], n, l, first, cnt);
+    const int ob = heap_ones_before[nseg - 1 + s];
+    const int ones = ee[q] - ob;                  // ones before j inside the segment
+    const int pos = ff[q] ? first + (cnt >> 1) + ones : first + (jj[q] - first) - ones;
+    nxt.l[a][pos] = ids[q];
+  }
+}
+
+__global__ void k_gather_leaf_order(int n, const int* __restrict__ perm, InputArrays in, Particles p,
+                                    int* id_out) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const int i = perm[s];
+    id_out[s] = i;
+    p.x[s] = in.x[i]; p.y[s] = in.y[i]; p.z[s] = in.z[i];
+    p.vx[s] = in.vx[i]; p.vy[s] = in.vy[i]; p.vz[s] = in.vz[i];
+    p.m[s] = in.m[i]; p.u[s] = in.u[i]; p.h[s] = in.h[i]; p.h0[s] = in.h[i];
+  }
+}
+
+// ---- stocking (KDTree::StockCellProperties) ------------------------------------------
+__device__ void finish_geometry(int n, const double* bmin, const double* bmax, double hmax,
+                                double theta2, CellGeom& g) {
+  if (n > 0) {
+    double dr[3];
+    for (int k = 0; k < 3; k++) {
+      g.rcell[k] = __dmul_rn(0.5, __dadd_rn(bmin[k], bmax[k]));
+      dr[k] = __dmul_rn(0.5, __dsub_rn(bmax[k], bmin[k]));
+    }
+    const double dd = dot3_rn(dr[0], dr[1], dr[2]);
+    g.cdistsqd = __ddiv_rn(fmax(dd, __dmul_rn(hmax, hmax)), theta2);
+    g.rmax = __dsqrt_rn(dd);
+  } else {
+    for (int k = 0; k < 3; k++) g.rcell[k] = 0.0;
+    g.cdistsqd = kBig;
+    g.rmax = 0.0;
+  }
+  g.hmax = hmax;
+}
+
+__device__ void stock_leaf(const Tree& t, const Particles& p, int c, double theta2) {
+  const int first = t.cell_first[c], n = t.cell_n[c];
+  double m = 0.0, r[3] = {0.0, 0.0, 0.0}, hmax = 0.0;
+  double bmin[3] = {kBig, kBig, kBig}, bmax[3] = {-kBig, -kBig, -kBig};
+  double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+  for (int j = 0; j < n; j++) {
+    const int s = first + j;
+    const double xs[3] = {p.x[s], p.y[s], p.z[s]};
+    const double hh = p.h[s], mm = p.m[s];
+    hmax = fmax(hmax, hh);
+    m += mm;
+    const double h2 = __dmul_rn(kKernRange, hh);
+    for (int k = 0; k < 3; k++) {
+      r[k] = fma(mm, xs[k], r[k]);
+      bmin[k] = fmin(bmin[k], xs[k]);
+      bmax[k] = fmax(bmax[k], xs[k]);
+      hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
+      hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
+    }
+  }
+  if (m > 0.0) for (int k = 0; k < 3; k++) r[k] /= m;
+  CellGeom g;
+  finish_geometry(n, bmin, bmax, hmax, theta2, g);
+  double q[5] = {0, 0, 0, 0, 0};
+  for (int j = 0; j < n; j++) {
+    const int s = first + j;
+    const double mm = p.m[s];
+    const double dx = p.x[s] - r[0], dy = p.y[s] - r[1], dz = p.z[s] - r[2];
+    const double drsqd = dx * dx + dy * dy + dz * dz;
+    q[0] += mm * (3.0 * dx * dx - drsqd);
+    q[1] += mm * 3.0 * dx * dy;
+    q[2] += mm * (3.0 * dy * dy - drsqd);
+    q[3] += mm * 3.0 * dz * dx;
+    q[4] += mm * 3.0 * dz * dy;
+  }
+  t.geom[c] = g;
+  CellBox b, hb;
+  for (int k = 0; k < 3; k++) { b.bbmin[k] = bmin[k]; b.bbmax[k] = bmax[k]; hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
+  t.bb[c] = b;
+  t.hbox[c] = hb;
+  CellMoment mo;
+  for (int k = 0; k < 3; k++) mo.r[k] = r[k];
+  mo.m = m;
+  for (int k = 0; k < 5; k++) mo.q[k] = q[k];
+  mo.pad = 0.0;
+  t.mom[c] = mo;
+}
+
+__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+
+__device__ void stock_parent(const Tree& t, int c, int level, double theta2) {
+  const int c1 = c + 1, c2 = c2_of(c, level, t.ltot);
+  const int n1 = t.cell_n[c1], n2 = t.cell_n[c2];
+  double bmin[3] = {kBig, kBig, kBig}, bmax[3] = {-kBig, -kBig, -kBig};
+  double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+  double hmax = 0.0;
+  const int ch[2] = {c1, c2};
+  const int chn[2] = {n1, n2};
+  double cm[2], cr[2][3], cq[2][5];
+  for (int q = 0; q < 2; q++) {
+    const int cc = ch[q];
+    const double* bbp = reinterpret_cast<const double*>(&t.bb[cc]);
+    const double* hbp = reinterpret_cast<const double*>(&t.hbox[cc]);
+    const double* gp = reinterpret_cast<const double*>(&t.geom[cc]);
+    const double* mp = reinterpret_cast<const double*>(&t.mom[cc]);
+    if (chn[q] > 0) {
+      for (int k = 0; k < 3; k++) {
+        bmin[k] = fmin(ldcg(bbp + k), bmin[k]);
+        bmax[k] = fmax(ldcg(bbp + 3 + k), bmax[k]);
+        hbmin[k] = fmin(ldcg(hbp + k), hbmin[k]);
+        hbmax[k] = fmax(ldcg(hbp + 3 + k), hbmax[k]);
+      }
+      hmax = fmax(hmax, ldcg(gp + 4));
+    }
+    for (int k = 0; k < 3; k++) cr[q][k] = ldcg(mp + k);
+    cm[q] = ldcg(mp + 3);
+    for (int k = 0; k < 5; k++) cq[q][k] = ldcg(mp + 4 + k);
+  }
+  const int n = n1 + n2;
+  const double m = cm[0] + cm[1];
+  double r[3] = {0.0, 0.0, 0.0};
+  if (m > 0.0) for (int k = 0; k < 3; k++) r[k] = (cm[0] * cr[0][k] + cm[1] * cr[1][k]) / m;
+  CellGeom g;
+  finish_geometry(n, bmin, bmax, hmax, theta2, g);
+  double q[5] = {0, 0, 0, 0, 0};
+  for (int s = 0; s < 2; s++) {
+    if (!(cm[s] > 0.0)) continue;
+    const double dx = cr[s][0] - r[0], dy = cr[s][1] - r[1], dz = cr[s][2] - r[2];
+    const double drsqd = dx * dx + dy * dy + dz * dz;
+    for (int k = 0; k < 5; k++) q[k] += cq[s][k];
+    q[0] += cm[s] * (3.0 * dx * dx - drsqd);
+    q[1] += cm[s] * 3.0 * dx * dy;
+    q[2] += cm[s] * (3.0 * dy * dy - drsqd);
+    q[3] += cm[s] * 3.0 * dz * dx;
+    q[4] += cm[s] * 3.0 * dz * dy;
+  }
+  t.geom[c] = g;
+  CellBox b, hb;
+  for (int k = 0; k < 3; k++) { b.bbmin[k] = bmin[k]; b.bbmax[k] = bmax[k]; hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
+  t.bb[c] = b;
+  t.hbox[c] = hb;
+  CellMoment mo;
+  for (int k = 0; k < 3; k++) mo.r[k] = r[k];
+  mo.m = m;
+  for (int k = 0; k < 5; k++) mo.q[k] = q[k];
+  mo.pad = 0.0;
+  t.mom[c] = mo;
+}
+
+// Bottom-up climb: the second child to finish stocks the parent.
+__global__ void k_stock(Tree t, Particles p, double theta2) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= t.nleaf) return;
+  int c = t.leaf_cell[s];
+  stock_leaf(t, p, c, theta2);
+  int level = t.ltot;
+  while (level > 0) {
+    const int parent = t.cell_parent[c];
+    __threadfence();
+    const unsigned old = atomicAdd(&t.climb[parent], 1u);
+    if (old == 0u) return;
+    __threadfence();
+    level--;
+    c = parent;
+    stock_parent(t, c, level, theta2);
+  }
+}
+
+// KDTree::UpdateHmaxValues: hmax and hbox from the solved h; cdistsqd keeps its value.
+__global__ void k_update_hmax(Tree t, Particles p) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= t.nleaf) return;
+  int c = t.leaf_cell[s];
+  {
+    const int first = t.cell_first[c], n = t.cell_n[c];
+    double hmax = 0.0;
+    double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+    for (int j = 0; j < n; j++) {
+      const int q = first + j;
+      const double xs[3] = {p.x[q], p.y[q], p.z[q]};
+      const double hh = p.h[q];
+      hmax = fmax(hmax, hh);
+      const double h2 = __dmul_rn(kKernRange, hh);
+      for (int k = 0; k < 3; k++) {
+        hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
+        hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
+      }
+    }
+    t.geom[c].hmax = hmax;
+    CellBox hb;
+    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
+    t.hbox[c] = hb;
+  }
+  int level = t.ltot;
+  while (level > 0) {
+    const int parent = t.cell_parent[c];
+    __threadfence();
+    const unsigned old = atomicAdd(&t.climb[parent], 1u);
+    if (old == 0u) return;
+    __threadfence();
+    level--;
+    c = parent;
+    const int c1 = c + 1, c2 = c2_of(c, level, t.ltot);
+    double hmax = 0.0;
+    double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+    const int ch[2] = {c1, c2};
+    for (int q = 0; q < 2; q++) {
+      if (t.cell_n[ch[q]] <= 0) continue;
+      const double* hbp = reinterpret_cast<const double*>(&t.hbox[ch[q]]);
+      hmax = fmax(hmax, ldcg(&t.geom[ch[q]].hmax));
+      for (int k = 0; k < 3; k++) {
+        hbmin[k] = fmin(ldcg(hbp + k), hbmin[k]);
+        hbmax[k] = fmax(ldcg(hbp + 3 + k), hbmax[k]);
+      }
+    }
+    t.geom[c].hmax = hmax;
+    CellBox hb;
+    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
+    t.hbox[c] = hb;
+  }
+}
+
+int grid_for(int n, int block, int maxblocks = 152 * 16) {
+  int g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  return g < maxblocks ? g : maxblocks;
+}
+
+}  // namespace
+
+int sort_padded_size(int n) {
+  int P = kSortBlock;
+  while (P < n) P <<= 1;
+  return P;
+}
+
+int partition_blocks(int n) { return (n + kScanBlock - 1) / kScanBlock; }
+
+int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
+  int launches = 0;
+  const int n = a.n;
+  k_root_box_init<<<1, 32, 0, st>>>(a.rootkey);
+  k_root_box<<<grid_for(n, 256, 152 * 4), 256, 0, st>>>(a.in.x, a.in.y, a.in.z, a.in.h, n, a.rootkey);
+  k_root_box_store<<<1, 32, 0, st>>>(a.rootkey, a.ibox);
+  launches += 3;
+  const int P = a.P;
+  k_sort_init<<<dim3(grid_for(P, 256), 3), 256, 0, st>>>(a.in.x, a.in.y, a.in.z, n, P, a.sort);
+  k_bitonic_smem<<<dim3(P / kSortBlock, 3), kSortBlock / 2, 0, st>>>(a.sort, 2, kSortBlock, kSortBlock / 2);
+  launches += 2;
+  for (int k = 2 * kSortBlock; k <= P; k <<= 1) {
+    for (int j = k >> 1; j >= kSortBlock; j >>= 1) {
+      k_bitonic_global<<<dim3(grid_for(P / 2, 256, 1 << 20), 3), 256, 0, st>>>(a.sort, P, k, j);
+      launches++;
+    }
+    k_bitonic_smem<<<dim3(P / kSortBlock, 3), kSortBlock / 2, 0, st>>>(a.sort, k, k, kSortBlock / 2);
+    launches++;
+  }
+  BuildLists cur, nxt;
+  for (int q = 0; q < 3; q++) { cur.l[q] = a.sort.idx[q]; nxt.l[q] = a.lists_b[q]; }
+  const int nb = partition_blocks(n);
+  for (int l = 0; l < a.ltot; l++) {
+    const int nseg = 1 << l;
+    k_split_prepare<<<(nseg + 127) / 128, 128, 0, st>>>(l, cur, a.in.x, a.in.y, a.in.z, a.heap_first,
+                                                         a.heap_n, a.ibox, a.seg_axis);
+    k_mark_side<<<grid_for(n, 256), 256, 0, st>>>(l, n, cur, a.seg_axis, a.side);
+    k_part_count<<<dim3(nb, 3), 1024, 0, st>>>(n, cur, a.side, a.blocksum, nb);
+    k_part_scan<<<dim3(1, 3), 1024, 0, st>>>(a.blocksum, nb);
+    k_part_scatter<<<dim3(nb, 3), 1024, 0, st>>>(l, n, cur, nxt, a.side, a.blocksum, nb, a.heap_ones_before);
+    BuildLists tmp = cur; cur = nxt; nxt = tmp;
+    launches += 5;
+  }
+  k_gather_leaf_order<<<grid_for(n, 256), 256, 0, st>>>(n, cur.l[0], a.in, a.p, a.id_out);
+  cudaMemsetAsync(a.tree.climb, 0, sizeof(unsigned) * (size_t) a.tree.ncell, st);
+  k_stock<<<(a.tree.nleaf + 127) / 128, 128, 0, st>>>(a.tree, a.p, a.thetamaxsqd);
+  return launches + 2;
+}
+
+void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st) {
+  cudaMemsetAsync(t.climb, 0, sizeof(unsigned) * (size_t) t.ncell, st);
+  k_update_hmax<<<(t.nleaf + 127) / 128, 128, 0, st>>>(t, p);
+}
+
+}  // namespace gsph

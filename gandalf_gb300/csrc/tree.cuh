@@ -1,0 +1,44 @@
+// Host-side launchers of the tree kernels (tree.cu).
+#pragma once
+#include "gsph_state.cuh"
+
+namespace gsph {
+
+struct SortArrays {
+  unsigned long long* key[3];   // order-preserving coordinate keys, padded length P
+  int* idx[3];                  // particle indices, padded length P
+};
+
+struct BuildLists {
+  int* l[3];                    // per-axis position lists of particle indices
+};
+
+struct InputArrays {            // input order, fp64
+  const double *x, *y, *z, *vx, *vy, *vz, *m, *u, *h;
+};
+
+struct BuildArgs {
+  int n, ltot, P;
+  InputArrays in;
+  SortArrays sort;
+  int* lists_b[3];              // second buffer of the ping-pong position lists (length n)
+  unsigned char* side;          // per particle: 0 first child, 1 second child
+  unsigned char* seg_axis;      // per segment of the current level
+  int* blocksum;                // 3 * partition_blocks(n)
+  unsigned long long* rootkey;  // 6
+  double* ibox;                 // inherited boxes, heap-indexed, 6 per cell
+  const int* heap_first;        // heap-indexed segment tables (static per N)
+  const int* heap_n;
+  const int* heap_ones_before;
+  Particles p;                  // leaf-ordered destination
+  int* id_out;                  // input index of each slot
+  Tree tree;
+  double thetamaxsqd;
+};
+
+int sort_padded_size(int n);
+int partition_blocks(int n);
+int launch_build_tree(const BuildArgs& a, cudaStream_t st);   // returns kernels launched
+void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st);
+
+}  // namespace gsph

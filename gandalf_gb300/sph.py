@@ -1,0 +1,233 @@
+"""Host-side mirror of the reference's SPH neighbour-search interface on the GPU.
+
+``GradhSphTree`` stands in for ``GradhSphTree<3,GradhSphParticle>``
+(src/Headers/SphNeighbourSearch.h:173-227): the same calls in the same order —
+``BuildTree``, ``UpdateAllSphProperties``, ``UpdateAllSphHydroForces``,
+``UpdateAllSphForces`` — backed by the C ABI of libgsph_gb300.so.  Failures raise
+``GandalfError``, as the reference's ExceptionHandler does in Python mode
+(src/Common/Exception.cpp:49-60).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+EOS = {"energy_eqn": 0, "isothermal": 1}
+MULTIPOLE = {"monopole": 0, "quadrupole": 1}
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
+class GandalfError(RuntimeError):
+    """Raised for every failed call (the reference's GandalfError)."""
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_config(params: dict | None = None, **kw) -> _native.Config:
+    """Config from GANDALF-style parameters (unknown keys are ignored)."""
+    lib = _native.load()
+    cfg = _native.Config()
+    lib.gsph_config_defaults(ctypes.byref(cfg))
+    p = dict(params or {})
+    p.update(kw)
+    if "eos" in p and isinstance(p["eos"], str):
+        p["eos"] = EOS[p["eos"]]
+    if "gas_eos" in p:
+        p["eos"] = EOS[p["gas_eos"]] if isinstance(p["gas_eos"], str) else int(p["gas_eos"])
+    if "multipole" in p and isinstance(p["multipole"], str):
+        p["multipole"] = MULTIPOLE[p["multipole"]]
+    if "precision" in p and isinstance(p["precision"], str):
+        p["precision"] = PRECISION[p["precision"]]
+    if "Nleafmax" in p:
+        p["nleafmax"] = p["Nleafmax"]
+    for k in ("ndim", "nleafmax", "hydro_forces", "self_gravity", "eos", "multipole", "periodic", "precision"):
+        if k in p:
+            setattr(cfg, k, int(p[k]))
+    for k in ("h_fac", "h_converge", "alpha_visc", "beta_visc", "gamma_eos", "temp0", "mu_bar",
+              "thetamaxsqd"):
+        if k in p:
+            setattr(cfg, k, float(p[k]))
+    for k in range(3):
+        if "boxmin" in p:
+            cfg.boxmin[k] = float(p["boxmin"][k])
+        if "boxmax" in p:
+            cfg.boxmax[k] = float(p["boxmax"][k])
+    return cfg
+
+
+class GradhSphTree:
+    """One simulation's particle step on one GPU."""
+
+    def __init__(self, params: dict | None = None, device: int = 0, **kw):
+        self._lib = _native.load()
+        self.config = make_config(params, **kw)
+        self._ctx = self._lib.gsph_create(ctypes.byref(self.config), int(device))
+        if not self._ctx:
+            code = self._lib.gsph_create_error()
+            raise GandalfError(f"gsph_create failed: {_native.ERRORS.get(code, code)}")
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.gsph_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != _native.GSPH_OK:
+            msg = self._lib.gsph_last_error(self._ctx)
+            raise GandalfError(f"{what}: {_native.ERRORS.get(rc, rc)}: "
+                               f"{msg.decode() if msg else ''}")
+
+    # ---- import (Simulation::ImportArraySph) ------------------------------------------
+    def set_particles(self, ics: dict):
+        """Import x y z vx vy vz m u h from host numpy arrays or CUDA torch tensors."""
+        keys = ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")
+        first = ics["x"]
+        if hasattr(first, "is_cuda") and first.is_cuda:
+            arrs = [ics[k].contiguous().double() for k in keys]
+            ptrs = [ctypes.c_void_p(a.data_ptr()) for a in arrs]
+            self._keep = arrs
+            rc = self._lib.gsph_set_particles_device(self._ctx, len(arrs[0]), *ptrs)
+            self.n = len(arrs[0])
+        else:
+            arrs = [np.ascontiguousarray(ics[k], dtype=np.float64) for k in keys]
+            rc = self._lib.gsph_set_particles(self._ctx, len(arrs[0]), *[_dp(a) for a in arrs])
+            self.n = len(arrs[0])
+        self._check(rc, "set_particles")
+
+    def set_particles_aos(self, records: np.ndarray, offsets: dict):
+        """Import a structured array of particle records (byte offsets per field)."""
+        off = _native.FieldOffsets(**{k: int(offsets.get(k, -1)) for k, _ in _native.FieldOffsets._fields_})
+        rc = self._lib.gsph_set_particles_aos(self._ctx, records.ctypes.data, len(records),
+                                              records.dtype.itemsize, ctypes.byref(off))
+        self.n = len(records)
+        self._check(rc, "set_particles_aos")
+
+    def get_particles_aos(self, records: np.ndarray, offsets: dict):
+        off = _native.FieldOffsets(**{k: int(offsets.get(k, -1)) for k, _ in _native.FieldOffsets._fields_})
+        rc = self._lib.gsph_get_particles_aos(self._ctx, records.ctypes.data, len(records),
+                                              records.dtype.itemsize, ctypes.byref(off))
+        self._check(rc, "get_particles_aos")
+
+    # ---- the reference's virtual interface ----------------------------------------------
+    def BuildTree(self):
+        self._check(self._lib.gsph_build_tree(self._ctx), "BuildTree")
+
+    def UpdateAllSphProperties(self):
+        self._check(self._lib.gsph_update_all_sph_properties(self._ctx), "UpdateAllSphProperties")
+
+    def UpdateAllSphHydroForces(self):
+        self._check(self._lib.gsph_update_all_sph_hydro_forces(self._ctx), "UpdateAllSphHydroForces")
+
+    def UpdateAllSphForces(self):
+        self._check(self._lib.gsph_update_all_sph_forces(self._ctx), "UpdateAllSphForces")
+
+    def step(self):
+        """BuildTree + UpdateAllSphProperties + the configured force pass."""
+        self._check(self._lib.gsph_step(self._ctx), "step")
+
+    build_tree = BuildTree
+    update_all_sph_properties = UpdateAllSphProperties
+    update_all_sph_hydro_forces = UpdateAllSphHydroForces
+    update_all_sph_forces = UpdateAllSphForces
+
+    # ---- results --------------------------------------------------------------------------
+    def field(self, name: str) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.float64)
+        self._check(self._lib.gsph_get_field(self._ctx, _native.FIELD_ID[name], _dp(out)), "get_field")
+        return out
+
+    def field_device(self, name: str, out_ptr: int):
+        self._check(self._lib.gsph_get_field_device(self._ctx, _native.FIELD_ID[name],
+                                                    ctypes.c_void_p(out_ptr)), "get_field_device")
+
+    def results(self) -> dict:
+        return {k: self.field(k) for k in _native.FIELDS}
+
+    def stats(self) -> dict:
+        s = _native.Stats()
+        self._check(self._lib.gsph_get_stats(self._ctx, ctypes.byref(s)), "get_stats")
+        return {k: getattr(s, k) for k, _ in _native.Stats._fields_}
+
+    def set_stream(self, stream_ptr: int | None):
+        """Run on the given cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(self._lib.gsph_set_stream(self._ctx, ctypes.c_void_p(stream_ptr or 0)), "set_stream")
+
+    # ---- verification ---------------------------------------------------------------------
+    def set_recording(self, enable: bool, max_sph: int = 512):
+        self._check(self._lib.gsph_set_recording(self._ctx, int(enable), int(max_sph)), "set_recording")
+
+    def sph_neighbours(self) -> list:
+        tot = self._lib.gsph_get_sph_neighbours(self._ctx, None, None)
+        if tot < 0:
+            self._check(int(tot), "sph_neighbours")
+        off = np.zeros(self.n + 1, dtype=np.int64)
+        ids = np.zeros(max(int(tot), 1), dtype=np.int32)
+        r = self._lib.gsph_get_sph_neighbours(self._ctx, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                              ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        if r < 0:
+            self._check(int(r), "sph_neighbours")
+        return [ids[off[i]:off[i + 1]] for i in range(self.n)]
+
+    def direct_summary(self):
+        cnt = np.zeros(self.n, dtype=np.int64)
+        hsh = np.zeros(self.n, dtype=np.uint64)
+        self._check(self._lib.gsph_get_direct_summary(self._ctx, cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                                      hsh.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
+                    "direct_summary")
+        return cnt, hsh
+
+    def cell_summary(self):
+        st = self.stats()
+        nl = int(st["nleaf"])
+        leaf = np.zeros(nl, dtype=np.int32)
+        cnt = np.zeros(nl, dtype=np.int64)
+        hsh = np.zeros(nl, dtype=np.uint64)
+        self._check(self._lib.gsph_get_cell_summary(self._ctx, leaf.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                    cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                                    hsh.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
+                    "cell_summary")
+        return leaf, cnt, hsh
+
+    def tree(self) -> dict:
+        st = self.stats()
+        nc = int(st["ncell"])
+        cn = np.zeros(nc, dtype=np.int32)
+        cf = np.zeros(nc, dtype=np.int32)
+        order = np.zeros(self.n, dtype=np.int32)
+        data = np.zeros((nc, 31), dtype=np.float64)
+        P = ctypes.POINTER(ctypes.c_int32)
+        self._check(self._lib.gsph_get_tree(self._ctx, cn.ctypes.data_as(P), cf.ctypes.data_as(P),
+                                            order.ctypes.data_as(P), _dp(data)), "get_tree")
+        return {"cell_n": cn, "cell_first": cf, "order": order, "cells": data, "ltot": int(st["ltot"])}
+
+
+def mix64(ids: np.ndarray) -> np.ndarray:
+    """The order-independent hash term the kernels sum per list entry (splitmix64)."""
+    x = ids.astype(np.uint64) + np.uint64(0x9E3779B97F4A7C15)
+    with np.errstate(over="ignore"):
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+def list_hash(ids) -> np.uint64:
+    ids = np.asarray(ids)
+    if ids.size == 0:
+        return np.uint64(0)
+    with np.errstate(over="ignore"):
+        return np.sum(mix64(ids), dtype=np.uint64)

@@ -1,0 +1,176 @@
+/*
+ * gsph_gb300.h — C ABI of the GB300 grad-h SPH + KD-tree gravity particle step.
+ *
+ * One context holds one simulation's particles on one GPU.  The entry points replace the
+ * virtual methods a GANDALF Simulation calls on its SphNeighbourSearch object
+ * (GradhSphTree<ndim,GradhSphParticle>, src/Headers/SphNeighbourSearch.h:173-227):
+ *
+ *   gsph_build_tree                   <- HydroTree::BuildTree            src/Tree/HydroTree.cpp:309-372
+ *                                        (rebuild branch; also replaces BuildGhostTree
+ *                                        :381-441 and SearchBoundaryGhostParticles :494-543,
+ *                                        whose periodic images the kernels form on the fly)
+ *   gsph_update_all_sph_properties    <- GradhSphTree::UpdateAllSphProperties
+ *                                                                        src/GradhSph/GradhSphTree.cpp:82-271
+ *   gsph_update_all_sph_hydro_forces  <- GradhSphTree::UpdateAllSphHydroForces  :279-435
+ *   gsph_update_all_sph_forces        <- GradhSphTree::UpdateAllSphForces       :443-657
+ *
+ * Particles cross the boundary either as structure-of-arrays (plain double pointers) or
+ * as the caller's array-of-structures (GradhSphParticle records, Particle.h:285-368)
+ * described by byte offsets.  All calls are synchronous with respect to the host unless
+ * stated; none allocate pinned host memory; none abort the process.
+ *
+ * Return codes: GSPH_OK (0), a negative GSPH_ERR_* code on failure.  The context keeps
+ * a message for the last failure (gsph_last_error).
+ */
+#ifndef GSPH_GB300_H_
+#define GSPH_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSPH_ABI_VERSION 1
+
+#define GSPH_OK 0
+#define GSPH_ERR_INVALID -1        /* bad argument or particle data */
+#define GSPH_ERR_CUDA -2           /* CUDA runtime failure */
+#define GSPH_ERR_UNSUPPORTED -3    /* option outside the implemented path */
+#define GSPH_ERR_STATE -4          /* call made out of order (e.g. forces before h solve) */
+#define GSPH_ERR_NOT_CONVERGED -5  /* h-rho iteration failed; the reference raises
+                                      "Problem with convergence of h-rho iteration" */
+#define GSPH_ERR_CAPACITY -6       /* walk stack or hmax retry limit exhausted */
+
+typedef struct gsph_ctx gsph_ctx;
+
+enum gsph_eos { GSPH_EOS_ENERGY_EQN = 0, GSPH_EOS_ISOTHERMAL = 1 };
+enum gsph_multipole { GSPH_MONOPOLE = 0, GSPH_QUADRUPOLE = 1 };
+enum gsph_precision { GSPH_PRECISION_FP64 = 0, GSPH_PRECISION_MIXED = 1 };
+
+/* Run parameters; names follow the GANDALF parameter keys (src/Common/Parameters.cpp). */
+typedef struct gsph_config {
+  int32_t ndim;          /* must be 3 */
+  int32_t nleafmax;      /* "Nleafmax" (KD-tree leaf size), 1..32 */
+  int32_t hydro_forces;  /* "hydro_forces" */
+  int32_t self_gravity;  /* "self_gravity" */
+  int32_t eos;           /* "gas_eos": energy_eqn or isothermal */
+  int32_t multipole;     /* "multipole": monopole or quadrupole (geometric MAC) */
+  int32_t periodic;      /* 1: periodic in x, y and z ("boundary_lhs/rhs" = periodic) */
+  int32_t precision;     /* GSPH_PRECISION_FP64 or GSPH_PRECISION_MIXED */
+  double h_fac;          /* "h_fac" */
+  double h_converge;     /* "h_converge" */
+  double alpha_visc;     /* "alpha_visc" (avisc = mon97) */
+  double beta_visc;      /* "beta_visc" */
+  double gamma_eos;      /* "gamma_eos" */
+  double temp0;          /* "temp0" (isothermal) */
+  double mu_bar;         /* "mu_bar" (isothermal) */
+  double thetamaxsqd;    /* "thetamaxsqd" (geometric opening angle squared) */
+  double boxmin[3];      /* "boxmin[k]" (periodic box) */
+  double boxmax[3];      /* "boxmax[k]" */
+} gsph_config;
+
+/* Byte offsets of the fields inside one array-of-structures particle record.  r, v, a
+ * and atree point at 3 consecutive doubles.  An output offset of -1 skips that field. */
+typedef struct gsph_field_offsets {
+  int64_t r, v, m, h, u;                                   /* inputs */
+  int64_t rho, invomega, zeta, hfactor, hrangesqd, pressure, sound, div_v, dudt, a, atree,
+      gpot, gpot_hydro;                                    /* outputs */
+} gsph_field_offsets;
+
+/* Per-particle output fields for gsph_get_field (input order). */
+enum gsph_field {
+  GSPH_FIELD_H = 0, GSPH_FIELD_RHO, GSPH_FIELD_INVOMEGA, GSPH_FIELD_ZETA, GSPH_FIELD_HFACTOR,
+  GSPH_FIELD_PRESSURE, GSPH_FIELD_SOUND, GSPH_FIELD_U, GSPH_FIELD_DIV_V, GSPH_FIELD_DUDT,
+  GSPH_FIELD_AX, GSPH_FIELD_AY, GSPH_FIELD_AZ, GSPH_FIELD_AGX, GSPH_FIELD_AGY, GSPH_FIELD_AGZ,
+  GSPH_FIELD_GPOT, GSPH_FIELD_HRANGESQD, GSPH_FIELD_COUNT
+};
+
+/* Counters of the last step: interactions evaluated (used for the roofline), the
+ * status word of the kernels and the device time of each phase in milliseconds. */
+typedef struct gsph_stats {
+  int64_t n, ncell, nleaf, ltot;
+  int64_t density_pairs;   /* pair evaluations inside the kernel support, all iterations */
+  int64_t hydro_pairs;     /* SPH pairs of the force pass */
+  int64_t direct_pairs;    /* Newtonian particle-particle terms */
+  int64_t cell_pairs;      /* particle-multipole terms */
+  int64_t exact_checks;    /* mixed form: membership tests re-resolved in fp64 */
+  uint32_t status;
+  uint32_t launches;       /* kernels this library launched for the last step */
+  double ms_build, ms_density, ms_hmax, ms_forces, ms_total;
+} gsph_stats;
+
+/* ---- lifetime ------------------------------------------------------------------------- */
+int32_t gsph_abi_version(void);
+void gsph_config_defaults(gsph_config* cfg);     /* GANDALF defaults, kernel m4, Nleafmax 8 */
+gsph_ctx* gsph_create(const gsph_config* cfg, int32_t device);   /* NULL on failure */
+void gsph_destroy(gsph_ctx* ctx);
+const char* gsph_last_error(const gsph_ctx* ctx);
+int32_t gsph_create_error(void);                  /* code of the last failed gsph_create */
+
+/* Launch all further work of this context on the caller's CUDA stream (a cudaStream_t;
+ * NULL restores the context's own stream).  Calls still synchronise that stream before
+ * returning results to the host. */
+int32_t gsph_set_stream(gsph_ctx* ctx, void* stream);
+
+/* Measured fused multiply-add throughput of this GPU in GFLOP/s (2 flops per FMA):
+ * fp64 = 1 for double, 0 for float.  A calibration aid for roofline fractions of the
+ * pair loops, which run on the FP64 / FP32 pipes rather than tensor cores. */
+double gsph_fma_peak_gflops(int32_t device, int32_t fp64);
+
+/* ---- particle import (Simulation::ImportArraySph, src/Common/Simulation.cpp:1442) ------ */
+/* Host structure-of-arrays, n particles, input order.  Copies into device memory. */
+int32_t gsph_set_particles(gsph_ctx* ctx, int64_t n, const double* x, const double* y,
+                           const double* z, const double* vx, const double* vy, const double* vz,
+                           const double* m, const double* u, const double* h);
+/* Same, from device pointers (no host traffic). */
+int32_t gsph_set_particles_device(gsph_ctx* ctx, int64_t n, const double* x, const double* y,
+                                  const double* z, const double* vx, const double* vy,
+                                  const double* vz, const double* m, const double* u,
+                                  const double* h);
+/* Host array-of-structures (the reference's GradhSphParticle array): record stride and
+ * field offsets in bytes.  The records are kept on the device so gsph_get_particles_aos
+ * can write results back without touching other fields. */
+int32_t gsph_set_particles_aos(gsph_ctx* ctx, const void* base, int64_t n, int64_t stride,
+                               const gsph_field_offsets* off);
+
+/* ---- the step ---------------------------------------------------------------------------- */
+int32_t gsph_build_tree(gsph_ctx* ctx);
+int32_t gsph_update_all_sph_properties(gsph_ctx* ctx);   /* h-rho solve + tree hmax update */
+int32_t gsph_update_all_sph_hydro_forces(gsph_ctx* ctx);
+int32_t gsph_update_all_sph_forces(gsph_ctx* ctx);        /* hydro + self-gravity */
+/* build + properties + forces (hydro only or hydro + gravity, as configured) */
+int32_t gsph_step(gsph_ctx* ctx);
+
+/* ---- results ----------------------------------------------------------------------------- */
+/* One field for all particles in input order into host memory (n doubles). */
+int32_t gsph_get_field(gsph_ctx* ctx, int32_t field, double* out);
+/* Same into device memory. */
+int32_t gsph_get_field_device(gsph_ctx* ctx, int32_t field, double* out);
+/* Write results into the host records passed to gsph_set_particles_aos. */
+int32_t gsph_get_particles_aos(gsph_ctx* ctx, void* base, int64_t n, int64_t stride,
+                               const gsph_field_offsets* off);
+int32_t gsph_get_stats(gsph_ctx* ctx, gsph_stats* out);
+
+/* ---- verification (the reference's VERIFY_ALL checks, HydroTree.cpp:1900-1985) ----------- */
+/* Enable recording of interaction lists in the next force pass (max_sph entries per
+ * particle).  Costs atomics; for tests only. */
+int32_t gsph_set_recording(gsph_ctx* ctx, int32_t enable, int32_t max_sph);
+/* SPH neighbour lists of the last recorded force pass, input ids, CSR layout:
+ * offsets[n+1], ids[offsets[n]].  Call with ids == NULL to get the total count. */
+int64_t gsph_get_sph_neighbours(gsph_ctx* ctx, int64_t* offsets, int32_t* ids);
+/* Direct-sum partners per particle as (count, order-independent 64-bit hash of input
+ * ids), and multipole cells per leaf cell as (count, hash of depth-first cell ids). */
+int32_t gsph_get_direct_summary(gsph_ctx* ctx, int64_t* counts, uint64_t* hashes);
+int32_t gsph_get_cell_summary(gsph_ctx* ctx, int32_t* leaf_cells, int64_t* counts, uint64_t* hashes);
+/* The KD-tree: per depth-first cell N, and leaf membership as input ids in slot order
+ * (slot s holds input id order[s]; leaf cell c holds slots [first[c], first[c]+N[c])). */
+int32_t gsph_get_tree(gsph_ctx* ctx, int32_t* cell_n, int32_t* cell_first, int32_t* order,
+                      double* cell_data /* ncell x 31, layout of oracle cells */);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSPH_GB300_H_ */

@@ -96,6 +96,14 @@ inline double wpot(double s) {
 
 inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
+// splitmix64 term summed per list entry: an order-independent list hash.
+inline uint64_t mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
 struct Cell {
   int n, level, first;             // particles [first, first+n) of the leaf-ordered arrays
   double bbmin[3], bbmax[3], hbmin[3], hbmax[3], rcell[3], r[3], q[5];
@@ -120,6 +128,9 @@ struct Oracle {
   std::vector<std::vector<int>> hydro_neib, direct_neib;   // per particle (input ids)
   std::vector<std::vector<int>> gcell_list;                // per leaf (DFS ids)
   std::vector<int> gcell_leaf;
+  bool want_summary = false;                               // (count, hash) instead of lists
+  std::vector<int64_t> dir_count, cell_count;
+  std::vector<uint64_t> dir_hash, cell_hash;
   int64_t n_density_pairs = 0, n_hydro_pairs = 0, n_direct_pairs = 0, n_cell_pairs = 0;
 
   int c2_of(int c, int level) const { return c + (1 << (ltot - level)); }
@@ -560,7 +571,7 @@ struct Oracle {
         if (grav) direct_local.push_back(q);
         continue;
       }
-      if (want_lists) hydro_neib[i].push_back(j);
+      if (want_lists || want_summary) hydro_neib[i].push_back(j);
       pairs++;
       const double invh_j = 1.0 / h[j], invrho_j = 1.0 / rho[j];
       const double fac_j = (pressure[j] * invomega[j]) / (rho[j] * rho[j]);
@@ -692,16 +703,29 @@ struct Oracle {
 #pragma omp critical
           { gcell_leaf.push_back(lc); gcell_list.push_back(gcells); }
         }
+        if (want_summary) {
+          uint64_t hsh = 0;
+          for (int cc : gcells) hsh += mix64((uint64_t) cc);
+          cell_count[li] = (int64_t) gcells.size();
+          cell_hash[li] = hsh;
+        }
         for (int j = 0; j < cell.n; j++) {
           const int i = order[cell.first + j];
           gpot[i] = (m[i] / h[i]) * wpot(0.0);
           for (int k = 0; k < 3; k++) ag[k][i] = 0.0;
           std::vector<int> dl;
           const int64_t before = local_pairs;
-          pair_loop(i, near_id, near_r, true, want_lists ? &dl : nullptr, local_pairs);
+          pair_loop(i, near_id, near_r, true, (want_lists || want_summary) ? &dl : nullptr, local_pairs);
           local_direct += (int64_t) near_id.size() - (local_pairs - before);
           for (int id : direct_id) direct_term(i, x[0][id], x[1][id], x[2][id], m[id]);
           for (int cc : gcells) cell_term(i, cells[cc], quad);
+          if (want_summary) {
+            uint64_t hsh = 0;
+            for (int id : dl) hsh += mix64((uint64_t) id);
+            for (int id : direct_id) hsh += mix64((uint64_t) id);
+            dir_count[i] = (int64_t) (dl.size() + direct_id.size());
+            dir_hash[i] = hsh;
+          }
           if (want_lists) {
             dl.insert(dl.end(), direct_id.begin(), direct_id.end());
             direct_neib[i] = dl;
@@ -757,9 +781,14 @@ struct Oracle {
     pressure.assign(n, 0); sound.assign(n, 0); div_v.assign(n, 0); dudt.assign(n, 0);
     gpot.assign(n, 0); hrangesqd.assign(n, 0);
     for (int k = 0; k < 3; k++) { a[k].assign(n, 0); ag[k].assign(n, 0); }
-    if (want_lists) { hydro_neib.assign(n, {}); direct_neib.assign(n, {}); gcell_list.clear(); gcell_leaf.clear(); }
+    if (want_lists || want_summary) hydro_neib.assign(n, {});
+    if (want_lists) { direct_neib.assign(n, {}); gcell_list.clear(); gcell_leaf.clear(); }
     h_ghost = h;
     build_tree();
+    if (want_summary) {
+      dir_count.assign(n, 0); dir_hash.assign(n, 0);
+      cell_count.assign(leaves.size(), 0); cell_hash.assign(leaves.size(), 0);
+    }
     const int st = density();
     if (st != 0) return st;
     update_hmax(0);
@@ -793,7 +822,8 @@ int gsph_oracle_run(void* handle, int64_t n, const double* x, const double* y, c
   o->x[0].assign(x, x + n); o->x[1].assign(y, y + n); o->x[2].assign(z, z + n);
   o->v[0].assign(vx, vx + n); o->v[1].assign(vy, vy + n); o->v[2].assign(vz, vz + n);
   o->m.assign(m, m + n); o->u.assign(u, u + n); o->h.assign(h, h + n);
-  o->want_lists = want_lists != 0;
+  o->want_lists = want_lists == 1;
+  o->want_summary = want_lists == 2;
   o->n_density_pairs = o->n_hydro_pairs = o->n_direct_pairs = o->n_cell_pairs = 0;
   return o->run(nthreads);
 }
@@ -862,6 +892,19 @@ int64_t gsph_oracle_list(void* handle, int which, int32_t* off, int32_t* ids) {
   }
   return tot;
 }
+
+// Summaries of a run with want_lists == 2: direct partners per particle (input order)
+// and multipole cells per leaf (left-to-right leaf order), as (count, hash).
+void gsph_oracle_summary(void* handle, int64_t* dir_count, uint64_t* dir_hash, int32_t* leaf_cell,
+                         int64_t* cell_count, uint64_t* cell_hash) {
+  Oracle* o = static_cast<Oracle*>(handle);
+  for (int64_t i = 0; i < o->n; i++) { dir_count[i] = o->dir_count[i]; dir_hash[i] = o->dir_hash[i]; }
+  for (size_t q = 0; q < o->leaves.size(); q++) {
+    leaf_cell[q] = o->leaves[q]; cell_count[q] = o->cell_count[q]; cell_hash[q] = o->cell_hash[q];
+  }
+}
+
+int gsph_oracle_nleaf(void* handle) { return (int) static_cast<Oracle*>(handle)->leaves.size(); }
 
 // Interaction counts of the last run: density pair evaluations, hydro pairs,
 // direct pairs, cell-particle pairs.

@@ -82,6 +82,11 @@ def _load():
         lib.gsph_oracle_list.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int32),
                                          ctypes.POINTER(ctypes.c_int32)]
         lib.gsph_oracle_counts.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+        lib.gsph_oracle_summary.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint64),
+                                            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
+                                            ctypes.POINTER(ctypes.c_uint64)]
+        lib.gsph_oracle_nleaf.restype = i32
+        lib.gsph_oracle_nleaf.argtypes = [vp]
         _lib = lib
     return _lib
 
@@ -106,8 +111,12 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0) -> dict:
-    """One step of the restated algorithm; same result layout as oracle/refio.run."""
+def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0, summary: bool = False) -> dict:
+    """One step of the restated algorithm; same result layout as oracle/refio.run.
+
+    lists: full interaction lists (small N only); summary: SPH lists plus (count, hash)
+    of direct partners per particle and multipole cells per leaf.
+    """
     lib = _load()
     prm = make_params(params)
     h = lib.gsph_oracle_create(ctypes.byref(prm))
@@ -115,7 +124,8 @@ def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0) -> dict
         arrs = [np.ascontiguousarray(ics[k], dtype=np.float64)
                 for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")]
         n = len(arrs[0])
-        st = lib.gsph_oracle_run(h, n, *[_ptr(a) for a in arrs], int(lists), int(nthreads))
+        mode = 1 if lists else (2 if summary else 0)
+        st = lib.gsph_oracle_run(h, n, *[_ptr(a) for a in arrs], mode, int(nthreads))
         if st != 0:
             raise RuntimeError(f"oracle step failed with status {st}")
         out = np.empty((n, len(PARTICLE_FIELDS)))
@@ -134,6 +144,23 @@ def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0) -> dict
             "counts": dict(density_pairs=counts[0], hydro_pairs=counts[1],
                            direct_pairs=counts[2], cell_pairs=counts[3]),
         }
+        if summary:
+            tot = lib.gsph_oracle_list(h, 0, None, None)
+            off = np.zeros(n + 1, dtype=np.int32)
+            ids = np.zeros(max(tot, 1), dtype=np.int32)
+            lib.gsph_oracle_list(h, 0, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                 ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+            res["hydro_neib"] = [ids[off[i]:off[i + 1]] for i in range(n)]
+            nl = lib.gsph_oracle_nleaf(h)
+            dc = np.zeros(n, dtype=np.int64)
+            dh = np.zeros(n, dtype=np.uint64)
+            lc = np.zeros(nl, dtype=np.int32)
+            cc = np.zeros(nl, dtype=np.int64)
+            ch = np.zeros(nl, dtype=np.uint64)
+            P64, PU, P32 = ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)
+            lib.gsph_oracle_summary(h, dc.ctypes.data_as(P64), dh.ctypes.data_as(PU), lc.ctypes.data_as(P32),
+                                    cc.ctypes.data_as(P64), ch.ctypes.data_as(PU))
+            res.update(direct_count=dc, direct_hash=dh, leaf_cell=lc, cell_count=cc, cell_hash=ch)
         if lists:
             names = {0: "hydro_neib", 1: "grav_direct", 2: "gcell_lists"}
             for which, name in names.items():

@@ -1,0 +1,193 @@
+"""GPU (fp64 form) against the reference fixtures and the oracle, through the C ABI.
+
+Values: the FP64_TOL tolerances in tests/parity.py.  Lists: bit-exact — the SPH
+neighbour list of every particle, the direct-sum partner set (count and hash) of every
+particle, the multipole cell set (count and hash) of every leaf, and the KD-tree itself.
+"""
+import numpy as np
+import pytest
+
+from gandalf_gb300 import ics as ics_mod
+from gandalf_gb300.sph import GandalfError, GradhSphTree, list_hash
+from oracle import oracle
+from parity import check_fp64, csr_lists, load_golden, same_lists
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(ics, params, record=True, max_sph=512, precision="fp64"):
+    t = GradhSphTree(params, precision=precision)
+    t.set_particles(ics)
+    if record:
+        t.set_recording(True, max_sph)
+    t.step()
+    out = t.results()
+    return t, out
+
+
+def check_tree(t, d_cells, leaf_cell, leaf_lists):
+    tr = t.tree()
+    cells = tr["cells"]
+    assert np.array_equal(tr["cell_n"], d_cells[:, 0].astype(np.int32))
+    # geometry bit-exact: bb, rcell, rmax, cdistsqd (reference columns 4-9, 16-18, 23, 25)
+    assert np.array_equal(cells[:, 6:12], d_cells[:, 4:10])
+    assert np.array_equal(cells[:, 18:21], d_cells[:, 16:19])
+    assert np.array_equal(cells[:, 3], d_cells[:, 23])
+    assert np.array_equal(cells[:, 5], d_cells[:, 25])
+    # mass and centre of mass to rounding
+    np.testing.assert_allclose(cells[:, 2], d_cells[:, 22], rtol=1e-13, atol=0)
+    order = tr["order"]
+    for lc, mem in zip(leaf_cell, leaf_lists):
+        f = tr["cell_first"][lc]
+        assert np.array_equal(np.sort(order[f:f + tr["cell_n"][lc]]), mem)
+
+
+@pytest.mark.parametrize("name,gravity", [("cube2048", False), ("plummer2048", True)])
+def test_gpu_matches_reference_fixture(name, gravity):
+    ics, params, ref, d = load_golden(name)
+    t, out = run_gpu(ics, params)
+    check_fp64(out, ref, gravity)
+    check_tree(t, d["cells"], d["leaf_cell"], csr_lists(d["leaf_off"], d["leaf_ids"]))
+    assert same_lists(t.sph_neighbours(), csr_lists(d["hydro_off"], d["hydro_ids"])) == []
+    if gravity:
+        cnt, hsh = t.direct_summary()
+        assert np.array_equal(cnt, d["direct_count"])
+        assert np.array_equal(hsh, d["direct_hash"])
+        leaf, ccnt, chsh = t.cell_summary()
+        mine = {int(l): (int(c), int(h)) for l, c, h in zip(leaf, ccnt, chsh)}
+        for l, c, h in zip(d["gcell_leaf"], d["gcell_count"], d["gcell_hash"]):
+            assert mine[int(l)] == (int(c), int(h))
+    t.close()
+
+
+def compare_with_oracle(c, params, gravity):
+    r = oracle.run(c, params, summary=True)
+    t, out = run_gpu(c, params)
+    check_fp64(out, r["particles"], gravity)
+    assert same_lists(t.sph_neighbours(), r["hydro_neib"]) == []
+    if gravity:
+        cnt, hsh = t.direct_summary()
+        assert np.array_equal(cnt, r["direct_count"])
+        assert np.array_equal(hsh, r["direct_hash"])
+        leaf, ccnt, chsh = t.cell_summary()
+        assert np.array_equal(leaf, r["leaf_cell"])
+        assert np.array_equal(ccnt, r["cell_count"])
+        assert np.array_equal(chsh, r["cell_hash"])
+    st = t.stats()
+    assert st["hydro_pairs"] == r["counts"]["hydro_pairs"]
+    if gravity:
+        assert st["direct_pairs"] == r["counts"]["direct_pairs"]
+        assert st["cell_pairs"] == r["counts"]["cell_pairs"]
+    t.close()
+
+
+def test_gpu_periodic_cube_full_size_vs_oracle():
+    """The periodic-cube workload at its full size, N = 32768."""
+    c = ics_mod.periodic_cube(32768, seed=1234)
+    compare_with_oracle(c, c["params"], gravity=False)
+
+
+@pytest.mark.parametrize("n", [1000, 4099, 65536])
+def test_gpu_plummer_vs_oracle(n):
+    """Ragged (non power-of-two) and larger Plummer spheres."""
+    c = ics_mod.plummer_sphere(n, seed=77 + n)
+    compare_with_oracle(c, c["params"], gravity=True)
+
+
+@pytest.mark.parametrize("n", [1, 5, 9, 100])
+def test_gpu_tiny_open_sets(n):
+    """Tiny sets: a single-leaf tree and leaves with one particle."""
+    c = ics_mod.plummer_sphere(n, seed=5 + n)
+    compare_with_oracle(c, dict(c["params"], nleafmax=8), gravity=True)
+    compare_with_oracle(c, dict(c["params"], nleafmax=1), gravity=True)
+
+
+def test_gpu_step_equals_separate_calls():
+    c = ics_mod.plummer_sphere(4096, seed=3)
+    _, a = run_gpu(c, c["params"], record=False)
+    t = GradhSphTree(c["params"])
+    t.set_particles(c)
+    t.BuildTree()
+    t.UpdateAllSphProperties()
+    t.UpdateAllSphForces()
+    b = t.results()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_gpu_call_order_is_enforced():
+    c = ics_mod.periodic_cube(512, seed=3)
+    t = GradhSphTree(c["params"])
+    t.set_particles(c)
+    with pytest.raises(GandalfError, match="STATE"):
+        t.UpdateAllSphHydroForces()
+    t.BuildTree()
+    with pytest.raises(GandalfError, match="STATE"):
+        t.UpdateAllSphHydroForces()
+    t.UpdateAllSphProperties()
+    t.UpdateAllSphHydroForces()
+    with pytest.raises(GandalfError, match="STATE"):
+        t.UpdateAllSphForces()   # self_gravity is off
+
+
+def test_gpu_rejects_bad_particles():
+    c = ics_mod.periodic_cube(256, seed=3)
+    t = GradhSphTree(c["params"])
+    bad = dict(c)
+    bad["m"] = c["m"].copy()
+    bad["m"][7] = 0.0
+    with pytest.raises(GandalfError, match="INVALID"):
+        t.set_particles(bad)
+    bad = dict(c)
+    bad["x"] = c["x"].copy()
+    bad["x"][3] = 1.5   # outside the periodic box
+    with pytest.raises(GandalfError, match="INVALID"):
+        t.set_particles(bad)
+
+
+def gradh_record_dtype():
+    """A record with GradhSphParticle<3>'s field order (src/Headers/Particle.h:133-368)."""
+    fields = [("flags", "<u4"), ("ptype", "<i4"), ("iorig", "<i4"), ("sinkid", "<i4"),
+              ("levelneib", "<i4"), ("nstep", "<i4"), ("nlast", "<i4"), ("level", "<i4"),
+              ("r", "<f8", 3), ("v", "<f8", 3), ("a", "<f8", 3), ("atree", "<f8", 3),
+              ("r0", "<f8", 3), ("v0", "<f8", 3), ("a0", "<f8", 3), ("m", "<f8"), ("h", "<f8"),
+              ("h_dust", "<f8"), ("hrangesqd", "<f8"), ("hfactor", "<f8"), ("sound", "<f8"),
+              ("rho", "<f8"), ("pressure", "<f8"), ("u", "<f8"), ("u0", "<f8"), ("dudt0", "<f8"),
+              ("dudt", "<f8"), ("gpot", "<f8"), ("gpot_hydro", "<f8"), ("dt", "<f8"),
+              ("dt_next", "<f8"), ("tlast", "<f8"), ("ionfrac", "<f8"), ("Xion", "<f8"),
+              ("ueq", "<f8"), ("dt_therm", "<f8"), ("vsig_max", "<f8"), ("rad_pres", "<f8", 3),
+              ("ionstate", "<i4"), ("pad", "<i4"), ("div_v", "<f8"), ("alpha", "<f8"),
+              ("dalphadt", "<f8"), ("invomega", "<f8"), ("zeta", "<f8")]
+    return np.dtype(fields)
+
+
+def aos_offsets(dt):
+    off = {k: dt.fields[k][1] for k in ("r", "v", "m", "h", "u", "rho", "invomega", "zeta", "hfactor",
+                                         "hrangesqd", "pressure", "sound", "div_v", "dudt", "a",
+                                         "atree", "gpot", "gpot_hydro")}
+    return off
+
+
+def test_gpu_aos_records_roundtrip():
+    """The array-of-structures path gives the same results and leaves other fields alone."""
+    c = ics_mod.plummer_sphere(3000, seed=9)
+    _, soa = run_gpu(c, c["params"], record=False)
+    dt = gradh_record_dtype()
+    rec = np.zeros(len(c["x"]), dtype=dt)
+    rec["r"] = np.stack([c["x"], c["y"], c["z"]], 1)
+    rec["v"] = np.stack([c["vx"], c["vy"], c["vz"]], 1)
+    rec["m"], rec["u"], rec["h"] = c["m"], c["u"], c["h"]
+    rec["iorig"] = np.arange(len(rec))
+    rec["alpha"] = 1.0
+    t = GradhSphTree(c["params"])
+    off = aos_offsets(dt)
+    t.set_particles_aos(rec, off)
+    t.step()
+    t.get_particles_aos(rec, off)
+    assert np.array_equal(rec["h"], soa["h"])
+    assert np.array_equal(rec["rho"], soa["rho"])
+    assert np.array_equal(rec["a"][:, 0], soa["ax"])
+    assert np.array_equal(rec["atree"][:, 2], soa["agz"])
+    assert np.array_equal(rec["dudt"], soa["dudt"])
+    assert np.array_equal(rec["iorig"], np.arange(len(rec)))
+    assert np.all(rec["alpha"] == 1.0)
