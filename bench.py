@@ -350,7 +350,10 @@ def main():
         Rf = results[f]
         forms_out[f] = {"value": n * args.steps / (Rf["ms_total"] * 1e-3),
                         "ms_per_step": Rf["ms_total"] / args.steps,
-                        "phases_ms": {k: round(v, 4) for k, v in Rf["per"].items()}}
+                        "phases_ms": {k: round(v, 4) for k, v in Rf["per"].items()},
+                        "counts": {k: Rf["stats"][k] for k in ("density_pairs", "hydro_pairs",
+                                                               "direct_pairs", "cell_pairs",
+                                                               "exact_checks", "launches")}}
     if "fp64" in ok and "mixed" in ok:
         a, b = results["mixed"]["results"], results["fp64"]["results"]
         errs = {}

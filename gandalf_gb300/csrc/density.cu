@@ -25,7 +25,7 @@ namespace {
 constexpr int kDensWarps = 4;          // warps per block
 constexpr int kDensStack = 1024;       // walk stack entries per warp
 constexpr int kDensList = 1024;        // gather-list entries per warp
-constexpr int kMaxAttempts = 96;       // 1.05^96 ~ 108x growth of hmax
+constexpr int kMaxAttempts = 256;      // attempts of the (skipping) hmax sequence
 constexpr int kNodeBits = 25;          // depth-first ids < 2^25 (ltot <= 23)
 constexpr int kNoShift = 13;           // periodic image code for (0,0,0)
 
@@ -64,15 +64,19 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
   unsigned long long pairs = 0;
 
   // final per-particle results
-  double h_out = h_start, rho_out = 0.0, om_out = 0.0, zeta_out = 0.0;
-  bool fail = false, solved = false;
+  double h_out = h_start, rho_out = 0.0, om_out = 0.0, zeta_out = 0.0, hl_out = 0.0;
+  bool fail = false, stack_ok = true;
 
-  for (int attempt = 0; attempt < kMaxAttempts; attempt++) {
-    hmax = __dmul_rn(1.05, hmax);
-    const double hr = __dmul_rn(kKernRange, hmax);
+  // One attempt of the reference's cell loop with gather radius 2*hmax_list.
+  // GradhSph::ComputeH with hmax = hmax_list for every particle of the cell; returns
+  // true if some particle's h exceeded hmax (the cell must be redone).  mcheck keeps
+  // the largest h the reference's "h > hmax" test has seen.  (probe == true stops
+  // after the fixed-point phase.)
+  double mcheck = 0.0;
+  auto attempt = [&](double hmax_list, bool probe) -> bool {
+    const double hr = __dmul_rn(kKernRange, hmax_list);
     double gmin[3], gmax[3];
     for (int k = 0; k < 3; k++) { gmin[k] = __dsub_rn(bb.bbmin[k], hr); gmax[k] = __dadd_rn(bb.bbmax[k], hr); }
-    // periodic image codes needed by this gather box (ghost semantics)
     int nsh[3] = {1, 1, 1}, sh[3][3];
     for (int k = 0; k < 3; k++) {
       sh[k][0] = 1;
@@ -81,10 +85,8 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
         if (gmin[k] < prm.boxmin[k]) sh[k][nsh[k]++] = 0;   // images r - L of rhs particles
       }
     }
-
-    // ---- gather walk into the cached list (or detect that it does not fit) ----------
     WarpLists L{list, list, list, 0, 0, 0, kDensList};
-    bool overflow = false, stack_ok = true;
+    bool overflow = false;
     auto walk_all = [&](auto&& flush) {
       for (int a0 = 0; a0 < nsh[0]; a0++)
         for (int a1 = 0; a1 < nsh[1]; a1++)
@@ -109,11 +111,11 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
     walk_all([&]() { overflow = true; });
     const int ncached = L.na;
 
-    // ---- h-rho iteration, reference semantics (GradhSph::ComputeH) -------------------
-    double hi = h_start, h_lower = 0.0, h_upper = hmax;
+    double hi = h_start, h_lower = 0.0, h_upper = hmax_list;
     double rho = 0.0, om = 0.0, zeta = 0.0;
     int iteration = 0;
     bool done = !mine, abort_cell = false;
+    double mloc = 0.0;
     while (__any_sync(kFull, !done)) {
       iteration++;
       const double invh = 1.0 / hi;
@@ -158,8 +160,7 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
       if (!overflow) {
         consume(ncached);
       } else {
-        WarpLists L2{list, list, list, 0, 0, 0, kDensList};
-        L = L2;
+        L = WarpLists{list, list, list, 0, 0, 0, kDensList};
         walk_all([&]() { consume(L.na); });
         consume(L.na);
       }
@@ -174,6 +175,8 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
         const double hrho = prm.h_fac * pow(mi / rho, 1.0 / 3.0);
         if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
           done = true;
+        } else if (probe && iteration >= 30) {
+          done = true;                      // the bisection phase never exceeds hmax
         } else {
           if (iteration < 30) hi = hrho;
           else if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
@@ -185,23 +188,40 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
             done = true;
           }
           if (!done) {
-            if (hi > hmax) { abort_cell = true; done = true; }
+            mloc = fmax(mloc, hi);
+            if (hi > hmax_list) { abort_cell = true; done = true; }
             else if (!(hi > h_lower && hi < h_upper)) done = true;
           }
         }
       }
     }
-    if (__any_sync(kFull, abort_cell)) continue;   // retry the whole cell with larger hmax
-    if (mine) {
-      const double hrho = prm.h_fac * pow(mi / rho, 1.0 / 3.0);
-      h_out = fmax(hrho, h_lower);
-      rho_out = rho; om_out = om; zeta_out = zeta;
+    double mw = mloc;
+    for (int o = 16; o > 0; o >>= 1) mw = fmax(mw, __shfl_xor_sync(kFull, mw, o));
+    mcheck = fmax(mcheck, mw);
+    const bool any_abort = __any_sync(kFull, abort_cell);
+    if (!any_abort && !probe && mine) {
+      h_out = fmax(prm.h_fac * pow(mi / rho, 1.0 / 3.0), h_lower);
+      rho_out = rho; om_out = om; zeta_out = zeta; hl_out = h_lower;
     }
-    if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
-    if (__any_sync(kFull, fail) && lane == 0) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
-    solved = true;
-    break;
+    return any_abort;
+  };
+
+  // Reference sequence: hmax_k = 1.05 hmax_{k-1}, redo the cell while some h > hmax_k
+  // (GradhSphTree.cpp:154-240).  The h values an attempt visits before its abort do not
+  // depend on hmax_k, so every hmax_j below the largest h seen so far would abort too:
+  // the next attempt jumps to the first hmax_j of the same sequence at or above it.
+  bool solved = false;
+  double hk = __dmul_rn(1.05, hmax);
+  for (int a = 0; a < kMaxAttempts && !solved; a++) {
+    if (!attempt(hk, false)) {
+      solved = true;
+    } else {
+      int guard = 0;
+      do { hk = __dmul_rn(1.05, hk); } while (hk < mcheck && ++guard < 100000);
+    }
   }
+  if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
+  if (__any_sync(kFull, fail) && lane == 0) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
   if (!solved && lane == 0) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
   {
     unsigned long long tot = pairs;

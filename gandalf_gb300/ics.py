@@ -41,7 +41,7 @@ def periodic_cube(n: int = 32768, seed: int = 1234) -> dict:
     h = np.full(n, H_FAC * (1.0 / n) ** (1.0 / 3.0))
     ics = _pack(x, v, m, u, h)
     ics["params"] = dict(self_gravity=0, eos=0, periodic=1, boxmin=(0.0, 0.0, 0.0),
-                         boxmax=(1.0, 1.0, 1.0), gamma_eos=5.0 / 3.0)
+                         boxmax=(1.0, 1.0, 1.0), gamma_eos=5.0 / 3.0, thetamaxsqd=0.25)
     return ics
 
 
