@@ -81,6 +81,7 @@ SIGNATURES = {
                                      ctypes.POINTER(ctypes.c_uint64)]),
     "gsph_set_stream": (_I32, [_P, _P]),
     "gsph_fma_peak_gflops": (ctypes.c_double, [_I32, _I32]),
+    "gsph_kdtree_order_noalloc": (_I32, [_P, _P, _P, _P, _I32, _I32, _P, _P]),
     "gsph_get_tree": (_I32, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                              ctypes.POINTER(ctypes.c_int32), _D]),
 }

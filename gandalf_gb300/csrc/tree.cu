@@ -535,3 +535,124 @@ void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st) {
 }
 
 }  // namespace gsph
+
+// ======================================================================================
+// Allocation-free KD-tree ordering.
+//
+// For callers that cannot allocate device memory themselves — code whose device memory
+// is owned by another allocator (a pool that has reserved the whole GPU), or a
+// time-critical loop where cudaMalloc's implicit device synchronisation is not
+// acceptable.  The scratch this computation needs lives in one file-scope device array
+// of fixed size, held by every GPU that loads the library until the process exits.
+// ======================================================================================
+namespace gsph {
+namespace {
+
+constexpr int kNaMaxN = 32768;                              // particles
+constexpr int kNaMaxLtot = 13;                              // tree levels
+constexpr int kNaMaxCell = (1 << (kNaMaxLtot + 1)) - 1;     // depth-first cells
+constexpr int kNaMaxNb = (kNaMaxN + kScanBlock - 1) / kScanBlock;
+
+struct NoAllocScratch {
+  unsigned long long key[3][kNaMaxN];
+  int idx[3][kNaMaxN];
+  int listb[3][kNaMaxN];
+  double ibox[6 * kNaMaxCell];
+  int heap_first[kNaMaxCell];
+  int heap_n[kNaMaxCell];
+  int heap_ones[kNaMaxCell];
+  int blocksum[3 * kNaMaxNb];
+  unsigned long long rootkey[8];
+  unsigned char side[kNaMaxN];
+  unsigned char seg_axis[(kNaMaxCell + 1) / 2];
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Device address of g_noalloc_scratch, looked up once per device (host code cannot use
+// the symbol itself as a device pointer).
+constexpr int kNaMaxDevices = 64;
+NoAllocScratch* g_noalloc_ptr[kNaMaxDevices] = {};
+
+// Heap-indexed segment tables of level l (block l): first, count and the number of
+// second-child positions before each segment.
+__global__ void __launch_bounds__(1024) k_noalloc_heap_tables(int n, NoAllocScratch* s) {
+  __shared__ int ws[33];
+  const int l = blockIdx.x;
+  const int nseg = 1 << l;
+  int carry = 0;
+  for (int base = 0; base < nseg; base += 1024) {
+    const int q = base + threadIdx.x;
+    int f = 0, c = n;
+    if (q < nseg) {
+      for (int lev = l - 1; lev >= 0; lev--) {
+        const int half = c >> 1;
+        if ((q >> lev) & 1) { f += half; c -= half; } else { c = half; }
+      }
+    }
+    const int ones = q < nseg ? c - (c >> 1) : 0;
+    int total;
+    const int ex = block_exscan(ones, ws, total);
+    if (q < nseg) {
+      const int h = nseg - 1 + q;
+      s->heap_first[h] = f;
+      s->heap_n[h] = c;
+      s->heap_ones[h] = carry + ex;
+    }
+    carry += total;
+  }
+}
+
+}  // namespace
+}  // namespace gsph
+
+// Leaf-cell order of the reference KD-tree (KDTree::BuildTree, src/Tree/KDTree.cpp:219-595)
+// computed without allocating: see include/gsph_gb300.h.
+extern "C" int32_t gsph_kdtree_order_noalloc(const double* x, const double* y, const double* z,
+                                             const double* h, int32_t n, int32_t nleafmax,
+                                             int32_t* order, void* stream) {
+  using namespace gsph;
+  if (!x || !y || !z || !h || !order || n < 1 || nleafmax < 1) return -1;   // GSPH_ERR_INVALID
+  int ltot = 0;
+  while ((double) nleafmax * (double) (1 << ltot) < (double) n && ltot <= kNaMaxLtot) ltot++;
+  if (n > kNaMaxN || ltot > kNaMaxLtot) return -6;                          // GSPH_ERR_CAPACITY
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return -2;
+  if (!g_noalloc_ptr[dev]) {
+    NoAllocScratch* p = nullptr;
+    if (cudaGetSymbolAddress((void**) &p, g_noalloc_scratch) != cudaSuccess || !p) return -2;
+    g_noalloc_ptr[dev] = p;
+  }
+  NoAllocScratch* s = g_noalloc_ptr[dev];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  k_noalloc_heap_tables<<<ltot + 1, 1024, 0, st>>>(n, s);
+  k_root_box_init<<<1, 32, 0, st>>>(s->rootkey);
+  k_root_box<<<grid_for(n, 256, 152 * 4), 256, 0, st>>>(x, y, z, h, n, s->rootkey);
+  k_root_box_store<<<1, 32, 0, st>>>(s->rootkey, s->ibox);
+  SortArrays sa;
+  for (int q = 0; q < 3; q++) { sa.key[q] = s->key[q]; sa.idx[q] = s->idx[q]; }
+  const int P = sort_padded_size(n);
+  k_sort_init<<<dim3(grid_for(P, 256), 3), 256, 0, st>>>(x, y, z, n, P, sa);
+  k_bitonic_smem<<<dim3(P / kSortBlock, 3), kSortBlock / 2, 0, st>>>(sa, 2, kSortBlock, kSortBlock / 2);
+  for (int k = 2 * kSortBlock; k <= P; k <<= 1) {
+    for (int j = k >> 1; j >= kSortBlock; j >>= 1)
+      k_bitonic_global<<<dim3(grid_for(P / 2, 256, 1 << 20), 3), 256, 0, st>>>(sa, P, k, j);
+    k_bitonic_smem<<<dim3(P / kSortBlock, 3), kSortBlock / 2, 0, st>>>(sa, k, k, kSortBlock / 2);
+  }
+  BuildLists cur, nxt;
+  for (int q = 0; q < 3; q++) { cur.l[q] = s->idx[q]; nxt.l[q] = s->listb[q]; }
+  const int nb = partition_blocks(n);
+  for (int l = 0; l < ltot; l++) {
+    const int nseg = 1 << l;
+    k_split_prepare<<<(nseg + 127) / 128, 128, 0, st>>>(l, cur, x, y, z, s->heap_first, s->heap_n, s->ibox,
+                                                         s->seg_axis);
+    k_mark_side<<<grid_for(n, 256), 256, 0, st>>>(l, n, cur, s->seg_axis, s->side);
+    k_part_count<<<dim3(nb, 3), 1024, 0, st>>>(n, cur, s->side, s->blocksum, nb);
+    k_part_scan<<<dim3(1, 3), 1024, 0, st>>>(s->blocksum, nb);
+    k_part_scatter<<<dim3(nb, 3), 1024, 0, st>>>(l, n, cur, nxt, s->side, s->blocksum, nb, s->heap_ones);
+    BuildLists tmp = cur; cur = nxt; nxt = tmp;
+  }
+  if (cudaMemcpyAsync(order, cur.l[0], sizeof(int) * (size_t) n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return -2;
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}

@@ -169,6 +169,30 @@ int32_t gsph_get_cell_summary(gsph_ctx* ctx, int32_t* leaf_cells, int64_t* count
 int32_t gsph_get_tree(gsph_ctx* ctx, int32_t* cell_n, int32_t* cell_first, int32_t* order,
                       double* cell_data /* ncell x 31, layout of oracle cells */);
 
+/* ---- allocation-free KD-tree ordering --------------------------------------------------- */
+/* No counterpart in the reference: an extra entry point for callers that cannot allocate
+ * device memory — e.g. a host code whose device memory is all owned by its own pool
+ * allocator, or a time-critical loop that cannot afford cudaMalloc's implicit device
+ * synchronisation.  It computes the leaf order of the reference KD-tree (the slot order
+ * gsph_build_tree produces: order[s] = input index of slot s) for n <= GSPH_NOALLOC_MAX_N
+ * particles whose x, y, z, h are device arrays, writing n int32 to the device array
+ * order.  Work is enqueued on `stream` (a cudaStream_t, NULL for the legacy default
+ * stream) and the call returns without waiting for it.
+ *   Memory: no cudaMalloc/cudaFree or other allocating call.  Scratch is one fixed
+ *   ~2.6 MiB device array inside the library, held by every GPU that loads the library
+ *   until the process exits.  All calls on a device share it, so calls whose work
+ *   overlaps on the GPU race; serialise them (one stream, or events).  Each call fully
+ *   rewrites the scratch it reads, so nothing left by a previous call leaks into a result.
+ *   Set-up: the first call on each device (with that device current) looks up the
+ *   array's device address; make that first call before any stream capture.
+ *   Limits: 1 <= n <= GSPH_NOALLOC_MAX_N and a tree of at most 13 levels
+ *   (Nleafmax * 2^13 >= n).  Larger requests return GSPH_ERR_CAPACITY; bad pointers or
+ *   sizes GSPH_ERR_INVALID; CUDA failures GSPH_ERR_CUDA. */
+#define GSPH_NOALLOC_MAX_N 32768
+int32_t gsph_kdtree_order_noalloc(const double* x, const double* y, const double* z,
+                                  const double* h, int32_t n, int32_t nleafmax, int32_t* order,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif
