@@ -44,6 +44,7 @@ class Stats(ctypes.Structure):
                 ("ltot", ctypes.c_int64), ("density_pairs", ctypes.c_int64),
                 ("hydro_pairs", ctypes.c_int64), ("direct_pairs", ctypes.c_int64),
                 ("cell_pairs", ctypes.c_int64), ("exact_checks", ctypes.c_int64),
+                ("heavy_density", ctypes.c_int64), ("heavy_forces", ctypes.c_int64),
                 ("status", ctypes.c_uint32), ("launches", ctypes.c_uint32),
                 ("ms_build", ctypes.c_double), ("ms_density", ctypes.c_double),
                 ("ms_hmax", ctypes.c_double), ("ms_forces", ctypes.c_double),

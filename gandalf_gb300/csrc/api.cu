@@ -18,6 +18,7 @@
 #include "../../include/gsph_gb300.h"
 #include "gsph_state.cuh"
 #include "kernels.cuh"
+#include "mixed_state.cuh"
 #include "tree.cuh"
 
 using namespace gsph;
@@ -78,6 +79,14 @@ struct gsph_ctx {
   unsigned long long *rec_dir_cnt = nullptr, *rec_dir_hash = nullptr, *rec_cell_cnt = nullptr,
                      *rec_cell_hash = nullptr;
   size_t rec_bytes = 0;
+  // mixed-precision mirrors and the heavy-leaf hand-over list
+  float4 *mp_pos_hi = nullptr, *mp_pos_lo = nullptr, *mp_vel = nullptr, *mp_hyd = nullptr, *mp_aux = nullptr;
+  float4 *mc_geo_hi = nullptr, *mc_geo_lo = nullptr, *mc_com_hi = nullptr, *mc_com_lo = nullptr, *mc_quad = nullptr,
+         *mc_bbmin = nullptr, *mc_bbmax = nullptr, *mc_hbmin = nullptr, *mc_hbmax = nullptr;
+  float* mc_cdist = nullptr;
+  int* heavy_leaves = nullptr;
+  int* heavy_count = nullptr;
+  int max_leaf = 8;
   // timing
   cudaEvent_t ev[5] = {};
   gsph_stats last{};
@@ -206,6 +215,16 @@ int ensure_capacity(gsph_ctx* c, int n) {
     if (rc == GSPH_OK) rc = alloc(c, c->ibox, 6 * ((size_t) 2 * capc + 3));
     if (rc == GSPH_OK) rc = alloc(c, c->counters, 16);
     if (rc == GSPH_OK) rc = alloc(c, c->scratch_out, capn);
+    if (c->cfg.precision == GSPH_PRECISION_MIXED) {
+      float4** pf[5] = {&c->mp_pos_hi, &c->mp_pos_lo, &c->mp_vel, &c->mp_hyd, &c->mp_aux};
+      for (int q = 0; q < 5 && rc == GSPH_OK; q++) rc = alloc(c, *pf[q], capn);
+      float4** cf[9] = {&c->mc_geo_hi, &c->mc_geo_lo, &c->mc_com_hi, &c->mc_com_lo, &c->mc_quad,
+                        &c->mc_bbmin, &c->mc_bbmax, &c->mc_hbmin, &c->mc_hbmax};
+      for (int q = 0; q < 9 && rc == GSPH_OK; q++) rc = alloc(c, *cf[q], capc);
+      if (rc == GSPH_OK) rc = alloc(c, c->mc_cdist, capc);
+    }
+    if (rc == GSPH_OK) rc = alloc(c, c->heavy_leaves, (capc + 1) / 2);
+    if (rc == GSPH_OK) rc = alloc(c, c->heavy_count, 4);
     if (rc != GSPH_OK) { free_all(c); return rc; }
     c->cap = capn;
     c->cap_ncell = capc;
@@ -231,6 +250,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
     while (p2 < maxleaf) p2 <<= 1;
     if (p2 > 32) return fail(c, GSPH_ERR_UNSUPPORTED, "leaf cells hold more than 32 particles");
     c->lpg = 32 / p2;
+    c->max_leaf = maxleaf;
   }
   c->n = n;
   c->ltot = ltot;
@@ -277,6 +297,17 @@ Tree make_tree(gsph_ctx* c) {
   return t;
 }
 
+MixedParticles make_mixed_particles(gsph_ctx* c) {
+  return MixedParticles{c->mp_pos_hi, c->mp_pos_lo, c->mp_vel, c->mp_hyd, c->mp_aux};
+}
+
+MixedCells make_mixed_cells(gsph_ctx* c) {
+  return MixedCells{c->mc_geo_hi, c->mc_geo_lo, c->mc_cdist, c->mc_com_hi, c->mc_com_lo, c->mc_quad,
+                    c->mc_bbmin, c->mc_bbmax, c->mc_hbmin, c->mc_hbmax};
+}
+
+bool mixed(const gsph_ctx* c) { return c->cfg.precision == GSPH_PRECISION_MIXED; }
+
 DeviceCounters make_counters(gsph_ctx* c) {
   DeviceCounters d{};
   d.status = reinterpret_cast<unsigned*>(c->counters);
@@ -300,7 +331,6 @@ int check_config(const gsph_config* cfg, std::string& why) {
   if (cfg->eos != GSPH_EOS_ENERGY_EQN && cfg->eos != GSPH_EOS_ISOTHERMAL) { why = "unknown gas_eos"; return GSPH_ERR_UNSUPPORTED; }
   if (cfg->multipole != GSPH_MONOPOLE && cfg->multipole != GSPH_QUADRUPOLE) { why = "unknown multipole"; return GSPH_ERR_UNSUPPORTED; }
   if (cfg->precision != GSPH_PRECISION_FP64 && cfg->precision != GSPH_PRECISION_MIXED) { why = "unknown precision"; return GSPH_ERR_INVALID; }
-  if (cfg->precision == GSPH_PRECISION_MIXED) { why = "the mixed-precision form is not built into this library"; return GSPH_ERR_UNSUPPORTED; }
   if (cfg->self_gravity && cfg->periodic) { why = "periodic self-gravity needs Ewald sums (not implemented)"; return GSPH_ERR_UNSUPPORTED; }
   if (!cfg->hydro_forces) { why = "hydro_forces = 0 is not implemented"; return GSPH_ERR_UNSUPPORTED; }
   if (!(cfg->h_fac > 0.0) || !(cfg->h_converge > 0.0) || !(cfg->gamma_eos > 1.0) || !(cfg->thetamaxsqd > 0.0)) {
@@ -401,6 +431,12 @@ int read_status(gsph_ctx* c) {
   GSPH_CUDA(cudaStreamSynchronize(c->stream));
   c->last.status = (uint32_t) h[0];
   c->last.launches = c->launches;
+  if (mixed(c)) {
+    int hc[2] = {0, 0};
+    GSPH_CUDA(cudaMemcpy(hc, c->heavy_count + 2, sizeof(hc), cudaMemcpyDeviceToHost));
+    c->last.heavy_density = hc[0];
+    c->last.heavy_forces = hc[1];
+  }
   c->last.density_pairs = (int64_t) h[1];
   c->last.hydro_pairs = (int64_t) h[2];
   c->last.direct_pairs = (int64_t) h[3];
@@ -426,6 +462,10 @@ int do_build(gsph_ctx* c) {
   a.tree = make_tree(c);
   a.thetamaxsqd = c->cfg.thetamaxsqd;
   c->launches += (unsigned) launch_build_tree(a, c->stream);
+  if (mixed(c)) {
+    launch_mixed_prep_build(a.tree, a.p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
+    c->launches += 2;
+  }
   c->have_tree = true;
   c->have_props = c->have_forces = false;
   return check_launch(c, "build tree");
@@ -435,12 +475,25 @@ int do_props(gsph_ctx* c) {
   if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "tree not built");
   const Tree t = make_tree(c);
   const Particles p = make_particles(c);
-  launch_density(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+  HeavyList heavy{c->heavy_leaves, c->heavy_count};
+  if (mixed(c)) {
+    GSPH_CUDA(cudaMemsetAsync(c->heavy_count + 2, 0, 2 * sizeof(int), c->stream));
+    c->launches += (unsigned) launch_density_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
+                                                   make_params(c->cfg), make_counters(c), heavy, c->lpg, c->stream);
+  } else {
+    launch_density(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+    c->launches += 1;
+  }
   int rc = check_launch(c, "density");
   if (rc) return rc;
+  if (mixed(c)) GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
   cudaEventRecord(c->ev[2], c->stream);
   launch_update_hmax(t, p, c->stream);
-  c->launches += 2;
+  c->launches += 1;
+  if (mixed(c)) {
+    launch_mixed_prep_hydro(t, p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
+    c->launches += 2;
+  }
   c->have_props = true;
   return check_launch(c, "update hmax");
 }
@@ -456,9 +509,22 @@ int do_forces(gsph_ctx* c, bool gravity) {
     GSPH_CUDA(cudaMemsetAsync(c->rec_cell_cnt, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
     GSPH_CUDA(cudaMemsetAsync(c->rec_cell_hash, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
   }
-  if (gravity) launch_all_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
-  else launch_hydro_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
-  c->launches += 1;
+  HeavyList heavy{c->heavy_leaves, c->heavy_count};
+  if (mixed(c)) {
+    if (gravity) {
+      c->launches += (unsigned) launch_all_forces_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
+                                                        make_params(c->cfg), make_counters(c), heavy, c->lpg,
+                                                        c->max_leaf, c->stream);
+      GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 3, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    else
+      c->launches += (unsigned) launch_hydro_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
+                                                   make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+  } else {
+    if (gravity) launch_all_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+    else launch_hydro_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+    c->launches += 1;
+  }
   c->have_forces = true;
   return check_launch(c, "forces");
 }

@@ -22,6 +22,8 @@ struct WarpLists {
   int* c;
   int na, nb, nc;     // warp-uniform counts
   int cap;            // capacity of each list
+  // round-robin slicing of list a: keep the k-th emitted entry only if k % mod == sel
+  int mod = 1, sel = 0, emitted_a = 0;
 };
 
 // Returns false when the stack would overflow (status is then the caller's to set).
@@ -56,10 +58,14 @@ __device__ __forceinline__ bool warp_walk(int root, int ltot, const unsigned cha
       stack[top + 2 * r + 1] = node + 1;
     }
     top += 2 * nopen;
-    const unsigned ma = __ballot_sync(kFull, act == kEmitA);
+    const unsigned me = __ballot_sync(kFull, act == kEmitA);
+    bool keep = act == kEmitA;
+    if (L.mod > 1) keep = keep && ((L.emitted_a + __popc(me & lt)) % L.mod == L.sel);
+    L.emitted_a += __popc(me);
+    const unsigned ma = __ballot_sync(kFull, keep);
     const unsigned mb = __ballot_sync(kFull, act == kEmitB);
     const unsigned mc = __ballot_sync(kFull, act == kEmitC);
-    if (act == kEmitA) L.a[L.na + __popc(ma & lt)] = emit_tag(node, act);
+    if (keep) L.a[L.na + __popc(ma & lt)] = emit_tag(node, act);
     if (act == kEmitB) L.b[L.nb + __popc(mb & lt)] = emit_tag(node, act);
     if (act == kEmitC) L.c[L.nc + __popc(mc & lt)] = emit_tag(node, act);
     L.na += __popc(ma);

@@ -30,6 +30,20 @@ __host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long 
   return x ^ (x >> 31);
 }
 
+struct MixedParticles;
+struct MixedCells;
+struct HeavyList;
+
+// mixed-precision form (mixed.cu); each returns the number of kernels it launched
+int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                         const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
+                         int lanes_per_particle, cudaStream_t st);
+int launch_all_forces_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                            const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
+                            int lanes_per_particle, int max_leaf, cudaStream_t st);
+int launch_hydro_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                       const SphParams& prm, const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st);
+
 void launch_density(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
                     int lanes_per_particle, cudaStream_t st);
 void launch_hydro_forces(const Tree& t, const Particles& p, const SphParams& prm,

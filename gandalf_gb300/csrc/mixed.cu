@@ -1,2 +1,930 @@
-// Mixed-precision (fp32 pair arithmetic) form of the per-leaf kernels; see kernels.cuh.
+// Mixed-precision form of the per-leaf kernels: fp32 pair arithmetic, fp64 positions,
+// fp64 h-rho iteration logic, fp64 cell moments (kept as float hi/lo pairs for the
+// pair loops), and interaction lists identical to the fp64 form.
+//
+// Pair formulas are those of the fp64 kernels (density.cu, forces.cu; reference
+// src/GradhSph/GradhSph.cpp:141-690, src/Headers/NeighbourSearch.h:423-449) evaluated in
+// float.  Every membership decision — tree-walk near test and multipole acceptance
+// (src/Tree/Tree.cpp:627-735), SPH-neighbour test (src/Headers/NeighbourManager.h:521) —
+// is made in float with relative margin kMargin and re-made with the reference's fp64
+// arithmetic when the float value lands inside the margin, so the lists are the fp64
+// lists exactly.
+//
+// Load balance: the warp-per-leaf kernels hand a leaf over to a wide kernel when its
+// lists outgrow the warp's shared memory (density: the gather list; forces: the near or
+// direct-sum list).  The wide kernels give such a leaf a whole block — density: 8 warps
+// share the candidates of the cell; forces: one warp per particle.
+#include "gsph_state.cuh"
+#include "gsph_walk.cuh"
 #include "kernels.cuh"
+#include "mixed_state.cuh"
+
+namespace gsph {
+
+namespace {
+
+constexpr float kMargin = 6.103515625e-05f;   // 2^-14 relative
+constexpr int kNodeBits = 25;
+constexpr int kNoShift = 13;
+
+// ---- preparation --------------------------------------------------------------------
+__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
+  hi = __double2float_rn(v);
+  lo = __double2float_rn(v - (double) hi);
+}
+
+__global__ void k_prep_build_particles(Particles p, MixedParticles mp) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < p.n; s += gridDim.x * blockDim.x) {
+    float xh, xl, yh, yl, zh, zl;
+    split2(p.x[s], xh, xl);
+    split2(p.y[s], yh, yl);
+    split2(p.z[s], zh, zl);
+    mp.pos_hi[s] = make_float4(xh, yh, zh, __double2float_rn(p.m[s]));
+    mp.pos_lo[s] = make_float4(xl, yl, zl, 0.0f);
+  }
+}
+
+__global__ void k_prep_build_cells(Tree t, MixedCells mc) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < t.ncell; c += gridDim.x * blockDim.x) {
+    const CellGeom g = t.geom[c];
+    const CellMoment m = t.mom[c];
+    const CellBox b = t.bb[c];
+    float h[3], l[3];
+    for (int k = 0; k < 3; k++) split2(g.rcell[k], h[k], l[k]);
+    mc.geo_hi[c] = make_float4(h[0], h[1], h[2], __double2float_rn(g.rmax));
+    mc.geo_lo[c] = make_float4(l[0], l[1], l[2], __double2float_rn(g.hmax));
+    mc.cdist[c] = __double2float_rn(g.cdistsqd);
+    for (int k = 0; k < 3; k++) split2(m.r[k], h[k], l[k]);
+    mc.com_hi[c] = make_float4(h[0], h[1], h[2], __double2float_rn(m.m));
+    mc.com_lo[c] = make_float4(l[0], l[1], l[2], __double2float_rn(m.q[4]));
+    mc.quad[c] = make_float4(__double2float_rn(m.q[0]), __double2float_rn(m.q[1]), __double2float_rn(m.q[2]),
+                             __double2float_rn(m.q[3]));
+    mc.bbmin[c] = make_float4(__double2float_rd(b.bbmin[0]), __double2float_rd(b.bbmin[1]),
+                              __double2float_rd(b.bbmin[2]), 0.0f);
+    mc.bbmax[c] = make_float4(__double2float_ru(b.bbmax[0]), __double2float_ru(b.bbmax[1]),
+                              __double2float_ru(b.bbmax[2]), 0.0f);
+  }
+}
+
+__global__ void k_prep_hydro_particles(Particles p, MixedParticles mp) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < p.n; s += gridDim.x * blockDim.x) {
+    const double h = p.h[s], rho = p.rho[s];
+    mp.vel[s] = make_float4(__double2float_rn(p.vx[s]), __double2float_rn(p.vy[s]), __double2float_rn(p.vz[s]),
+                            __double2float_rn(h));
+    const double fac = (p.pressure[s] * p.invomega[s]) / (rho * rho);
+    mp.hyd[s] = make_float4(__double2float_rn(1.0 / h), __double2float_rn(fac), __double2float_rn(1.0 / rho),
+                            __double2float_rn(p.sound[s]));
+    mp.aux[s] = make_float4(__double2float_rn(p.hfactor[s]), __double2float_rn(p.zeta[s]),
+                            __double2float_rn(p.hrangesqd[s]), 0.0f);
+  }
+}
+
+__global__ void k_prep_hydro_cells(Tree t, MixedCells mc) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < t.ncell; c += gridDim.x * blockDim.x) {
+    const CellGeom g = t.geom[c];
+    const CellBox hb = t.hbox[c];
+    float4 lo = mc.geo_lo[c];
+    lo.w = __double2float_rn(g.hmax);
+    mc.geo_lo[c] = lo;
+    mc.hbmin[c] = make_float4(__double2float_rd(hb.bbmin[0]), __double2float_rd(hb.bbmin[1]),
+                              __double2float_rd(hb.bbmin[2]), 0.0f);
+    mc.hbmax[c] = make_float4(__double2float_ru(hb.bbmax[0]), __double2float_ru(hb.bbmax[1]),
+                              __double2float_ru(hb.bbmax[2]), 0.0f);
+  }
+}
+
+// ---- helpers ------------------------------------------------------------------------------
+template <int LPG>
+__device__ __forceinline__ double gsum_d(double v) {
+#pragma unroll
+  for (int o = 1; o < LPG; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float fsqrt_pos(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
+
+__device__ __forceinline__ bool fbox_overlap(const float* amin, const float* amax, float4 bmin, float4 bmax) {
+  if (amin[0] > bmax.x || bmin.x > amax[0]) return false;
+  if (amin[1] > bmax.y || bmin.y > amax[1]) return false;
+  if (amin[2] > bmax.z || bmin.z > amax[2]) return false;
+  return true;
+}
+
+__device__ __forceinline__ double shift_of(int code, int k, const SphParams& prm) {
+  const int d = (k == 0 ? code % 3 : (k == 1 ? (code / 3) % 3 : code / 9)) - 1;
+  return d == 0 ? 0.0 : (d > 0 ? prm.boxsize[k] : -prm.boxsize[k]);
+}
+
+// ==========================================================================================
+// Density / h solve, mixed form.
+//
+// One cell's solve, shared by the warp kernel (WARPS = 1) and the wide kernel (WARPS = 8,
+// the cell's candidate leaves dealt round-robin to the warps; per-iteration sums are
+// combined across warps in shared memory, in warp order).
+// ==========================================================================================
+constexpr int kDensStack = 1024;
+constexpr int kDensListNormal = 256;    // leaves a warp handles alone
+constexpr int kDensListWide = 1024;     // per warp in the wide kernel
+constexpr int kMaxAttempts = 256;
+
+struct DensSmem {
+  double part[8][8][3];   // [warp][group][rho, omega, zeta]
+  int flag[8];
+};
+
+template <int LPG, int WARPS>
+__device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, const MixedParticles& mp,
+                                             const MixedCells& mc, const SphParams& prm, const DeviceCounters& cnt,
+                                             int leaf, int* stack, int* list, int list_cap, bool give_up,
+                                             DensSmem* sm) {
+  const int lane = threadIdx.x & 31;
+  const int wib = WARPS > 1 ? (threadIdx.x >> 5) : 0;
+  const int g = lane / LPG, sl = lane % LPG;
+  const int c = t.leaf_cell[leaf];
+  const int first = t.cell_first[c], ncell = t.cell_n[c];
+  const bool mine = g < ncell;
+  const int slot = first + (mine ? g : 0);
+  const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
+  const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
+  const double h_start = p.h[slot];
+  const CellBox bb = t.bb[c];
+  const double hmax0 = t.geom[c].hmax;
+  unsigned long long pairs = 0;
+  bool fail = false, stack_ok = true;
+  double mcheck = 0.0;
+  double h_out = h_start, rho_out = 0.0, om_out = 0.0, zeta_out = 0.0;
+
+  // returns 1 if the cell aborts (some h > hmax_list), 2 if the warp gives up (list too
+  // long for a warp on its own; only when give_up), 0 when solved
+  auto attempt = [&](double hmax_list) -> int {
+    const double hr = __dmul_rn(kKernRange, hmax_list);
+    double gmin[3], gmax[3];
+    for (int k = 0; k < 3; k++) { gmin[k] = __dsub_rn(bb.bbmin[k], hr); gmax[k] = __dadd_rn(bb.bbmax[k], hr); }
+    int nsh[3] = {1, 1, 1}, sh[3][3];
+    for (int k = 0; k < 3; k++) {
+      sh[k][0] = 1;
+      if (prm.periodic) {
+        if (gmax[k] > prm.boxmax[k]) sh[k][nsh[k]++] = 2;
+        if (gmin[k] < prm.boxmin[k]) sh[k][nsh[k]++] = 0;
+      }
+    }
+    WarpLists L{list, list, list, 0, 0, 0, list_cap};
+    L.mod = WARPS; L.sel = wib;
+    bool overflow = false;
+    auto walk_all = [&](auto&& flush) {
+      L.emitted_a = 0;
+      for (int a0 = 0; a0 < nsh[0]; a0++)
+        for (int a1 = 0; a1 < nsh[1]; a1++)
+          for (int a2 = 0; a2 < nsh[2]; a2++) {
+            const int code = sh[0][a0] + 3 * sh[1][a1] + 9 * sh[2][a2];
+            float bmin[3], bmax[3];
+            for (int k = 0; k < 3; k++) {
+              const double s = shift_of(code, k, prm);
+              bmin[k] = __double2float_rd(gmin[k] - s);
+              bmax[k] = __double2float_ru(gmax[k] - s);
+            }
+            auto decide = [&](int node, int level) -> int {
+              if (t.cell_n[node] == 0) return kSkip;
+              if (!fbox_overlap(bmin, bmax, mc.bbmin[node], mc.bbmax[node])) return kSkip;
+              return level == t.ltot ? kEmitA : kOpen;
+            };
+            auto tag = [&](int node, int) { return node | (code << kNodeBits); };
+            stack_ok = stack_ok && warp_walk(0, t.ltot, t.cell_level, stack, kDensStack, L, decide, tag, flush);
+          }
+    };
+    walk_all([&]() { overflow = true; });
+    if (give_up && __any_sync(kFull, overflow)) return 2;
+    const int ncached = L.na;
+
+    double hi = h_start, h_lower = 0.0, h_upper = hmax_list;
+    double rho = 0.0, om = 0.0, zeta = 0.0;
+    int iteration = 0;
+    bool done = !mine, abort_cell = false;
+    double mloc = 0.0;
+    for (;;) {
+      bool any_active = __any_sync(kFull, !done);
+      if (WARPS > 1) any_active = __syncthreads_or(any_active);
+      if (!any_active) break;
+      iteration++;
+      const double invh = 1.0 / hi;
+      const double invhsqd = invh * invh;
+      const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
+      float srho = 0.0f, som = 0.0f, sze = 0.0f;
+      auto consume = [&](int count) {
+        if (done) return;
+        for (int e = 0; e < count; e++) {
+          const int tagv = list[e];
+          const int node = tagv & ((1 << kNodeBits) - 1);
+          const int code = tagv >> kNodeBits;
+          const int f = t.cell_first[node], nn = t.cell_n[node];
+          for (int q = sl; q < nn; q += LPG) {
+            const int j = f + q;
+            float dx, dy, dz;
+            const float4 pjh = mp.pos_hi[j];
+            if (code == kNoShift) {
+              const float4 pjl = mp.pos_lo[j];
+              dx = (pjh.x - pih.x) + (pjl.x - pil.x);
+              dy = (pjh.y - pih.y) + (pjl.y - pil.y);
+              dz = (pjh.z - pih.z) + (pjl.z - pil.z);
+            } else {
+              // periodic image (ghost semantics, fp64): exists only near the boundary
+              const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+              double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+              const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+              bool ok = true;
+              if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
+              if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
+              if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
+              if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
+              if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
+              if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
+              if (!ok) continue;
+              dx = (float) (__dadd_rn(xj, sx) - xi);
+              dy = (float) (__dadd_rn(yj, sy) - yi);
+              dz = (float) (__dadd_rn(zj, sz) - zi);
+            }
+            const float ssqd = (dx * dx + dy * dy + dz * dz) * invhsqd_f;
+            if (ssqd < 4.0f) {
+              const float s = fsqrt_pos(ssqd);
+              const float mj = pjh.w;
+              srho = fmaf(mj, m4f_w0(s), srho);
+              som = fmaf(mj * invh_f, m4f_womega(s), som);
+              sze = fmaf(mj, m4f_wzeta(s), sze);
+              pairs++;
+            }
+          }
+        }
+      };
+      if (!overflow) {
+        consume(ncached);
+      } else {
+        L = WarpLists{list, list, list, 0, 0, 0, list_cap};
+        L.mod = WARPS; L.sel = wib;
+        walk_all([&]() { consume(L.na); });
+        consume(L.na);
+      }
+      double drho = gsum_d<LPG>((double) srho);
+      double dom = gsum_d<LPG>((double) som);
+      double dze = gsum_d<LPG>((double) sze);
+      if (WARPS > 1) {
+        if (sl == 0) { sm->part[wib][g][0] = drho; sm->part[wib][g][1] = dom; sm->part[wib][g][2] = dze; }
+        __syncthreads();
+        drho = dom = dze = 0.0;
+        for (int w = 0; w < WARPS; w++) { drho += sm->part[w][g][0]; dom += sm->part[w][g][1]; dze += sm->part[w][g][2]; }
+        __syncthreads();
+      }
+      if (!done) {
+        const double hfac3 = invh * invh * invh;
+        rho = drho * hfac3;
+        om = dom * hfac3;
+        zeta = dze * invhsqd;
+        const double hrho = prm.h_fac * pow(mi / rho, 1.0 / 3.0);
+        if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
+          done = true;
+        } else {
+          if (iteration < 30) hi = hrho;
+          else if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
+          else if (iteration < 150) {
+            if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
+            hi = 0.5 * (h_lower + h_upper);
+          } else {
+            fail = true;
+            done = true;
+          }
+          if (!done) {
+            mloc = fmax(mloc, hi);
+            if (hi > hmax_list) { abort_cell = true; done = true; }
+            else if (!(hi > h_lower && hi < h_upper)) done = true;
+          }
+        }
+      }
+    }
+    double mw = mloc;
+    for (int o = 16; o > 0; o >>= 1) mw = fmax(mw, __shfl_xor_sync(kFull, mw, o));
+    mcheck = fmax(mcheck, mw);
+    bool any_abort = __any_sync(kFull, abort_cell);
+    if (WARPS > 1) any_abort = __syncthreads_or(any_abort);
+    if (!any_abort && mine) {
+      h_out = fmax(prm.h_fac * pow(mi / rho, 1.0 / 3.0), h_lower);
+      rho_out = rho; om_out = om; zeta_out = zeta;
+    }
+    return any_abort ? 1 : 0;
+  };
+
+  // The reference's hmax sequence with the exact skip-ahead of density.cu.
+  bool solved = false;
+  double hk = __dmul_rn(1.05, hmax0);
+  for (int a = 0; a < kMaxAttempts && !solved; a++) {
+    const int r = attempt(hk);
+    if (r == 2) return false;   // handed over to the wide kernel
+    if (r == 0) {
+      solved = true;
+    } else {
+      int guard = 0;
+      do { hk = __dmul_rn(1.05, hk); } while (hk < mcheck && ++guard < 100000);
+    }
+  }
+  if (lane == 0 && wib == 0) {
+    if (!solved) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
+  }
+  if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
+  if (__any_sync(kFull, fail) && lane == 0) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
+  unsigned long long tot = pairs;
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
+  if (lane == 0) atomicAdd(cnt.density_pairs, tot);
+  if (mine && sl == 0 && wib == 0) {
+    const double hfin = h_out;
+    const double invh = 1.0 / hfin;
+    p.h[slot] = hfin;
+    p.rho[slot] = rho_out;
+    p.hfactor[slot] = invh * invh * invh * invh;
+    p.hrangesqd[slot] = __dmul_rn(__dmul_rn(kKernRangeSqd, hfin), hfin);
+    p.div_v[slot] = 0.0;
+    const double drho = -(1.0 / 3.0) * hfin / rho_out;
+    const double io = 1.0 / (1.0 - drho * om_out);
+    p.invomega[slot] = io;
+    p.zeta[slot] = drho * zeta_out * io;
+    double u = p.u[slot];
+    const double gm1 = prm.gamma_eos - 1.0;
+    if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
+    p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
+    p.pressure[slot] = gm1 * rho_out * u;
+  }
+  return true;
+}
+
+constexpr int kDensWarps = 4;
+
+template <int LPG>
+__global__ void __launch_bounds__(kDensWarps * 32)
+k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
+                HeavyList heavy) {
+  __shared__ int s_stack[kDensWarps][kDensStack];
+  __shared__ int s_list[kDensWarps][kDensListNormal];
+  const int wib = threadIdx.x >> 5;
+  const int leaf = blockIdx.x * kDensWarps + wib;
+  if (leaf >= t.nleaf) return;
+  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack[wib], s_list[wib], kDensListNormal,
+                                       true, nullptr);
+  if (!ok && (threadIdx.x & 31) == 0) {
+    const int k = atomicAdd(heavy.count, 1);
+    heavy.leaves[k] = leaf;
+  }
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(256)
+k_density_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
+                     HeavyList heavy) {
+  extern __shared__ int s_dyn[];
+  int* s_stack = s_dyn;                                   // 8 x kDensStack
+  int* s_list = s_dyn + 8 * kDensStack;                   // 8 x kDensListWide
+  DensSmem* sm = reinterpret_cast<DensSmem*>(s_dyn + 8 * (kDensStack + kDensListWide));
+  const int wib = threadIdx.x >> 5;
+  const int nh = *heavy.count;
+  for (int k = blockIdx.x; k < nh; k += gridDim.x) {
+    density_cell<LPG, 8>(t, p, mp, mc, prm, cnt, heavy.leaves[k], s_stack + wib * kDensStack,
+                         s_list + wib * kDensListWide, kDensListWide, false, sm);
+    __syncthreads();
+  }
+}
+
+// ==========================================================================================
+// Forces, mixed form.
+// ==========================================================================================
+struct AccF {
+  float ah[3], ag[3], gpot, dudt, divv;
+};
+
+struct TargetF {
+  float4 ph, pl, vel, hyd, aux;   // see MixedParticles
+  double x, y, z, hrs;            // fp64 copies for exact membership checks
+  int slot;
+};
+
+__device__ __forceinline__ void load_target_f(const Particles& p, const MixedParticles& mp, int s, TargetF& T) {
+  T.ph = mp.pos_hi[s]; T.pl = mp.pos_lo[s]; T.vel = mp.vel[s]; T.hyd = mp.hyd[s]; T.aux = mp.aux[s];
+  T.x = p.x[s]; T.y = p.y[s]; T.z = p.z[s]; T.hrs = p.hrangesqd[s];
+  T.slot = s;
+}
+
+// SPH neighbour (1), direct term (0): float test with margin, exact fp64 when ambiguous.
+__device__ __forceinline__ int sph_member(const Particles& p, const TargetF& T, int j, float d2, float hrsj,
+                                          const SphParams& prm, unsigned long long& exact) {
+  const float thr = fmaxf(T.aux.z, hrsj);
+  if (d2 < thr * (1.0f - kMargin)) return 1;
+  if (d2 > thr * (1.0f + kMargin)) return 0;
+  exact++;
+  double dx = __dsub_rn(p.x[j], T.x), dy = __dsub_rn(p.y[j], T.y), dz = __dsub_rn(p.z[j], T.z);
+  if (prm.periodic) {
+    // the reference's image: nearest to the leaf centre, then corrected about the particle
+    // (forces.cu k_hydro_fp64); for leaf cells far smaller than the box both give the
+    // nearest image of j about i
+    double* dd[3] = {&dx, &dy, &dz};
+    for (int k = 0; k < 3; k++) {
+      if (*dd[k] > prm.boxhalf[k]) *dd[k] = __dsub_rn(*dd[k], prm.boxsize[k]);
+      else if (*dd[k] < -prm.boxhalf[k]) *dd[k] = __dadd_rn(*dd[k], prm.boxsize[k]);
+    }
+  }
+  const double drsqd = dot3_rn(dx, dy, dz);
+  return (drsqd >= T.hrs && drsqd >= p.hrangesqd[j]) ? 0 : 1;
+}
+
+__device__ __forceinline__ float pair_pressure_f(const SphParams& prm, const TargetF& T, float wi, float wj,
+                                                 float facj, float invrhoj, float soundj, float mj, float dvdr,
+                                                 float& dudt) {
+  float paux = T.hyd.y * wi + facj * wj;
+  if (dvdr < 0.0f) {
+    const float winvrho = 0.25f * (wi + wj) * (T.hyd.z + invrhoj);
+    const float vsignal = T.hyd.w + soundj - (float) (prm.beta_visc * prm.alpha_visc) * dvdr;
+    const float av = (float) prm.alpha_visc * vsignal * dvdr * winvrho;
+    paux -= av;
+    dudt -= 0.5f * mj * av * dvdr;
+  }
+  return paux;
+}
+
+__device__ __forceinline__ void hydro_pair_f(const SphParams& prm, const MixedParticles& mp, const TargetF& T, int j,
+                                             float dx, float dy, float dz, float d2, float mj, AccF& A) {
+  const float4 vj = mp.vel[j], hj = mp.hyd[j], xj = mp.aux[j];
+  const float drmag = fsqrt_pos(d2);
+  float ux = dx, uy = dy, uz = dz;
+  if (drmag > 0.0f) { const float inv = 1.0f / drmag; ux *= inv; uy *= inv; uz *= inv; }
+  const float wi = T.aux.x * m4f_w1(drmag * T.hyd.x);
+  const float wj = xj.x * m4f_w1(drmag * hj.x);
+  const float dvdr = (vj.x - T.vel.x) * ux + (vj.y - T.vel.y) * uy + (vj.z - T.vel.z) * uz;
+  A.divv -= mj * dvdr * wi;
+  const float paux = pair_pressure_f(prm, T, wi, wj, hj.y, hj.z, hj.w, mj, dvdr, A.dudt);
+  A.ah[0] += mj * ux * paux; A.ah[1] += mj * uy * paux; A.ah[2] += mj * uz * paux;
+}
+
+__device__ __forceinline__ void hydro_grav_pair_f(const SphParams& prm, const MixedParticles& mp, const TargetF& T,
+                                                  int j, float dx, float dy, float dz, float d2, float mj, AccF& A) {
+  const float4 vj = mp.vel[j], hj = mp.hyd[j], xj = mp.aux[j];
+  const float r2 = d2 + 1.0e-20f;
+  const float invdrmag = rsqrtf(r2);
+  const float drmag = r2 * invdrmag;
+  const float ux = dx * invdrmag, uy = dy * invdrmag, uz = dz * invdrmag;
+  const float dvdr = (vj.x - T.vel.x) * ux + (vj.y - T.vel.y) * uy + (vj.z - T.vel.z) * uz;
+  const float si = drmag * T.hyd.x, sj = drmag * hj.x;
+  const float wi = T.aux.x * m4f_w1(si);
+  const float wj = xj.x * m4f_w1(sj);
+  const float paux = pair_pressure_f(prm, T, wi, wj, hj.y, hj.z, hj.w, mj, dvdr, A.dudt);
+  A.ah[0] += mj * ux * paux; A.ah[1] += mj * uy * paux; A.ah[2] += mj * uz * paux;
+  const float pg = 0.5f * (T.hyd.x * T.hyd.x * m4f_wgrav(si) + T.aux.y * wi + hj.x * hj.x * m4f_wgrav(sj) + xj.y * wj);
+  A.ag[0] += mj * ux * pg; A.ag[1] += mj * uy * pg; A.ag[2] += mj * uz * pg;
+  A.gpot += 0.5f * mj * (T.hyd.x * m4f_wpot(si) + hj.x * m4f_wpot(sj));
+  A.divv -= mj * dvdr * wi;
+}
+
+__device__ __forceinline__ void direct_term_f(float dx, float dy, float dz, float mj, AccF& A) {
+  const float r2 = dx * dx + dy * dy + dz * dz + 1.0e-20f;
+  const float inv = rsqrtf(r2);
+  const float inv3 = inv * inv * inv * mj;
+  A.ag[0] += dx * inv3; A.ag[1] += dy * inv3; A.ag[2] += dz * inv3;
+  A.gpot += mj * inv;
+}
+
+__device__ __forceinline__ void cell_term_f(const MixedCells& mc, int cc, const TargetF& T, bool quad, AccF& A) {
+  const float4 ch = mc.com_hi[cc], cl = mc.com_lo[cc];
+  const float dx = (T.ph.x - ch.x) + (T.pl.x - cl.x);
+  const float dy = (T.ph.y - ch.y) + (T.pl.y - cl.y);
+  const float dz = (T.ph.z - ch.z) + (T.pl.z - cl.z);
+  const float r2 = dx * dx + dy * dy + dz * dz + 1.0e-20f;
+  const float inv = rsqrtf(r2);
+  const float inv2 = inv * inv;
+  const float mon = ch.w * inv2 * inv;
+  A.ag[0] -= mon * dx; A.ag[1] -= mon * dy; A.ag[2] -= mon * dz;
+  A.gpot += ch.w * inv;
+  if (quad) {
+    const float4 q = mc.quad[cc];
+    const float q4 = cl.w;
+    const float inv5 = inv2 * inv2 * inv;
+    const float qzz = -(q.x + q.z);
+    const float qx = q.x * dx + q.y * dy + q.w * dz;
+    const float qy = q.y * dx + q.z * dy + q4 * dz;
+    const float qz = q.w * dx + q4 * dy + qzz * dz;
+    const float qscalar = qx * dx + qy * dy + qz * dz;
+    const float qfactor = 2.5f * qscalar * inv5 * inv2;
+    A.ag[0] += qx * inv5 - qfactor * dx;
+    A.ag[1] += qy * inv5 - qfactor * dy;
+    A.ag[2] += qz * inv5 - qfactor * dz;
+    A.gpot += 0.5f * qscalar * inv5;
+  }
+}
+
+// Gravity-walk decision (Tree::ComputeGravityInteractionAndGhostList) for one cell:
+// float test with margins, exact fp64 re-test when a float value is inside the margin.
+struct LeafGeo {
+  float4 hi, lo;                // rcell hi/lo, rmax, hmax
+  double rc[3], rmax, hrangemax;  // fp64
+};
+
+__device__ __forceinline__ int grav_decide(const Tree& t, const MixedCells& mc, const LeafGeo& G, int node, int level,
+                                           unsigned long long& exact) {
+  const int on = t.cell_n[node];
+  const float4 gh = mc.geo_hi[node], gl = mc.geo_lo[node];
+  const float dx = (gh.x - G.hi.x) + (gl.x - G.lo.x);
+  const float dy = (gh.y - G.hi.y) + (gl.y - G.lo.y);
+  const float dz = (gh.z - G.hi.z) + (gl.z - G.lo.z);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  const float a1 = gh.w + G.hi.w + 2.0f * G.lo.w;
+  const float a2 = G.hi.w + gh.w + 2.0f * gl.w;
+  const float thr = fmaxf(a1 * a1, a2 * a2);
+  int near;
+  if (d2 < thr * (1.0f - kMargin)) near = 1;
+  else if (d2 > thr * (1.0f + kMargin)) near = 0;
+  else near = -1;
+  const float cd = mc.cdist[node];
+  int open_mac;   // 1: too close (open), 0: accept
+  if (d2 < cd * (1.0f - kMargin)) open_mac = 1;
+  else if (d2 > cd * (1.0f + kMargin)) open_mac = 0;
+  else open_mac = -1;
+  if (near < 0 || (near == 0 && open_mac < 0)) {
+    exact++;
+    const CellGeom o = t.geom[node];
+    const double ddx = __dsub_rn(o.rcell[0], G.rc[0]);
+    const double ddy = __dsub_rn(o.rcell[1], G.rc[1]);
+    const double ddz = __dsub_rn(o.rcell[2], G.rc[2]);
+    const double drsqd = dot3_rn(ddx, ddy, ddz);
+    const double t1 = sq_rn(__dadd_rn(__dadd_rn(o.rmax, G.rmax), G.hrangemax));
+    const double t2 = sq_rn(__dadd_rn(__dadd_rn(G.rmax, o.rmax), __dmul_rn(kKernRange, o.hmax)));
+    near = (drsqd <= t1 || drsqd <= t2) ? 1 : 0;
+    open_mac = drsqd < o.cdistsqd ? 1 : 0;
+  }
+  if (near) {
+    if (level < t.ltot) return kOpen;
+    return on == 0 ? kSkip : kEmitA;
+  }
+  if (on == 0) return kSkip;
+  if (!open_mac) return (level == t.ltot && on == 1) ? kEmitB : kEmitC;
+  return level < t.ltot ? kOpen : kEmitB;
+}
+
+__device__ __forceinline__ void load_leaf_geo(const Tree& t, const MixedCells& mc, int c, LeafGeo& G) {
+  G.hi = mc.geo_hi[c];
+  G.lo = mc.geo_lo[c];
+  const CellGeom g = t.geom[c];
+  for (int k = 0; k < 3; k++) G.rc[k] = g.rcell[k];
+  G.rmax = g.rmax;
+  G.hrangemax = __dmul_rn(kKernRange, g.hmax);
+}
+
+template <int LPG>
+__device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Particles& p, const DeviceCounters& cnt,
+                                                  bool mine, int sl, int slot, const AccF& A, double gpot0,
+                                                  unsigned long long ndir, unsigned long long dhash, bool grav) {
+  double ah[3], ag[3], gp, du, dv;
+  for (int k = 0; k < 3; k++) { ah[k] = gsum_d<LPG>((double) A.ah[k]); ag[k] = gsum_d<LPG>((double) A.ag[k]); }
+  gp = gsum_d<LPG>((double) A.gpot);
+  du = gsum_d<LPG>((double) A.dudt);
+  dv = gsum_d<LPG>((double) A.divv);
+  if (cnt.record) {
+    unsigned long long dc = ndir, dh = dhash;
+    for (int o = 1; o < LPG; o <<= 1) { dc += __shfl_xor_sync(kFull, dc, o); dh += __shfl_xor_sync(kFull, dh, o); }
+    if (mine && sl == 0) { cnt.rec_dir_cnt[slot] = dc; cnt.rec_dir_hash[slot] = dh; }
+  }
+  if (!(mine && sl == 0)) return;
+  const double rho = p.rho[slot];
+  const double invrho = 1.0 / rho;
+  const double divv = dv * invrho;
+  const double P = (prm.gamma_eos - 1.0) * rho * p.u[slot];
+  p.div_v[slot] = divv;
+  p.dudt[slot] = du - P * divv * invrho * p.invomega[slot];
+  p.ax[slot] = ah[0] + ag[0]; p.ay[slot] = ah[1] + ag[1]; p.az[slot] = ah[2] + ag[2];
+  p.agx[slot] = ag[0]; p.agy[slot] = ag[1]; p.agz[slot] = ag[2];
+  p.gpot[slot] = grav ? gpot0 + gp : 0.0;
+}
+
+constexpr int kFStack = 1024;
+constexpr int kFListA = 256, kFListB = 128, kFListC = 1024;         // warp-per-leaf
+constexpr int kWListA = 256, kWListB = 512, kWListC = 1024;         // wide kernel, per warp
+
+// One leaf (or one particle of a leaf) through the gravity walk and all its terms.
+// LPG = lanes per particle; pfirst = first particle of the leaf this warp owns.
+// give_up: hand the leaf over when the near or direct list overflows.
+template <int LPG>
+__device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& p, const MixedParticles& mp,
+                                                const MixedCells& mc, const SphParams& prm, const DeviceCounters& cnt,
+                                                int leaf, int pfirst, int* stack, int* la, int* lb, int* lc, int capa,
+                                                int capb, int capc, bool give_up) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane / LPG, sl = lane % LPG;
+  const int c = t.leaf_cell[leaf];
+  const int first = t.cell_first[c], ncell = t.cell_n[c];
+  const int pidx = pfirst + g;
+  const bool mine = pidx < ncell;
+  const int slot = first + (mine ? pidx : 0);
+  TargetF T;
+  load_target_f(p, mp, slot, T);
+  LeafGeo G;
+  load_leaf_geo(t, mc, c, G);
+  const bool quad = prm.multipole == 1;
+  AccF A = {};
+  unsigned long long nsph = 0, ndir = 0, ncellp = 0, exact = 0, dhash = 0, chash = 0, ccount = 0;
+  bool gave_up = false;
+  // lists have separate capacities: WarpLists keeps one, so the flush test is done here
+  WarpLists L{la, lb, lc, 0, 0, 0, 1 << 30};
+  auto consume_c = [&]() {
+    if (!mine) return;
+    for (int e = sl; e < L.nc; e += LPG) {
+      cell_term_f(mc, L.c[e], T, quad, A);
+      ncellp++;
+      if (cnt.record && g == 0) { chash += mix64((unsigned long long) L.c[e]); ccount++; }
+    }
+  };
+  auto consume_ab = [&]() {
+    if (!mine) return;
+    for (int e = 0; e < L.na; e++) {
+      const int node = L.a[e];
+      const int f = t.cell_first[node], nn = t.cell_n[node];
+      for (int q = sl; q < nn; q += LPG) {
+        const int j = f + q;
+        const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+        const float dx = (pjh.x - T.ph.x) + (pjl.x - T.pl.x);
+        const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
+        const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (sph_member(p, T, j, d2, mp.aux[j].z, prm, exact)) {
+          hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
+          nsph++;
+          if (cnt.record) {
+            const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
+            if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
+          }
+        } else {
+          direct_term_f(dx, dy, dz, pjh.w, A);
+          ndir++;
+          if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
+        }
+      }
+    }
+    for (int e = 0; e < L.nb; e++) {
+      const int node = L.b[e];
+      const int f = t.cell_first[node], nn = t.cell_n[node];
+      for (int q = sl; q < nn; q += LPG) {
+        const int j = f + q;
+        const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+        const float dx = (pjh.x - T.ph.x) + (pjl.x - T.pl.x);
+        const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
+        const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
+        direct_term_f(dx, dy, dz, pjh.w, A);
+        ndir++;
+        if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
+      }
+    }
+  };
+  // the walk, with per-list flushing
+  const unsigned lt = (1u << lane) - 1u;
+  if (lane == 0) stack[0] = 0;
+  int top = 1;
+  bool stack_ok = true;
+  __syncwarp();
+  while (top > 0) {
+    const int take = top < 32 ? top : 32;
+    int node = -1;
+    if (lane < take) node = stack[top - 1 - lane];
+    top -= take;
+    __syncwarp();
+    int act = kSkip, level = 0;
+    if (node >= 0) { level = t.cell_level[node]; act = grav_decide(t, mc, G, node, level, exact); }
+    const unsigned mo = __ballot_sync(kFull, act == kOpen);
+    const int nopen = __popc(mo);
+    if (top + 2 * nopen > kFStack) { stack_ok = false; break; }
+    if (act == kOpen) {
+      const int r = __popc(mo & lt);
+      stack[top + 2 * r] = c2_of(node, level, t.ltot);
+      stack[top + 2 * r + 1] = node + 1;
+    }
+    top += 2 * nopen;
+    const unsigned ma = __ballot_sync(kFull, act == kEmitA);
+    const unsigned mb = __ballot_sync(kFull, act == kEmitB);
+    const unsigned mcm = __ballot_sync(kFull, act == kEmitC);
+    if (act == kEmitA) L.a[L.na + __popc(ma & lt)] = node;
+    if (act == kEmitB) L.b[L.nb + __popc(mb & lt)] = node;
+    if (act == kEmitC) L.c[L.nc + __popc(mcm & lt)] = node;
+    L.na += __popc(ma); L.nb += __popc(mb); L.nc += __popc(mcm);
+    __syncwarp();
+    if (L.nc > capc - 32) { consume_c(); L.nc = 0; __syncwarp(); }
+    if (L.na > capa - 32 || L.nb > capb - 32) {
+      if (give_up) { gave_up = true; break; }
+      consume_ab(); L.na = 0; L.nb = 0; __syncwarp();
+    }
+  }
+  if (gave_up) return false;
+  consume_ab();
+  consume_c();
+  if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
+  unsigned long long a1 = nsph, a2 = ndir, a3 = ncellp, a4 = exact;
+  for (int o = 16; o > 0; o >>= 1) {
+    a1 += __shfl_xor_sync(kFull, a1, o); a2 += __shfl_xor_sync(kFull, a2, o);
+    a3 += __shfl_xor_sync(kFull, a3, o); a4 += __shfl_xor_sync(kFull, a4, o);
+  }
+  if (lane == 0) {
+    atomicAdd(cnt.hydro_pairs, a1); atomicAdd(cnt.direct_pairs, a2);
+    atomicAdd(cnt.cell_pairs, a3); atomicAdd(cnt.exact_checks, a4);
+  }
+  if (cnt.record && pfirst == 0) {
+    unsigned long long cc = ccount, ch = chash;
+    for (int o = 16; o > 0; o >>= 1) { cc += __shfl_xor_sync(kFull, cc, o); ch += __shfl_xor_sync(kFull, ch, o); }
+    if (lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
+  }
+  const double gpot0 = (p.m[slot] / p.h[slot]) * m4_wpot(0.0);
+  finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, gpot0, ndir, dhash, true);
+  return true;
+}
+
+constexpr int kForceWarps = 4;
+
+template <int LPG>
+__global__ void __launch_bounds__(kForceWarps * 32)
+k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
+                   HeavyList heavy) {
+  __shared__ int s_stack[kForceWarps][kFStack];
+  __shared__ int s_a[kForceWarps][kFListA];
+  __shared__ int s_b[kForceWarps][kFListB];
+  __shared__ int s_c[kForceWarps][kFListC];
+  const int wib = threadIdx.x >> 5;
+  const int leaf = blockIdx.x * kForceWarps + wib;
+  if (leaf >= t.nleaf) return;
+  const bool ok = all_forces_leaf<LPG>(t, p, mp, mc, prm, cnt, leaf, 0, s_stack[wib], s_a[wib], s_b[wib], s_c[wib],
+                                       kFListA, kFListB, kFListC, true);
+  if (!ok && (threadIdx.x & 31) == 0) {
+    const int k = atomicAdd(heavy.count, 1);
+    heavy.leaves[k] = leaf;
+  }
+}
+
+// One warp per particle of each heavy leaf (8 warps per block for Nleafmax <= 8).
+__global__ void __launch_bounds__(256)
+k_all_forces_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
+                        HeavyList heavy, int warps_per_leaf) {
+  extern __shared__ int s_dyn[];
+  const int wib = threadIdx.x >> 5;
+  const int per = kFStack + kWListA + kWListB + kWListC;
+  int* base = s_dyn + wib * per;
+  const int nh = *heavy.count;
+  const int total = nh * warps_per_leaf;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int item = blockIdx.x * (blockDim.x >> 5) + wib; item < total; item += nw) {
+    const int leaf = heavy.leaves[item / warps_per_leaf];
+    const int pf = item % warps_per_leaf;
+    for (int q = pf; q < 32; q += warps_per_leaf) {
+      if (q >= t.cell_n[t.leaf_cell[leaf]]) break;
+      all_forces_leaf<32>(t, p, mp, mc, prm, cnt, leaf, q, base, base + kFStack, base + kFStack + kWListA,
+                          base + kFStack + kWListA + kWListB, kWListA, kWListB, kWListC, false);
+    }
+  }
+}
+
+// ---- hydro only (periodic or open), warp per leaf ----------------------------------------
+template <int LPG>
+__global__ void __launch_bounds__(kForceWarps * 32)
+k_hydro_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt) {
+  __shared__ int s_stack[kForceWarps][kFStack];
+  __shared__ int s_list[kForceWarps][512];
+  const int wib = threadIdx.x >> 5;
+  const int leaf = blockIdx.x * kForceWarps + wib;
+  if (leaf >= t.nleaf) return;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / LPG, sl = lane % LPG;
+  const int c = t.leaf_cell[leaf];
+  const int first = t.cell_first[c], ncell = t.cell_n[c];
+  const bool mine = g < ncell;
+  const int slot = first + (mine ? g : 0);
+  TargetF T;
+  load_target_f(p, mp, slot, T);
+  AccF A = {};
+  unsigned long long npairs = 0, exact = 0;
+  WarpLists L{s_list[wib], s_list[wib], s_list[wib], 0, 0, 0, 512};
+  const float4 bmin_f = mc.bbmin[c], bmax_f = mc.bbmax[c], hmin_f = mc.hbmin[c], hmax_f = mc.hbmax[c];
+  const float half[3] = {(float) prm.boxhalf[0], (float) prm.boxhalf[1], (float) prm.boxhalf[2]};
+  const float size[3] = {(float) prm.boxsize[0], (float) prm.boxsize[1], (float) prm.boxsize[2]};
+  // Superset of the reference's PeriodicBoxOverlap: along each axis the boxes overlap
+  // for some periodic image of the second (outward-rounded float boxes, widened by a
+  // margin of the box size); membership is decided per pair afterwards.
+  auto pbox = [&](float4 amin, float4 amax, float4 bmin, float4 bmax) -> bool {
+    const float a0[3] = {amin.x, amin.y, amin.z}, a1[3] = {amax.x, amax.y, amax.z};
+    const float b0[3] = {bmin.x, bmin.y, bmin.z}, b1[3] = {bmax.x, bmax.y, bmax.z};
+    for (int k = 0; k < 3; k++) {
+      bool ok = !(a0[k] > b1[k] || b0[k] > a1[k]);
+      if (!ok && prm.periodic) {
+        const float slack = size[k] * kMargin;
+        for (int sgn = -1; sgn <= 1 && !ok; sgn += 2) {
+          const float lo = b0[k] + sgn * size[k] - slack, hi = b1[k] + sgn * size[k] + slack;
+          ok = !(a0[k] > hi || lo > a1[k]);
+        }
+      }
+      if (!ok) return false;
+    }
+    return true;
+  };
+  auto decide = [&](int node, int level) -> int {
+    if (t.cell_n[node] == 0) return kSkip;
+    if (!(pbox(bmin_f, bmax_f, mc.hbmin[node], mc.hbmax[node]) || pbox(hmin_f, hmax_f, mc.bbmin[node], mc.bbmax[node])))
+      return kSkip;
+    return level == t.ltot ? kEmitA : kOpen;
+  };
+  auto tag = [](int node, int) { return node; };
+  auto consume = [&]() {
+    if (!mine) return;
+    for (int e = 0; e < L.na; e++) {
+      const int node = L.a[e];
+      const int f = t.cell_first[node], nn = t.cell_n[node];
+      for (int q = sl; q < nn; q += LPG) {
+        const int j = f + q;
+        const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+        float d[3] = {(pjh.x - T.ph.x) + (pjl.x - T.pl.x), (pjh.y - T.ph.y) + (pjl.y - T.pl.y),
+                      (pjh.z - T.ph.z) + (pjl.z - T.pl.z)};
+        if (prm.periodic) {
+          const double xj[3] = {p.x[j], p.y[j], p.z[j]}, xi[3] = {T.x, T.y, T.z};
+          for (int k = 0; k < 3; k++) {
+            if (fabsf(d[k]) > half[k] * 0.5f) {
+              double dd = xj[k] - xi[k];
+              if (dd > prm.boxhalf[k]) dd -= prm.boxsize[k];
+              else if (dd < -prm.boxhalf[k]) dd += prm.boxsize[k];
+              d[k] = (float) dd;
+            }
+          }
+        }
+        const float d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (!sph_member(p, T, j, d2, mp.aux[j].z, prm, exact)) continue;
+        hydro_pair_f(prm, mp, T, j, d[0], d[1], d[2], d2, pjh.w, A);
+        npairs++;
+        if (cnt.record) {
+          const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
+          if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
+        }
+      }
+    }
+  };
+  const bool ok = warp_walk(0, t.ltot, t.cell_level, s_stack[wib], kFStack, L, decide, tag, consume);
+  consume();
+  if (!ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
+  unsigned long long a1 = npairs, a4 = exact;
+  for (int o = 16; o > 0; o >>= 1) { a1 += __shfl_xor_sync(kFull, a1, o); a4 += __shfl_xor_sync(kFull, a4, o); }
+  if (lane == 0) { atomicAdd(cnt.hydro_pairs, a1); atomicAdd(cnt.exact_checks, a4); }
+  finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, 0.0, 0, 0, false);
+}
+
+int grid1(int n) { return n < 1 ? 1 : (n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8; }
+
+}  // namespace
+
+void launch_mixed_prep_build(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                             cudaStream_t st) {
+  k_prep_build_particles<<<grid1(p.n), 256, 0, st>>>(p, mp);
+  k_prep_build_cells<<<grid1(t.ncell), 256, 0, st>>>(t, mc);
+}
+
+void launch_mixed_prep_hydro(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                             cudaStream_t st) {
+  k_prep_hydro_particles<<<grid1(p.n), 256, 0, st>>>(p, mp);
+  k_prep_hydro_cells<<<grid1(t.ncell), 256, 0, st>>>(t, mc);
+}
+
+#define GSPH_MIXED_LPG(KERNEL, LPG, GRID, BLOCK, SMEM, ...)                               \
+  switch (LPG) {                                                                         \
+    case 32: KERNEL<32><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;                  \
+    case 16: KERNEL<16><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;                  \
+    case 8: KERNEL<8><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;                    \
+    case 4: KERNEL<4><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;                    \
+    case 2: KERNEL<2><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;                    \
+    default: KERNEL<1><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;                   \
+  }
+
+int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                         const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
+                         int lanes_per_particle, cudaStream_t st) {
+  cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
+  const int blocks = (t.nleaf + kDensWarps - 1) / kDensWarps;
+  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, blocks, kDensWarps * 32, 0, t, p, mp, mc, prm, cnt, heavy)
+  const size_t smem = sizeof(int) * 8 * (kDensStack + kDensListWide) + sizeof(DensSmem);
+  for (auto f : {k_density_mixed_wide<1>, k_density_mixed_wide<2>, k_density_mixed_wide<4>,
+                 k_density_mixed_wide<8>, k_density_mixed_wide<16>, k_density_mixed_wide<32>})
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  GSPH_MIXED_LPG(k_density_mixed_wide, lanes_per_particle, 152 * 2, 256, smem, t, p, mp, mc, prm, cnt, heavy)
+  return 2;
+}
+
+int launch_all_forces_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                            const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
+                            int lanes_per_particle, int max_leaf, cudaStream_t st) {
+  cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
+  const int blocks = (t.nleaf + kForceWarps - 1) / kForceWarps;
+  GSPH_MIXED_LPG(k_all_forces_mixed, lanes_per_particle, blocks, kForceWarps * 32, 0, t, p, mp, mc, prm, cnt, heavy)
+  const size_t smem = sizeof(int) * 8 * (kFStack + kWListA + kWListB + kWListC);
+  cudaFuncSetAttribute(k_all_forces_mixed_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  const int wpl = max_leaf < 8 ? max_leaf : 8;
+  k_all_forces_mixed_wide<<<152 * 2, 256, smem, st>>>(t, p, mp, mc, prm, cnt, heavy, wpl < 1 ? 1 : wpl);
+  return 2;
+}
+
+int launch_hydro_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
+                       const SphParams& prm, const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st) {
+  const int blocks = (t.nleaf + kForceWarps - 1) / kForceWarps;
+  GSPH_MIXED_LPG(k_hydro_mixed, lanes_per_particle, blocks, kForceWarps * 32, 0, t, p, mp, mc, prm, cnt)
+  return 1;
+}
+
+}  // namespace gsph

@@ -96,6 +96,8 @@ typedef struct gsph_stats {
   int64_t direct_pairs;    /* Newtonian particle-particle terms */
   int64_t cell_pairs;      /* particle-multipole terms */
   int64_t exact_checks;    /* mixed form: membership tests re-resolved in fp64 */
+  int64_t heavy_density;   /* leaf cells the h solve handed to its wide kernel */
+  int64_t heavy_forces;    /* leaf cells the force pass handed to its wide kernel */
   uint32_t status;
   uint32_t launches;       /* kernels this library launched for the last step */
   double ms_build, ms_density, ms_hmax, ms_forces, ms_total;

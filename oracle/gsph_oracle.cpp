@@ -773,6 +773,10 @@ struct Oracle {
     }
   }
 
+  // Set when the h solve's results are supplied by the caller (force pass only).
+  bool given = false;
+  std::vector<double> g_h, g_rho, g_invomega, g_zeta, g_pressure, g_sound;
+
   int run(int nthreads) {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -789,8 +793,20 @@ struct Oracle {
       dir_count.assign(n, 0); dir_hash.assign(n, 0);
       cell_count.assign(leaves.size(), 0); cell_hash.assign(leaves.size(), 0);
     }
-    const int st = density();
-    if (st != 0) return st;
+    if (given) {
+      // GradhSph::ComputeH's outputs taken as given (GradhSph.cpp:262-317)
+      for (int64_t i = 0; i < n; i++) {
+        h[i] = g_h[i]; rho[i] = g_rho[i]; invomega[i] = g_invomega[i]; zeta[i] = g_zeta[i];
+        pressure[i] = g_pressure[i]; sound[i] = g_sound[i];
+        const double invh = 1.0 / h[i];
+        hfactor[i] = std::pow(invh, 3 + 1);
+        hrangesqd[i] = kKernRangeSqd * h[i] * h[i];
+        if (p.eos == 1) u[i] = p.temp0 / (p.gamma_eos - 1.0) / p.mu_bar;
+      }
+    } else {
+      const int st = density();
+      if (st != 0) return st;
+    }
     update_hmax(0);
     if (p.self_gravity) all_forces(); else hydro_forces();
     return 0;
@@ -803,6 +819,10 @@ struct Oracle {
 extern "C" {
 
 enum { GSPH_ORACLE_NOUT = 20 };
+
+int gsph_oracle_run(void* handle, int64_t n, const double* x, const double* y, const double* z,
+                    const double* vx, const double* vy, const double* vz, const double* m,
+                    const double* u, const double* h, int want_lists, int nthreads);
 
 void* gsph_oracle_create(const Params* p) {
   Oracle* o = new Oracle();
@@ -826,6 +846,22 @@ int gsph_oracle_run(void* handle, int64_t n, const double* x, const double* y, c
   o->want_summary = want_lists == 2;
   o->n_density_pairs = o->n_hydro_pairs = o->n_direct_pairs = o->n_cell_pairs = 0;
   return o->run(nthreads);
+}
+
+// Force pass only: the h solve's results (h rho invomega zeta pressure sound, input
+// order) are supplied instead of computed; the tree is built from the input h as usual.
+int gsph_oracle_run_given(void* handle, int64_t n, const double* x, const double* y, const double* z,
+                          const double* vx, const double* vy, const double* vz, const double* m,
+                          const double* u, const double* h, const double* hs, const double* rho,
+                          const double* invomega, const double* zeta, const double* pressure,
+                          const double* sound, int want_lists, int nthreads) {
+  Oracle* o = static_cast<Oracle*>(handle);
+  o->given = true;
+  o->g_h.assign(hs, hs + n); o->g_rho.assign(rho, rho + n); o->g_invomega.assign(invomega, invomega + n);
+  o->g_zeta.assign(zeta, zeta + n); o->g_pressure.assign(pressure, pressure + n); o->g_sound.assign(sound, sound + n);
+  const int st = gsph_oracle_run(handle, n, x, y, z, vx, vy, vz, m, u, h, want_lists, nthreads);
+  o->given = false;
+  return st;
 }
 
 // Per-particle results, n x 20 doubles in the order of oracle/refio.py PARTICLE_FIELDS.

@@ -85,6 +85,8 @@ def _load():
         lib.gsph_oracle_summary.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint64),
                                             ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
                                             ctypes.POINTER(ctypes.c_uint64)]
+        lib.gsph_oracle_run_given.restype = i32
+        lib.gsph_oracle_run_given.argtypes = [vp, i64] + [dp] * 15 + [i32, i32]
         lib.gsph_oracle_nleaf.restype = i32
         lib.gsph_oracle_nleaf.argtypes = [vp]
         _lib = lib
@@ -111,11 +113,14 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0, summary: bool = False) -> dict:
+def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0, summary: bool = False,
+        given: dict | None = None) -> dict:
     """One step of the restated algorithm; same result layout as oracle/refio.run.
 
     lists: full interaction lists (small N only); summary: SPH lists plus (count, hash)
-    of direct partners per particle and multipole cells per leaf.
+    of direct partners per particle and multipole cells per leaf.  given: the h solve's
+    results (h rho invomega zeta pressure sound, input order) to use instead of solving
+    — the force pass and its lists for exactly those smoothing lengths.
     """
     lib = _load()
     prm = make_params(params)
@@ -125,7 +130,13 @@ def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0, summary
                 for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")]
         n = len(arrs[0])
         mode = 1 if lists else (2 if summary else 0)
-        st = lib.gsph_oracle_run(h, n, *[_ptr(a) for a in arrs], mode, int(nthreads))
+        if given is None:
+            st = lib.gsph_oracle_run(h, n, *[_ptr(a) for a in arrs], mode, int(nthreads))
+        else:
+            gv = [np.ascontiguousarray(given[k], dtype=np.float64)
+                  for k in ("h", "rho", "invomega", "zeta", "pressure", "sound")]
+            st = lib.gsph_oracle_run_given(h, n, *[_ptr(a) for a in arrs], *[_ptr(a) for a in gv], mode,
+                                           int(nthreads))
         if st != 0:
             raise RuntimeError(f"oracle step failed with status {st}")
         out = np.empty((n, len(PARTICLE_FIELDS)))

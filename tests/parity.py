@@ -72,3 +72,56 @@ def csr_lists(off, ids):
 def same_lists(a, b):
     bad = [i for i, (x, y) in enumerate(zip(a, b)) if not np.array_equal(np.sort(x), np.sort(y))]
     return bad
+
+
+def mixed_errors(got: dict, ref: dict) -> dict:
+    """Relative errors of the mixed form against fp64: per-particle relative error of
+    each scalar (rms and max), and for the acceleration vectors |Δa|/|a| per particle
+    plus the normalised rms sqrt(sum |Δa|^2 / sum |a|^2)."""
+    out = {}
+    for k in ("h", "rho", "pressure", "invomega"):
+        if k not in got:
+            continue
+        e = np.abs(got[k] - ref[k]) / np.abs(ref[k])
+        out[k] = (float(np.sqrt(np.mean(e * e))), float(e.max()))
+    for name, ks in (("a", ("ax", "ay", "az")), ("ag", ("agx", "agy", "agz"))):
+        if ks[0] not in got:
+            continue
+        A = np.stack([got[k] for k in ks], 1)
+        B = np.stack([ref[k] for k in ks], 1)
+        nb = np.linalg.norm(B, axis=1)
+        if not np.any(nb > 0):
+            continue
+        d = np.linalg.norm(A - B, axis=1)
+        e = d / np.maximum(nb, 1e-300)
+        out[name] = (float(np.sqrt(np.mean(e * e))), float(e.max()))
+        out[name + "_nrms"] = float(np.sqrt(np.sum(d * d) / np.sum(nb * nb)))
+    for k in ("dudt", "gpot", "div_v"):
+        if k not in got:
+            continue
+        b = ref[k]
+        if not np.any(b != 0):
+            continue
+        e = np.abs(got[k] - b) / (np.abs(b) + 1e-3 * np.sqrt(np.mean(b * b)))
+        out[k] = (float(np.sqrt(np.mean(e * e))), float(e.max()))
+    return out
+
+
+# Mixed form against fp64: rms and max of the relative errors (mixed_errors).
+MIXED_TOL = {"h": (1e-5, 1e-2), "rho": (1e-4, 1e-2), "pressure": (1e-4, 1e-2), "invomega": (1e-4, 1e-2),
+             "a": (1e-4, 5e-2), "ag": (1e-4, 5e-2), "a_nrms": 1e-4, "ag_nrms": 1e-4,
+             "dudt": (1e-3, 1e-1), "gpot": (1e-5, 1e-3), "div_v": (1e-3, 1e-1)}
+
+
+def check_mixed(got: dict, ref: dict):
+    errs = mixed_errors(got, ref)
+    bad = []
+    for k, v in errs.items():
+        tol = MIXED_TOL[k]
+        if isinstance(v, tuple):
+            if not (v[0] <= tol[0] and v[1] <= tol[1]):
+                bad.append(f"{k}: rms {v[0]:.2e} max {v[1]:.2e} > {tol}")
+        elif not v <= tol:
+            bad.append(f"{k}: {v:.2e} > {tol}")
+    assert not bad, "; ".join(bad) + f" | all: {errs}"
+    return errs
