@@ -212,20 +212,24 @@ def run_form(c, params, precision, steps, warmup, flush):
 
 
 def run_e2e(c, params, precision, steps, warmup):
+    """Records in, step, records out through the C ABI; separate pinned input and output
+    record buffers so every step starts from the same inputs, as the device-resident
+    loop does."""
     from gandalf_gb300.sph import GradhSphTree
     import torch
     buf, rec, off = gradh_records(c)
+    obuf, orec, _ = gradh_records(c)
     t = GradhSphTree(params, precision=precision, device=torch.cuda.current_device())
     for _ in range(max(1, warmup)):
         t.set_particles_aos(rec, off)
         t.step()
-        t.get_particles_aos(rec, off)
+        t.get_particles_aos(orec, off)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         t.set_particles_aos(rec, off)
         t.step()
-        t.get_particles_aos(rec, off)
+        t.get_particles_aos(orec, off)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     t.close()

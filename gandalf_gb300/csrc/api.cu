@@ -479,7 +479,8 @@ int do_props(gsph_ctx* c) {
   if (mixed(c)) {
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count + 2, 0, 2 * sizeof(int), c->stream));
     c->launches += (unsigned) launch_density_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
-                                                   make_params(c->cfg), make_counters(c), heavy, c->lpg, c->stream);
+                                                   make_params(c->cfg), make_counters(c), heavy, c->lpg, c->max_leaf,
+                                                   c->stream);
   } else {
     launch_density(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
     c->launches += 1;

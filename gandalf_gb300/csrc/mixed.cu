@@ -135,8 +135,10 @@ struct DensSmem {
 template <int LPG, int WARPS>
 __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, const MixedParticles& mp,
                                              const MixedCells& mc, const SphParams& prm, const DeviceCounters& cnt,
-                                             int leaf, int* stack, int* list, int list_cap, bool give_up,
-                                             DensSmem* sm) {
+                                             int leaf, int* stack, int* list, int list_cap, float2* compact,
+                                             int kcap, bool give_up, DensSmem* sm) {
+  // WARPS > 1: the block's warps share the cell, each keeping every WARPS-th leaf of
+  // the gather list; per-iteration sums are added across warps in warp order.
   const int lane = threadIdx.x & 31;
   const int wib = WARPS > 1 ? (threadIdx.x >> 5) : 0;
   const int g = lane / LPG, sl = lane % LPG;
@@ -196,7 +198,70 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     if (give_up && __any_sync(kFull, overflow)) return 2;
     const int ncached = L.na;
 
+    // The candidate's separation from this particle in float (false: that periodic
+    // image does not exist, ghost semantics as in the fp64 form).
+    auto cand = [&](int j, int code, float& d2, float& mj) -> bool {
+      float dx, dy, dz;
+      const float4 pjh = mp.pos_hi[j];
+      mj = pjh.w;
+      if (code == kNoShift) {
+        const float4 pjl = mp.pos_lo[j];
+        dx = (pjh.x - pih.x) + (pjl.x - pil.x);
+        dy = (pjh.y - pih.y) + (pjl.y - pil.y);
+        dz = (pjh.z - pih.z) + (pjl.z - pil.z);
+      } else {
+        const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+        const double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+        const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+        bool ok = true;
+        if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
+        if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
+        if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
+        if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
+        if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
+        if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
+        if (!ok) return false;
+        dx = (float) (__dadd_rn(xj, sx) - xi);
+        dy = (float) (__dadd_rn(yj, sy) - yi);
+        dz = (float) (__dadd_rn(zj, sz) - zi);
+      }
+      d2 = dx * dx + dy * dy + dz * dz;
+      return true;
+    };
+
+    // Per-particle compact lists of (d^2, m) for the pairs inside 2 hmax_list (the
+    // reference's own pre-filter, GradhSphTree.cpp:205-219), built once per attempt; a
+    // particle whose list does not fit loops over the candidates instead.
+    const unsigned gmask = LPG == 32 ? kFull : (((1u << LPG) - 1u) << (g * LPG));
+    const unsigned ltm = (1u << lane) - 1u;
+    float2* clist = compact + g * kcap;
+    int ccount = 0;
+    const float lim2 = (float) (kKernRangeSqd * hmax_list * hmax_list) * (1.0f + kMargin);
+    if (!overflow) {
+      for (int e = 0; e < ncached; e++) {
+        const int tagv = list[e];
+        const int node = tagv & ((1 << kNodeBits) - 1);
+        const int code = tagv >> kNodeBits;
+        const int f = t.cell_first[node], nn = t.cell_n[node];
+        for (int q0 = 0; q0 < nn; q0 += LPG) {
+          const int q = q0 + sl;
+          float d2 = 0.0f, mj = 0.0f;
+          bool keep = false;
+          if (mine && q < nn) keep = cand(f + q, code, d2, mj) && d2 <= lim2;
+          const unsigned b = __ballot_sync(kFull, keep);
+          if (keep) {
+            const int pos = ccount + __popc(b & gmask & ltm);
+            if (pos < kcap) clist[pos] = make_float2(d2, mj);
+          }
+          ccount += __popc(b & gmask);
+        }
+      }
+    }
+    const bool use_compact = !overflow && ccount <= kcap;
+
     double hi = h_start, h_lower = 0.0, h_upper = hmax_list;
+    double invh = 1.0 / hi, hrho_last = hi;
+    const double inv_m = 1.0 / mi, inv_hfac = 1.0 / prm.h_fac;
     double rho = 0.0, om = 0.0, zeta = 0.0;
     int iteration = 0;
     bool done = !mine, abort_cell = false;
@@ -206,10 +271,19 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
       if (WARPS > 1) any_active = __syncthreads_or(any_active);
       if (!any_active) break;
       iteration++;
-      const double invh = 1.0 / hi;
       const double invhsqd = invh * invh;
       const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
       float srho = 0.0f, som = 0.0f, sze = 0.0f;
+      auto add = [&](float d2, float mj) {
+        const float ssqd = d2 * invhsqd_f;
+        if (ssqd < 4.0f) {
+          const float s = fsqrt_pos(ssqd);
+          srho = fmaf(mj, m4f_w0(s), srho);
+          som = fmaf(mj * invh_f, m4f_womega(s), som);
+          sze = fmaf(mj, m4f_wzeta(s), sze);
+          pairs++;
+        }
+      };
       auto consume = [&](int count) {
         if (done) return;
         for (int e = 0; e < count; e++) {
@@ -218,44 +292,14 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
           const int code = tagv >> kNodeBits;
           const int f = t.cell_first[node], nn = t.cell_n[node];
           for (int q = sl; q < nn; q += LPG) {
-            const int j = f + q;
-            float dx, dy, dz;
-            const float4 pjh = mp.pos_hi[j];
-            if (code == kNoShift) {
-              const float4 pjl = mp.pos_lo[j];
-              dx = (pjh.x - pih.x) + (pjl.x - pil.x);
-              dy = (pjh.y - pih.y) + (pjl.y - pil.y);
-              dz = (pjh.z - pih.z) + (pjl.z - pil.z);
-            } else {
-              // periodic image (ghost semantics, fp64): exists only near the boundary
-              const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
-              double xj = p.x[j], yj = p.y[j], zj = p.z[j];
-              const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
-              bool ok = true;
-              if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
-              if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
-              if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
-              if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
-              if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
-              if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
-              if (!ok) continue;
-              dx = (float) (__dadd_rn(xj, sx) - xi);
-              dy = (float) (__dadd_rn(yj, sy) - yi);
-              dz = (float) (__dadd_rn(zj, sz) - zi);
-            }
-            const float ssqd = (dx * dx + dy * dy + dz * dz) * invhsqd_f;
-            if (ssqd < 4.0f) {
-              const float s = fsqrt_pos(ssqd);
-              const float mj = pjh.w;
-              srho = fmaf(mj, m4f_w0(s), srho);
-              som = fmaf(mj * invh_f, m4f_womega(s), som);
-              sze = fmaf(mj, m4f_wzeta(s), sze);
-              pairs++;
-            }
+            float d2, mj;
+            if (cand(f + q, code, d2, mj)) add(d2, mj);
           }
         }
       };
-      if (!overflow) {
+      if (use_compact) {
+        if (!done) for (int e = sl; e < ccount; e += LPG) { const float2 v = clist[e]; add(v.x, v.y); }
+      } else if (!overflow) {
         consume(ncached);
       } else {
         L = WarpLists{list, list, list, 0, 0, 0, list_cap};
@@ -263,9 +307,13 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         walk_all([&]() { consume(L.na); });
         consume(L.na);
       }
-      double drho = gsum_d<LPG>((double) srho);
-      double dom = gsum_d<LPG>((double) som);
-      double dze = gsum_d<LPG>((double) sze);
+#pragma unroll
+      for (int o = 1; o < LPG; o <<= 1) {
+        srho += __shfl_xor_sync(kFull, srho, o);
+        som += __shfl_xor_sync(kFull, som, o);
+        sze += __shfl_xor_sync(kFull, sze, o);
+      }
+      double drho = srho, dom = som, dze = sze;
       if (WARPS > 1) {
         if (sl == 0) { sm->part[wib][g][0] = drho; sm->part[wib][g][1] = dom; sm->part[wib][g][2] = dze; }
         __syncthreads();
@@ -274,22 +322,33 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         __syncthreads();
       }
       if (!done) {
-        const double hfac3 = invh * invh * invh;
+        const double hfac3 = invh * invhsqd;
         rho = drho * hfac3;
         om = dom * hfac3;
         zeta = dze * invhsqd;
-        const double hrho = prm.h_fac * pow(mi / rho, 1.0 / 3.0);
+        // h_fac (m/rho)^(1/3) = h_fac h w^(-1/3) with w = rho h^3 / m: float reciprocal
+        // cube root refined by one fp64 Newton step (relative error ~1e-14)
+        const double w = drho * inv_m;
+        double r = (double) rcbrtf((float) w);
+        r = r * (4.0 / 3.0 - (w * (1.0 / 3.0)) * (r * r * r));
+        const double hrho = prm.h_fac * hi * r;
+        hrho_last = hrho;
         if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
           done = true;
         } else {
-          if (iteration < 30) hi = hrho;
-          else if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
-          else if (iteration < 150) {
-            if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
-            hi = 0.5 * (h_lower + h_upper);
+          if (iteration < 30) {
+            invh = invh * (w * r * r) * inv_hfac;   // 1 / hrho
+            hi = hrho;
           } else {
-            fail = true;
-            done = true;
+            if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
+            else if (iteration < 150) {
+              if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
+              hi = 0.5 * (h_lower + h_upper);
+            } else {
+              fail = true;
+              done = true;
+            }
+            invh = 1.0 / hi;
           }
           if (!done) {
             mloc = fmax(mloc, hi);
@@ -301,11 +360,11 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     }
     double mw = mloc;
     for (int o = 16; o > 0; o >>= 1) mw = fmax(mw, __shfl_xor_sync(kFull, mw, o));
-    mcheck = fmax(mcheck, mw);
     bool any_abort = __any_sync(kFull, abort_cell);
     if (WARPS > 1) any_abort = __syncthreads_or(any_abort);
+    mcheck = fmax(mcheck, mw);
     if (!any_abort && mine) {
-      h_out = fmax(prm.h_fac * pow(mi / rho, 1.0 / 3.0), h_lower);
+      h_out = fmax(hrho_last, h_lower);
       rho_out = rho; om_out = om; zeta_out = zeta;
     }
     return any_abort ? 1 : 0;
@@ -324,9 +383,7 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
       do { hk = __dmul_rn(1.05, hk); } while (hk < mcheck && ++guard < 100000);
     }
   }
-  if (lane == 0 && wib == 0) {
-    if (!solved) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
-  }
+  if (lane == 0 && !solved) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
   if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
   if (__any_sync(kFull, fail) && lane == 0) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
   unsigned long long tot = pairs;
@@ -354,37 +411,53 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
 }
 
 constexpr int kDensWarps = 4;
+constexpr int kCompactPerWarp = 1536;   // float2 entries shared by the warp's particle groups
+
+size_t dens_smem_normal() {
+  return sizeof(float2) * kDensWarps * kCompactPerWarp + sizeof(int) * kDensWarps * (kDensStack + kDensListNormal);
+}
+size_t dens_smem_wide() {
+  return sizeof(float2) * 8 * kCompactPerWarp + sizeof(int) * 8 * (kDensStack + kDensListWide) + sizeof(DensSmem);
+}
 
 template <int LPG>
 __global__ void __launch_bounds__(kDensWarps * 32)
 k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
-                HeavyList heavy) {
-  __shared__ int s_stack[kDensWarps][kDensStack];
-  __shared__ int s_list[kDensWarps][kDensListNormal];
+                HeavyList heavy, bool handover) {
+  extern __shared__ float2 s_dyn2[];
+  float2* s_compact = s_dyn2;
+  int* s_stack = reinterpret_cast<int*>(s_dyn2 + kDensWarps * kCompactPerWarp);
+  int* s_list = s_stack + kDensWarps * kDensStack;
   const int wib = threadIdx.x >> 5;
   const int leaf = blockIdx.x * kDensWarps + wib;
   if (leaf >= t.nleaf) return;
-  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack[wib], s_list[wib], kDensListNormal,
-                                       true, nullptr);
+  const int kcap = kCompactPerWarp / (32 / LPG);
+  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack + wib * kDensStack,
+                                       s_list + wib * kDensListNormal, kDensListNormal,
+                                       s_compact + wib * kCompactPerWarp, kcap, handover, nullptr);
   if (!ok && (threadIdx.x & 31) == 0) {
     const int k = atomicAdd(heavy.count, 1);
     heavy.leaves[k] = leaf;
   }
 }
 
+// Heavy cells: 8 warps share each cell's candidates.
 template <int LPG>
 __global__ void __launch_bounds__(256)
 k_density_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
                      HeavyList heavy) {
-  extern __shared__ int s_dyn[];
-  int* s_stack = s_dyn;                                   // 8 x kDensStack
-  int* s_list = s_dyn + 8 * kDensStack;                   // 8 x kDensListWide
-  DensSmem* sm = reinterpret_cast<DensSmem*>(s_dyn + 8 * (kDensStack + kDensListWide));
+  extern __shared__ float2 s_dyn2[];
+  float2* s_compact = s_dyn2;
+  int* s_stack = reinterpret_cast<int*>(s_dyn2 + 8 * kCompactPerWarp);
+  int* s_list = s_stack + 8 * kDensStack;
+  DensSmem* sm = reinterpret_cast<DensSmem*>(s_list + 8 * kDensListWide);
   const int wib = threadIdx.x >> 5;
+  const int kcap = kCompactPerWarp / (32 / LPG);
   const int nh = *heavy.count;
   for (int k = blockIdx.x; k < nh; k += gridDim.x) {
     density_cell<LPG, 8>(t, p, mp, mc, prm, cnt, heavy.leaves[k], s_stack + wib * kDensStack,
-                         s_list + wib * kDensListWide, kDensListWide, false, sm);
+                         s_list + wib * kDensListWide, kDensListWide, s_compact + wib * kCompactPerWarp, kcap,
+                         false, sm);
     __syncthreads();
   }
 }
@@ -603,11 +676,20 @@ constexpr int kWListA = 256, kWListB = 512, kWListC = 1024;         // wide kern
 // One leaf (or one particle of a leaf) through the gravity walk and all its terms.
 // LPG = lanes per particle; pfirst = first particle of the leaf this warp owns.
 // give_up: hand the leaf over when the near or direct list overflows.
-template <int LPG>
+// Block-shared partial sums of the sliced wide kernel: [slice][particle][9 values].
+struct ForceSmem {
+  double acc[8][32][9];
+  unsigned long long dcnt[8][32], dhash[8][32], ccnt[8], chash[8];
+};
+
+// SLICES > 1: the block's SLICES warps share the leaf, each keeping every SLICES-th
+// emitted list entry (sel = its slice), and their partial sums are added in slice order.
+template <int LPG, int SLICES>
 __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& p, const MixedParticles& mp,
                                                 const MixedCells& mc, const SphParams& prm, const DeviceCounters& cnt,
                                                 int leaf, int pfirst, int* stack, int* la, int* lb, int* lc, int capa,
-                                                int capb, int capc, bool give_up) {
+                                                int capb, int capc, bool give_up, int sel = 0,
+                                                ForceSmem* fs = nullptr) {
   const int lane = threadIdx.x & 31;
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
@@ -679,6 +761,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   if (lane == 0) stack[0] = 0;
   int top = 1;
   bool stack_ok = true;
+  int ea = 0, eb = 0, ec = 0;   // entries emitted so far (slicing)
   __syncwarp();
   while (top > 0) {
     const int take = top < 32 ? top : 32;
@@ -697,12 +780,20 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
       stack[top + 2 * r + 1] = node + 1;
     }
     top += 2 * nopen;
-    const unsigned ma = __ballot_sync(kFull, act == kEmitA);
-    const unsigned mb = __ballot_sync(kFull, act == kEmitB);
-    const unsigned mcm = __ballot_sync(kFull, act == kEmitC);
-    if (act == kEmitA) L.a[L.na + __popc(ma & lt)] = node;
-    if (act == kEmitB) L.b[L.nb + __popc(mb & lt)] = node;
-    if (act == kEmitC) L.c[L.nc + __popc(mcm & lt)] = node;
+    bool ka = act == kEmitA, kb = act == kEmitB, kc = act == kEmitC;
+    if (SLICES > 1) {
+      const unsigned xa = __ballot_sync(kFull, ka), xb = __ballot_sync(kFull, kb), xc = __ballot_sync(kFull, kc);
+      ka = ka && ((ea + __popc(xa & lt)) % SLICES == sel);
+      kb = kb && ((eb + __popc(xb & lt)) % SLICES == sel);
+      kc = kc && ((ec + __popc(xc & lt)) % SLICES == sel);
+      ea += __popc(xa); eb += __popc(xb); ec += __popc(xc);
+    }
+    const unsigned ma = __ballot_sync(kFull, ka);
+    const unsigned mb = __ballot_sync(kFull, kb);
+    const unsigned mcm = __ballot_sync(kFull, kc);
+    if (ka) L.a[L.na + __popc(ma & lt)] = node;
+    if (kb) L.b[L.nb + __popc(mb & lt)] = node;
+    if (kc) L.c[L.nc + __popc(mcm & lt)] = node;
     L.na += __popc(ma); L.nb += __popc(mb); L.nc += __popc(mcm);
     __syncwarp();
     if (L.nc > capc - 32) { consume_c(); L.nc = 0; __syncwarp(); }
@@ -724,13 +815,61 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     atomicAdd(cnt.hydro_pairs, a1); atomicAdd(cnt.direct_pairs, a2);
     atomicAdd(cnt.cell_pairs, a3); atomicAdd(cnt.exact_checks, a4);
   }
-  if (cnt.record && pfirst == 0) {
-    unsigned long long cc = ccount, ch = chash;
+  unsigned long long cc = ccount, ch = chash;
+  if (cnt.record) {
     for (int o = 16; o > 0; o >>= 1) { cc += __shfl_xor_sync(kFull, cc, o); ch += __shfl_xor_sync(kFull, ch, o); }
-    if (lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
   }
   const double gpot0 = (p.m[slot] / p.h[slot]) * m4_wpot(0.0);
-  finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, gpot0, ndir, dhash, true);
+  if (SLICES == 1) {
+    if (cnt.record && pfirst == 0 && lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
+    finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, gpot0, ndir, dhash, true);
+    return true;
+  }
+  // sliced: reduce each particle inside the warp, then across slices in slice order
+  double v[9];
+  for (int k = 0; k < 3; k++) { v[k] = (double) A.ah[k]; v[3 + k] = (double) A.ag[k]; }
+  v[6] = A.gpot; v[7] = A.dudt; v[8] = A.divv;
+  unsigned long long dc = ndir, dh = dhash;
+  for (int o = 1; o < LPG; o <<= 1) {
+    for (int k = 0; k < 9; k++) v[k] += __shfl_xor_sync(kFull, v[k], o);
+    dc += __shfl_xor_sync(kFull, dc, o);
+    dh += __shfl_xor_sync(kFull, dh, o);
+  }
+  if (sl == 0) {
+    for (int k = 0; k < 9; k++) fs->acc[sel][g][k] = v[k];
+    fs->dcnt[sel][g] = dc;
+    fs->dhash[sel][g] = dh;
+  }
+  if (lane == 0) { fs->ccnt[sel] = cc; fs->chash[sel] = ch; }
+  __syncthreads();
+  if (sel == 0) {
+    if (mine && sl == 0) {
+      double tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      unsigned long long tdc = 0, tdh = 0;
+      for (int w = 0; w < SLICES; w++) {
+        for (int k = 0; k < 9; k++) tot[k] += fs->acc[w][g][k];
+        tdc += fs->dcnt[w][g];
+        tdh += fs->dhash[w][g];
+      }
+      if (cnt.record) { cnt.rec_dir_cnt[slot] = tdc; cnt.rec_dir_hash[slot] = tdh; }
+      const double rho = p.rho[slot];
+      const double invrho = 1.0 / rho;
+      const double divv = tot[8] * invrho;
+      const double P = (prm.gamma_eos - 1.0) * rho * p.u[slot];
+      p.div_v[slot] = divv;
+      p.dudt[slot] = tot[7] - P * divv * invrho * p.invomega[slot];
+      p.ax[slot] = tot[0] + tot[3]; p.ay[slot] = tot[1] + tot[4]; p.az[slot] = tot[2] + tot[5];
+      p.agx[slot] = tot[3]; p.agy[slot] = tot[4]; p.agz[slot] = tot[5];
+      p.gpot[slot] = gpot0 + tot[6];
+    }
+    if (cnt.record && lane == 0) {
+      unsigned long long tc = 0, th = 0;
+      for (int w = 0; w < SLICES; w++) { tc += fs->ccnt[w]; th += fs->chash[w]; }
+      cnt.rec_cell_cnt[leaf] = tc;
+      cnt.rec_cell_hash[leaf] = th;
+    }
+  }
+  __syncthreads();
   return true;
 }
 
@@ -747,33 +886,29 @@ k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphPar
   const int wib = threadIdx.x >> 5;
   const int leaf = blockIdx.x * kForceWarps + wib;
   if (leaf >= t.nleaf) return;
-  const bool ok = all_forces_leaf<LPG>(t, p, mp, mc, prm, cnt, leaf, 0, s_stack[wib], s_a[wib], s_b[wib], s_c[wib],
-                                       kFListA, kFListB, kFListC, true);
+  const bool ok = all_forces_leaf<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, 0, s_stack[wib], s_a[wib], s_b[wib],
+                                          s_c[wib], kFListA, kFListB, kFListC, true);
   if (!ok && (threadIdx.x & 31) == 0) {
     const int k = atomicAdd(heavy.count, 1);
     heavy.leaves[k] = leaf;
   }
 }
 
-// One warp per particle of each heavy leaf (8 warps per block for Nleafmax <= 8).
+// Heavy leaves: the block's 8 warps share each leaf, each taking an eighth of its
+// near-leaf, direct-leaf and cell lists for all of its particles.
+template <int LPG>
 __global__ void __launch_bounds__(256)
 k_all_forces_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
-                        HeavyList heavy, int warps_per_leaf) {
+                        HeavyList heavy) {
   extern __shared__ int s_dyn[];
   const int wib = threadIdx.x >> 5;
   const int per = kFStack + kWListA + kWListB + kWListC;
   int* base = s_dyn + wib * per;
+  ForceSmem* fs = reinterpret_cast<ForceSmem*>(s_dyn + 8 * per);
   const int nh = *heavy.count;
-  const int total = nh * warps_per_leaf;
-  const int nw = gridDim.x * (blockDim.x >> 5);
-  for (int item = blockIdx.x * (blockDim.x >> 5) + wib; item < total; item += nw) {
-    const int leaf = heavy.leaves[item / warps_per_leaf];
-    const int pf = item % warps_per_leaf;
-    for (int q = pf; q < 32; q += warps_per_leaf) {
-      if (q >= t.cell_n[t.leaf_cell[leaf]]) break;
-      all_forces_leaf<32>(t, p, mp, mc, prm, cnt, leaf, q, base, base + kFStack, base + kFStack + kWListA,
-                          base + kFStack + kWListA + kWListB, kWListA, kWListB, kWListC, false);
-    }
+  for (int k = blockIdx.x; k < nh; k += gridDim.x) {
+    all_forces_leaf<LPG, 8>(t, p, mp, mc, prm, cnt, heavy.leaves[k], 0, base, base + kFStack, base + kFStack + kWListA,
+                            base + kFStack + kWListA + kWListB, kWListA, kWListB, kWListC, false, wib, fs);
   }
 }
 
@@ -895,15 +1030,21 @@ void launch_mixed_prep_hydro(const Tree& t, const Particles& p, const MixedParti
 
 int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
                          const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
-                         int lanes_per_particle, cudaStream_t st) {
+                         int lanes_per_particle, int max_leaf, cudaStream_t st) {
   cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
   const int blocks = (t.nleaf + kDensWarps - 1) / kDensWarps;
-  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, blocks, kDensWarps * 32, 0, t, p, mp, mc, prm, cnt, heavy)
-  const size_t smem = sizeof(int) * 8 * (kDensStack + kDensListWide) + sizeof(DensSmem);
+  const size_t smem_n = dens_smem_normal();
+  for (auto f : {k_density_mixed<1>, k_density_mixed<2>, k_density_mixed<4>, k_density_mixed<8>,
+                 k_density_mixed<16>, k_density_mixed<32>})
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_n);
+  (void) max_leaf;
+  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, blocks, kDensWarps * 32, smem_n, t, p, mp, mc, prm, cnt, heavy,
+                 true)
+  const size_t smem = dens_smem_wide();
   for (auto f : {k_density_mixed_wide<1>, k_density_mixed_wide<2>, k_density_mixed_wide<4>,
                  k_density_mixed_wide<8>, k_density_mixed_wide<16>, k_density_mixed_wide<32>})
     cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-  GSPH_MIXED_LPG(k_density_mixed_wide, lanes_per_particle, 152 * 2, 256, smem, t, p, mp, mc, prm, cnt, heavy)
+  GSPH_MIXED_LPG(k_density_mixed_wide, lanes_per_particle, 152, 256, smem, t, p, mp, mc, prm, cnt, heavy)
   return 2;
 }
 
@@ -913,10 +1054,12 @@ int launch_all_forces_mixed(const Tree& t, const Particles& p, const MixedPartic
   cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
   const int blocks = (t.nleaf + kForceWarps - 1) / kForceWarps;
   GSPH_MIXED_LPG(k_all_forces_mixed, lanes_per_particle, blocks, kForceWarps * 32, 0, t, p, mp, mc, prm, cnt, heavy)
-  const size_t smem = sizeof(int) * 8 * (kFStack + kWListA + kWListB + kWListC);
-  cudaFuncSetAttribute(k_all_forces_mixed_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-  const int wpl = max_leaf < 8 ? max_leaf : 8;
-  k_all_forces_mixed_wide<<<152 * 2, 256, smem, st>>>(t, p, mp, mc, prm, cnt, heavy, wpl < 1 ? 1 : wpl);
+  const size_t smem = sizeof(int) * 8 * (kFStack + kWListA + kWListB + kWListC) + sizeof(ForceSmem);
+  for (auto f : {k_all_forces_mixed_wide<1>, k_all_forces_mixed_wide<2>, k_all_forces_mixed_wide<4>,
+                 k_all_forces_mixed_wide<8>, k_all_forces_mixed_wide<16>, k_all_forces_mixed_wide<32>})
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  (void) max_leaf;
+  GSPH_MIXED_LPG(k_all_forces_mixed_wide, lanes_per_particle, 152 * 2, 256, smem, t, p, mp, mc, prm, cnt, heavy)
   return 2;
 }
 
