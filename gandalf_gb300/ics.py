@@ -77,6 +77,24 @@ def plummer_sphere(n: int = 262144, seed: int = 4321, rtrunc: float = 10.0) -> d
     return ics
 
 
+def with_stars(ics: dict, nstar: int = 64, rmax: float = 0.5, mass: float = 1.0e-3, h: float = 0.01,
+               sigma_v: float = 0.0, seed: int = 99) -> dict:
+    """Add ``nstar`` star particles, uniform in the sphere r < rmax, to a particle set.
+
+    Stars carry x y z vx vy vz m h (h: the star's softening length, used in the mean-h
+    kernel of the SPH-star gravity); velocities are Gaussian with ``sigma_v`` per axis.
+    """
+    rng = np.random.default_rng(seed)
+    r = rmax * rng.random(nstar) ** (1.0 / 3.0)
+    x = r[:, None] * _unit_vectors(rng, nstar)
+    v = rng.normal(0.0, sigma_v, (nstar, 3)) if sigma_v > 0 else np.zeros((nstar, 3))
+    ics = dict(ics)
+    ics["stars"] = {"x": x[:, 0].copy(), "y": x[:, 1].copy(), "z": x[:, 2].copy(),
+                    "vx": v[:, 0].copy(), "vy": v[:, 1].copy(), "vz": v[:, 2].copy(),
+                    "m": np.full(nstar, mass), "h": np.full(nstar, h)}
+    return ics
+
+
 def _unit_vectors(rng, n):
     cost = 2.0 * rng.random(n) - 1.0
     phi = 2.0 * math.pi * rng.random(n)

@@ -47,6 +47,7 @@ const double kBig = 9.9e20;               // src/Headers/Constants.h:72
 const double kKernRange = 2.0;
 const double kKernRangeSqd = 4.0;
 const double kGhostRange = 2.5;           // src/Headers/Hydrodynamics.h:52
+const double kTwoPi = 6.28318530717959;   // src/Headers/Constants.h:62
 
 struct Params {
   int32_t self_gravity, eos, periodic, nleafmax, multipole, hydro_forces, pad0, pad1;
@@ -122,7 +123,11 @@ struct Oracle {
   std::vector<int> leaves;         // DFS ids of leaves, left to right
   // outputs (input order)
   std::vector<double> rho, invomega, zeta, hfactor, pressure, sound, div_v, dudt, gpot, hrangesqd;
-  std::vector<double> a[3], ag[3];
+  std::vector<double> a[3], ag[3], gpot_hydro;
+  // star particles (NbodyParticle r, v, m, h) and the star <- gas results
+  int nstar = 0;
+  std::vector<double> sx[3], sv[3], sm, sh;
+  std::vector<double> s_a[3], s_adot[3], s_gpot;
   // optional lists
   bool want_lists = false;
   std::vector<std::vector<int>> hydro_neib, direct_neib;   // per particle (input ids)
@@ -368,6 +373,16 @@ struct Oracle {
     const double drho = -invndim * hi / rho_;   // Sph.h:264-268
     invom = 1.0 - drho * invom;
     invomega[i] = 1.0 / invom;
+    // SPH-star conservative-gravity zeta term (Hubber et al. 2013; GradhSph.cpp:282-297,
+    // the default conservative_sph_star_gravity = 1 with softened N-body gravity)
+    for (int s_ = 0; s_ < nstar; s_++) {
+      const double ih = 2.0 / (hi + sh[s_]);
+      const double ihsqd = ih * ih;
+      double dr[3];
+      for (int k = 0; k < 3; k++) dr[k] = sx[k][s_] - rp[k];
+      const double ssqd = dot3(dr, dr) * ihsqd;
+      zet += sm[s_] * ihsqd * wzeta(std::sqrt(ssqd));
+    }
     zeta[i] = drho * zet * invomega[i];
     // thermal properties (GradhSph::ComputeThermalProperties, EOS)
     if (p.eos == 1) u[i] = p.temp0 / (p.gamma_eos - 1.0) / p.mu_bar;
@@ -773,6 +788,126 @@ struct Oracle {
     }
   }
 
+  // ---------------------------------------------------------------------------------
+  // Gas <- stars: GradhSph::ComputeStarGravForces (src/GradhSph/GradhSph.cpp:698-743),
+  // after gpot_hydro is taken (GradhSphTree.cpp:596-606; :385-391 in the hydro-only pass).
+  void gas_from_stars() {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      gpot_hydro[i] = gpot[i];
+      if (nstar == 0) continue;
+      double at[3] = {0.0, 0.0, 0.0}, pot = 0.0;
+      for (int s_ = 0; s_ < nstar; s_++) {
+        double dr[3];
+        for (int k = 0; k < 3; k++) dr[k] = sx[k][s_] - x[k][i];
+        const double drsqd = dot3(dr, dr) + kSmall;
+        const double drmag = std::sqrt(drsqd);
+        const double invdrmag = 1.0 / drmag;
+        const double invhmean = 2.0 / (h[i] + sh[s_]);
+        const double paux = sm[s_] * invhmean * invhmean * wgrav(drmag * invhmean) * invdrmag;
+        for (int k = 0; k < 3; k++) at[k] += paux * dr[k];
+        pot += sm[s_] * invhmean * wpot(drmag * invhmean);
+      }
+      for (int k = 0; k < 3; k++) { ag[k][i] += at[k]; a[k][i] += at[k]; }
+      gpot[i] += pot;
+    }
+  }
+
+  // Star <- gas: HydroTree::UpdateAllStarGasForces (src/Tree/HydroTree.cpp:551-654) with
+  // Tree::ComputeStarGravityInteractionList (src/Tree/Tree.cpp:747-885) and
+  // NbodyHermite4::CalculateDirectHydroForces (src/Nbody/NbodyHermite4.cpp:151-245).
+  void stars_from_gas() {
+    for (int k = 0; k < 3; k++) { s_a[k].assign(nstar, 0.0); s_adot[k].assign(nstar, 0.0); }
+    s_gpot.assign(nstar, 0.0);
+    const bool quad = p.multipole == 1;
+#pragma omp parallel for schedule(dynamic)
+    for (int s_ = 0; s_ < nstar; s_++) {
+      const double rs[3] = {sx[0][s_], sx[1][s_], sx[2][s_]};
+      const double vs[3] = {sv[0][s_], sv[1][s_], sv[2][s_]};
+      const double hrangemax = kKernRange * sh[s_];
+      std::vector<int> near_id, direct_id, gcells;
+      walk([&](int cc, const Cell& o) -> int {
+        double dr[3];
+        for (int k = 0; k < 3; k++) dr[k] = o.rcell[k] - rs[k];
+        const double drsqd = dot3(dr, dr);
+        const double reach = 0.5 * hrangemax + o.rmax + 0.5 * kKernRange * o.hmax;
+        if (drsqd < reach * reach) {
+          if (o.level < ltot) return 1;
+          for (int j = 0; j < o.n; j++) near_id.push_back(order[o.first + j]);
+          return 0;
+        }
+        if (drsqd > o.cdistsqd && o.n > 0) {
+          if (o.level == ltot && o.n == 1) direct_id.push_back(order[o.first]);
+          else gcells.push_back(cc);
+          return 0;
+        }
+        if (drsqd <= o.cdistsqd && o.n > 0) {
+          if (o.level < ltot) return 1;
+          for (int j = 0; j < o.n; j++) direct_id.push_back(order[o.first + j]);
+        }
+        return 0;
+      });
+      double acc[3] = {0.0, 0.0, 0.0}, adot[3] = {0.0, 0.0, 0.0}, pot = 0.0;
+      for (int j : near_id) {
+        double dr[3], dv[3];
+        for (int k = 0; k < 3; k++) { dr[k] = x[k][j] - rs[k]; dv[k] = v[k][j] - vs[k]; }
+        const double drsqd = dot3(dr, dr);
+        const double drmag = std::sqrt(drsqd);
+        const double invdrmag = 1.0 / drmag;
+        const double invhmean = 2.0 / (sh[s_] + h[j]);
+        const double drdt = dot3(dv, dr) * invdrmag;
+        const double paux = m[j] * invhmean * invhmean * wgrav(drmag * invhmean) * invdrmag;
+        const double wkern = w0(drmag * invhmean) * (double) std::pow((float) invhmean, 3.0f);
+        for (int k = 0; k < 3; k++) acc[k] += paux * dr[k];
+        for (int k = 0; k < 3; k++)
+          adot[k] += paux * dv[k] - 3.0 * paux * drdt * invdrmag * dr[k] +
+                     2.0 * kTwoPi * m[j] * drdt * wkern * invdrmag * dr[k];
+        pot += m[j] * invhmean * wpot(drmag * invhmean);
+      }
+      for (int j : direct_id) {
+        double dr[3], dv[3];
+        for (int k = 0; k < 3; k++) { dr[k] = x[k][j] - rs[k]; dv[k] = v[k][j] - vs[k]; }
+        const double drsqd = dot3(dr, dr);
+        const double drmag = std::sqrt(drsqd);
+        const double invdrmag = 1.0 / drmag;
+        const double drdt = dot3(dv, dr) * invdrmag;
+        const double inv3 = invdrmag * invdrmag * invdrmag;
+        for (int k = 0; k < 3; k++) acc[k] += m[j] * dr[k] * inv3;
+        for (int k = 0; k < 3; k++) adot[k] += m[j] * inv3 * (dv[k] - 3.0 * drdt * invdrmag * dr[k]);
+        pot += m[j] * invdrmag;
+      }
+      for (int cc : gcells) {
+        const Cell& c = cells[cc];
+        double dr[3];
+        if (quad) {
+          for (int k = 0; k < 3; k++) dr[k] = rs[k] - c.r[k];
+          const double drsqd = dot3(dr, dr) + kSmall;
+          const double invdrsqd = 1.0 / drsqd;
+          const double invdrmag = std::sqrt(invdrsqd);
+          const double invdr5 = invdrsqd * invdrsqd * invdrmag;
+          for (int k = 0; k < 3; k++) acc[k] -= c.m * dr[k] * invdrsqd * invdrmag;
+          const double* q = c.q;
+          const double qscalar = q[0] * dr[0] * dr[0] + q[2] * dr[1] * dr[1] - (q[0] + q[2]) * dr[2] * dr[2] +
+                                 2.0 * (q[1] * dr[0] * dr[1] + q[3] * dr[0] * dr[2] + q[4] * dr[1] * dr[2]);
+          const double qfactor = 2.5 * qscalar * invdr5 * invdrsqd;
+          acc[0] += (q[0] * dr[0] + q[1] * dr[1] + q[3] * dr[2]) * invdr5 - qfactor * dr[0];
+          acc[1] += (q[1] * dr[0] + q[2] * dr[1] + q[4] * dr[2]) * invdr5 - qfactor * dr[1];
+          acc[2] += (q[3] * dr[0] + q[4] * dr[1] - (q[0] + q[2]) * dr[2]) * invdr5 - qfactor * dr[2];
+          pot += c.m * invdrmag + 0.5 * qscalar * invdr5;
+        } else {
+          for (int k = 0; k < 3; k++) dr[k] = c.r[k] - rs[k];
+          const double drsqd = dot3(dr, dr) + kSmall;
+          const double invdrsqd = 1.0 / drsqd;
+          const double invdrmag = std::sqrt(invdrsqd);
+          pot += c.m * invdrmag;
+          for (int k = 0; k < 3; k++) acc[k] += c.m * dr[k] * invdrsqd * invdrmag;
+        }
+      }
+      for (int k = 0; k < 3; k++) { s_a[k][s_] = acc[k]; s_adot[k][s_] = adot[k]; }
+      s_gpot[s_] = pot;
+    }
+  }
+
   // Set when the h solve's results are supplied by the caller (force pass only).
   bool given = false;
   std::vector<double> g_h, g_rho, g_invomega, g_zeta, g_pressure, g_sound;
@@ -783,7 +918,7 @@ struct Oracle {
 #endif
     rho.assign(n, 0); invomega.assign(n, 1); zeta.assign(n, 0); hfactor.assign(n, 0);
     pressure.assign(n, 0); sound.assign(n, 0); div_v.assign(n, 0); dudt.assign(n, 0);
-    gpot.assign(n, 0); hrangesqd.assign(n, 0);
+    gpot.assign(n, 0); hrangesqd.assign(n, 0); gpot_hydro.assign(n, 0);
     for (int k = 0; k < 3; k++) { a[k].assign(n, 0); ag[k].assign(n, 0); }
     if (want_lists || want_summary) hydro_neib.assign(n, {});
     if (want_lists) { direct_neib.assign(n, {}); gcell_list.clear(); gcell_leaf.clear(); }
@@ -809,6 +944,8 @@ struct Oracle {
     }
     update_hmax(0);
     if (p.self_gravity) all_forces(); else hydro_forces();
+    gas_from_stars();
+    if (nstar > 0 && p.self_gravity) stars_from_gas();
     return 0;
   }
 };
@@ -873,7 +1010,7 @@ void gsph_oracle_particles(void* handle, double* out) {
     r[4] = o->hfactor[i]; r[5] = o->pressure[i]; r[6] = o->sound[i]; r[7] = o->u[i];
     r[8] = o->div_v[i]; r[9] = o->dudt[i];
     for (int k = 0; k < 3; k++) { r[10 + k] = o->a[k][i]; r[13 + k] = o->ag[k][i]; }
-    r[16] = o->gpot[i]; r[17] = o->gpot[i]; r[18] = o->hrangesqd[i]; r[19] = 0.0;
+    r[16] = o->gpot[i]; r[17] = o->gpot_hydro[i]; r[18] = o->hrangesqd[i]; r[19] = 0.0;
   }
 }
 
@@ -937,6 +1074,32 @@ void gsph_oracle_summary(void* handle, int64_t* dir_count, uint64_t* dir_hash, i
   for (int64_t i = 0; i < o->n; i++) { dir_count[i] = o->dir_count[i]; dir_hash[i] = o->dir_hash[i]; }
   for (size_t q = 0; q < o->leaves.size(); q++) {
     leaf_cell[q] = o->leaves[q]; cell_count[q] = o->cell_count[q]; cell_hash[q] = o->cell_hash[q];
+  }
+}
+
+// Star particles for the following runs (nstar = 0 removes them).
+void gsph_oracle_set_stars(void* handle, int nstar, const double* x, const double* y, const double* z,
+                           const double* vx, const double* vy, const double* vz, const double* m,
+                           const double* h) {
+  Oracle* o = static_cast<Oracle*>(handle);
+  o->nstar = nstar;
+  const double* r[3] = {x, y, z};
+  const double* v[3] = {vx, vy, vz};
+  for (int k = 0; k < 3; k++) { o->sx[k].assign(r[k], r[k] + nstar); o->sv[k].assign(v[k], v[k] + nstar); }
+  o->sm.assign(m, m + nstar);
+  o->sh.assign(h, h + nstar);
+}
+
+// Star results of the last run: nstar x 7 doubles (a[3], adot[3], gpot).
+void gsph_oracle_stars(void* handle, double* out) {
+  Oracle* o = static_cast<Oracle*>(handle);
+  for (int s_ = 0; s_ < o->nstar; s_++) {
+    double* r = out + (int64_t) s_ * 7;
+    for (int k = 0; k < 3; k++) {
+      r[k] = o->s_a[k].empty() ? 0.0 : o->s_a[k][s_];
+      r[3 + k] = o->s_adot[k].empty() ? 0.0 : o->s_adot[k][s_];
+    }
+    r[6] = o->s_gpot.empty() ? 0.0 : o->s_gpot[s_];
   }
 }
 

@@ -20,6 +20,8 @@ LIB = os.path.join(BUILD_DIR, "libgsph_oracle.so")
 PARTICLE_FIELDS = ["h", "rho", "invomega", "zeta", "hfactor", "pressure", "sound", "u",
                    "div_v", "dudt", "ax", "ay", "az", "agx", "agy", "agz", "gpot",
                    "gpot_hydro", "hrangesqd", "levelneib"]
+STAR_KEYS = ("x", "y", "z", "vx", "vy", "vz", "m", "h")
+STAR_FIELDS = ["ax", "ay", "az", "adotx", "adoty", "adotz", "gpot"]
 CELL_FIELDS = ["N", "level", "m", "rmax", "hmax", "cdistsqd", "bbmin0", "bbmin1", "bbmin2",
                "bbmax0", "bbmax1", "bbmax2", "hbmin0", "hbmin1", "hbmin2", "hbmax0", "hbmax1",
                "hbmax2", "rcell0", "rcell1", "rcell2", "r0", "r1", "r2", "q0", "q1", "q2", "q3",
@@ -89,6 +91,8 @@ def _load():
         lib.gsph_oracle_run_given.argtypes = [vp, i64] + [dp] * 15 + [i32, i32]
         lib.gsph_oracle_nleaf.restype = i32
         lib.gsph_oracle_nleaf.argtypes = [vp]
+        lib.gsph_oracle_set_stars.argtypes = [vp, i32] + [dp] * 8
+        lib.gsph_oracle_stars.argtypes = [vp, dp]
         _lib = lib
     return _lib
 
@@ -126,6 +130,11 @@ def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0, summary
     prm = make_params(params)
     h = lib.gsph_oracle_create(ctypes.byref(prm))
     try:
+        stars = ics.get("stars")
+        ns = 0 if stars is None else len(stars["x"])
+        if ns:
+            sarr = [np.ascontiguousarray(stars[k], dtype=np.float64) for k in STAR_KEYS]
+            lib.gsph_oracle_set_stars(h, ns, *[_ptr(a) for a in sarr])
         arrs = [np.ascontiguousarray(ics[k], dtype=np.float64)
                 for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")]
         n = len(arrs[0])
@@ -148,7 +157,13 @@ def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0, summary
         lib.gsph_oracle_order(h, order.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
         counts = (ctypes.c_int64 * 4)()
         lib.gsph_oracle_counts(h, counts)
+        star_res = None
+        if ns:
+            so = np.empty((ns, len(STAR_FIELDS)))
+            lib.gsph_oracle_stars(h, _ptr(so))
+            star_res = {k: so[:, i].copy() for i, k in enumerate(STAR_FIELDS)}
         res = {
+            "stars": star_res,
             "particles": {k: out[:, i].copy() for i, k in enumerate(PARTICLE_FIELDS)},
             "cells": {k: cells[:, i].copy() for i, k in enumerate(CELL_FIELDS)},
             "order": order, "ltot": lib.gsph_oracle_ltot(h),

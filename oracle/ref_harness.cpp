@@ -9,12 +9,15 @@
 //   zero accelerations                         src/Hydrodynamics/SphSimulation.cpp:416-431
 //   GradhSphTree::UpdateAllSphForces | UpdateAllSphHydroForces
 //                                              src/GradhSph/GradhSphTree.cpp:279-657
+//   HydroTree::UpdateAllStarGasForces (stars)  src/Tree/HydroTree.cpp:551-654
 // and then re-runs the reference's own walks on the built tree to extract neighbour and
 // gravity interaction lists (src/Tree/Tree.cpp:561-735, src/Headers/NeighbourManager.h).
 //
 // usage: gsph_ref_harness <input.bin> <outdir>
-//   input.bin  : written by oracle/refio.py (header + SoA particle arrays, input order)
+//   input.bin  : written by oracle/refio.py (header + SoA particle arrays, input order,
+//                then, when the header's nstar > 0, the star arrays x y z vx vy vz m h)
 //   outdir     : receives particles.bin, cells.bin, leaves.bin, lists.bin, timing.txt
+//                and, with stars, stars.bin (a[3] adot[3] gpot per star)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -42,7 +45,8 @@ struct InHeader {
   int32_t periodic;       // 0 open, 1 periodic in x,y,z
   int32_t nleafmax;
   int32_t multipole;      // 0 monopole, 1 quadrupole
-  int32_t pad0, pad1;
+  int32_t nstar;          // star particles following the gas arrays
+  int32_t pad1;
   double h_fac, h_converge, alpha_visc, beta_visc, gamma_eos, thetamaxsqd, temp0, mu_bar;
   double boxmin[3], boxmax[3];
 };
@@ -78,6 +82,12 @@ int main(int argc, char** argv) {
     arr[a].resize(N);
     if (std::fread(arr[a].data(), sizeof(double), N, fin) != (size_t) N) die("short array");
   }
+  const int NS = hd.nstar;
+  std::vector<double> sarr[8];
+  for (int a = 0; a < 8 && NS > 0; a++) {
+    sarr[a].resize(NS);
+    if (std::fread(sarr[a].data(), sizeof(double), NS, fin) != (size_t) NS) die("short star array");
+  }
   std::fclose(fin);
   // x y z vx vy vz m u h
   std::vector<double>& h_in = arr[8];
@@ -91,7 +101,7 @@ int main(int argc, char** argv) {
   auto I = [&](const char* k, int v) { params->intparams[k] = v; };
   auto F = [&](const char* k, double v) { params->floatparams[k] = v; };
   S("ic", "python"); S("sim", "sph"); S("run_id", "refrun"); S("out_file_form", "column");
-  I("ndim", 3); I("Nhydro", N); I("Nstar", 0); I("dimensionless", 1);
+  I("ndim", 3); I("Nhydro", N); I("Nstar", NS); I("dimensionless", 1);
   S("kernel", "m4"); I("tabulated_kernel", 0);
   F("h_fac", hd.h_fac); F("h_converge", hd.h_converge);
   S("avisc", "mon97"); S("acond", "none"); S("time_dependent_avisc", "none");
@@ -119,6 +129,8 @@ int main(int argc, char** argv) {
   base->PreSetupForPython();
   const char* names[9] = {"x", "y", "z", "vx", "vy", "vz", "m", "u", "h"};
   for (int a = 0; a < 9; a++) base->ImportArray(arr[a].data(), N, names[a]);
+  const char* snames[8] = {"x", "y", "z", "vx", "vy", "vz", "m", "h"};
+  for (int a = 0; a < 8 && NS > 0; a++) base->ImportArray(sarr[a].data(), NS, snames[a], "star");
   // Never initialised on the Python path (Simulation.h:163); the inputs carry h.
   base->initial_h_provided = true;
   const double t_setup0 = now_s();
@@ -154,6 +166,25 @@ int main(int argc, char** argv) {
   if (hd.self_gravity) neib->UpdateAllSphForces(sph, sim->nbody, sim->simbox, sim->ewald);
   else neib->UpdateAllSphHydroForces(sph, sim->nbody, sim->simbox);
   const double t4 = now_s();
+
+  // ---- star <- gas forces (HydroTree::UpdateAllStarGasForces) --------------------------
+  std::vector<double> sout((size_t) NS * 7);
+  if (NS > 0) {
+    Nbody<3>* nb = sim->nbody;
+    for (int s = 0; s < nb->Nnbody; s++) {
+      NbodyParticle<3>* st = nb->nbodydata[s];
+      for (int k = 0; k < 3; k++) { st->a[k] = 0; st->adot[k] = 0; }
+      st->gpot = 0;
+      st->flags.set(active);
+    }
+    if (hd.self_gravity) neib->UpdateAllStarGasForces(sph, nb, sim->simbox, sim->ewald);
+    for (int s = 0; s < NS; s++) {
+      NbodyParticle<3>* st = nb->nbodydata[s];
+      double* o = &sout[(size_t) s * 7];
+      for (int k = 0; k < 3; k++) { o[k] = st->a[k]; o[3 + k] = st->adot[k]; }
+      o[6] = st->gpot;
+    }
+  }
 
   // ---- per-particle results (input order) --------------------------------------------
   const int NP = 20;
@@ -258,6 +289,7 @@ int main(int argc, char** argv) {
   write_block(f, gs_off); write_block(f, gs_ids);
   write_block(f, gcell_leaf); write_block(f, gcell_off); write_block(f, gcell_ids);
   std::fclose(f);
+  if (NS > 0) { f = std::fopen("stars.bin", "wb"); write_block(f, sout); std::fclose(f); }
   f = std::fopen("timing.txt", "w");
   std::fprintf(f, "setup %.6f\nbuild_tree %.6f\nghosts %.6f\nsph_properties %.6f\nforces %.6f\n"
                "step_total %.6f\nltot %d\nncell %d\n",

@@ -35,19 +35,28 @@ def available() -> bool:
     return os.path.exists(HARNESS)
 
 
+STAR_KEYS = ("x", "y", "z", "vx", "vy", "vz", "m", "h")
+STAR_FIELDS = ["ax", "ay", "az", "adotx", "adoty", "adotz", "gpot"]
+
+
 def write_input(path: str, ics: dict, params: dict) -> None:
+    """ics may carry ``stars``: a dict of star arrays (STAR_KEYS)."""
     p = dict(DEFAULTS)
     p.update(params)
     n = len(ics["x"])
+    stars = ics.get("stars")
+    nstar = 0 if stars is None else len(stars["x"])
     with open(path, "wb") as f:
         f.write(b"GSPHIN01")
         f.write(struct.pack("<8i", n, int(p["self_gravity"]), int(p["eos"]), int(p["periodic"]),
-                            int(p["nleafmax"]), int(p["multipole"]), 0, 0))
+                            int(p["nleafmax"]), int(p["multipole"]), nstar, 0))
         f.write(struct.pack("<8d", p["h_fac"], p["h_converge"], p["alpha_visc"], p["beta_visc"],
                             p["gamma_eos"], p["thetamaxsqd"], p["temp0"], p["mu_bar"]))
         f.write(struct.pack("<6d", *p["boxmin"], *p["boxmax"]))
         for key in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h"):
             f.write(np.ascontiguousarray(ics[key], dtype="<f8").tobytes())
+        for key in STAR_KEYS if nstar else ():
+            f.write(np.ascontiguousarray(stars[key], dtype="<f8").tobytes())
 
 
 def _blocks(path, dtype):
@@ -87,6 +96,11 @@ def run(ics: dict, params: dict, workdir: str | None = None) -> dict:
     cells = cells.reshape(-1, len(CELL_FIELDS))
     leafcell, leafoff, leafpart = _blocks(os.path.join(tmp, "leaves.bin"), "<i4")
     lb = _blocks(os.path.join(tmp, "lists.bin"), "<i4")
+    stars = None
+    if ics.get("stars") is not None and len(ics["stars"]["x"]):
+        (sb,) = _blocks(os.path.join(tmp, "stars.bin"), "<f8")
+        sb = sb.reshape(-1, len(STAR_FIELDS))
+        stars = {k: sb[:, i].copy() for i, k in enumerate(STAR_FIELDS)}
     timing = {}
     with open(os.path.join(tmp, "timing.txt")) as f:
         for line in f:
@@ -99,5 +113,5 @@ def run(ics: dict, params: dict, workdir: str | None = None) -> dict:
         "hydro_neib": _csr(lb[0], lb[1]), "grav_direct": _csr(lb[2], lb[3]),
         "grav_smooth": _csr(lb[4], lb[5]),
         "gcell_leaf": lb[6], "gcell_lists": _csr(lb[7], lb[8]),
-        "timing": timing,
+        "timing": timing, "stars": stars,
     }

@@ -9,6 +9,8 @@ oracle/Makefile.ref) on small seeded particle sets and stores, per case:
   hydro_*       SPH neighbour lists per particle (sorted input ids, CSR)
   direct_*      Newtonian direct-sum partners per particle as (count, hash)
   gcell_*       multipole cells per leaf as (count, hash)
+  star_*        (cases with stars) star inputs x y z vx vy vz m h and the reference's
+                star <- gas results (oracle/refio.STAR_FIELDS order)
 Hashes are sums of splitmix64(id) (gandalf_gb300.sph.list_hash).
 
     python tests/golden/make_golden.py     # needs oracle/_ref built
@@ -30,6 +32,8 @@ from oracle import refio  # noqa: E402
 CASES = {
     "cube2048": lambda: ics_mod.periodic_cube(2048, seed=11),
     "plummer2048": lambda: ics_mod.plummer_sphere(2048, seed=12),
+    "plummer_stars2048": lambda: ics_mod.with_stars(ics_mod.plummer_sphere(2048, seed=13), 16, h=0.05,
+                                                    sigma_v=0.1, seed=14),
 }
 
 
@@ -56,6 +60,10 @@ def make(name):
     out["gcell_leaf"] = r["gcell_leaf"].astype(np.int32)
     out["gcell_count"] = np.array([len(l) for l in r["gcell_lists"]], dtype=np.int64)
     out["gcell_hash"] = np.array([list_hash(l) for l in r["gcell_lists"]], dtype=np.uint64)
+    if c.get("stars") is not None:
+        for k in refio.STAR_KEYS:
+            out["star_" + k] = c["stars"][k]
+        out["star_results"] = np.stack([r["stars"][k] for k in refio.STAR_FIELDS], axis=1)
     for k, v in prm.items():
         out["param_" + k] = np.asarray(v)
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")

@@ -12,9 +12,15 @@ PARTICLE_FIELDS = ["h", "rho", "invomega", "zeta", "hfactor", "pressure", "sound
 INPUT_KEYS = ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")
 
 
+STAR_KEYS = ("x", "y", "z", "vx", "vy", "vz", "m", "h")
+STAR_FIELDS = ["ax", "ay", "az", "adotx", "adoty", "adotz", "gpot"]
+
+
 def load_golden(name):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     ics = {k: d[k] for k in INPUT_KEYS}
+    if "star_x" in d.files:
+        ics["stars"] = {k: d["star_" + k] for k in STAR_KEYS}
     params = {k[6:]: d[k].tolist() for k in d.files if k.startswith("param_")}
     parts = {k: d["particles"][:, i] for i, k in enumerate(PARTICLE_FIELDS)}
     return ics, params, parts, d
@@ -63,6 +69,21 @@ def check_fp64(got: dict, ref: dict, gravity: bool):
         assert_vec_close("atree", (got["agx"], got["agy"], got["agz"]),
                          (ref["agx"], ref["agy"], ref["agz"]), FP64_TOL["ag"])
         assert_close("gpot", got["gpot"], ref["gpot"], FP64_TOL["gpot"])
+
+
+# Star <- gas results (FP64): summation order and rsqrt/pow differences only.
+STAR_TOL = {"a": 1e-12, "adot": 1e-11, "gpot": 1e-12}
+
+
+def check_stars(got: dict, ref: dict):
+    assert_vec_close("star a", (got["ax"], got["ay"], got["az"]), (ref["ax"], ref["ay"], ref["az"]), STAR_TOL["a"])
+    assert_vec_close("star adot", (got["adotx"], got["adoty"], got["adotz"]),
+                     (ref["adotx"], ref["adoty"], ref["adotz"]), STAR_TOL["adot"])
+    assert_close("star gpot", got["gpot"], ref["gpot"], STAR_TOL["gpot"])
+
+
+def star_results(d):
+    return {k: d["star_results"][:, i] for i, k in enumerate(STAR_FIELDS)}
 
 
 def csr_lists(off, ids):

@@ -4,10 +4,10 @@ import pytest
 
 from oracle import oracle
 from gandalf_gb300.sph import list_hash
-from parity import load_golden, check_fp64, csr_lists, same_lists
+from parity import assert_close, check_fp64, check_stars, csr_lists, load_golden, same_lists, star_results
 
 
-@pytest.mark.parametrize("name,gravity", [("cube2048", False), ("plummer2048", True)])
+@pytest.mark.parametrize("name,gravity", [("cube2048", False), ("plummer2048", True), ("plummer_stars2048", True)])
 def test_oracle_matches_reference_fixture(name, gravity):
     ics, params, ref, d = load_golden(name)
     r = oracle.run(ics, params, lists=True, nthreads=2)
@@ -44,3 +44,18 @@ def test_oracle_plants_a_mistake_and_sees_it():
     r = oracle.run(bad, params, nthreads=2)
     with pytest.raises(AssertionError):
         check_fp64(r["particles"], ref, False)
+
+
+def test_oracle_star_coupling_matches_reference():
+    """Gas <- star terms (including the conservative zeta term of the h solve), gpot_hydro
+    without the stars, and star <- gas forces (a, adot, gpot) against the reference."""
+    ics, params, ref, d = load_golden("plummer_stars2048")
+    r = oracle.run(ics, params, nthreads=2)
+    assert_close("gpot_hydro", r["particles"]["gpot_hydro"], ref["gpot_hydro"], 1e-11)
+    check_stars(r["stars"], star_results(d))
+    # the stars matter: without them the gas potential is off by far more than the tolerance
+    no_stars = dict(ics)
+    no_stars.pop("stars")
+    r0 = oracle.run(no_stars, params, nthreads=2)
+    with pytest.raises(AssertionError):
+        assert_close("gpot", r0["particles"]["gpot"], ref["gpot"], 1e-6)
