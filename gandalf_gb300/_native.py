@@ -17,7 +17,7 @@ ERRORS = {-1: "GSPH_ERR_INVALID", -2: "GSPH_ERR_CUDA", -3: "GSPH_ERR_UNSUPPORTED
           -4: "GSPH_ERR_STATE", -5: "GSPH_ERR_NOT_CONVERGED", -6: "GSPH_ERR_CAPACITY"}
 
 FIELDS = ["h", "rho", "invomega", "zeta", "hfactor", "pressure", "sound", "u", "div_v", "dudt",
-          "ax", "ay", "az", "agx", "agy", "agz", "gpot", "hrangesqd"]
+          "ax", "ay", "az", "agx", "agy", "agz", "gpot", "hrangesqd", "gpot_hydro"]
 FIELD_ID = {k: i for i, k in enumerate(FIELDS)}
 
 
@@ -85,7 +85,12 @@ SIGNATURES = {
     "gsph_kdtree_order_noalloc": (_I32, [_P, _P, _P, _P, _I32, _I32, _P, _P]),
     "gsph_get_tree": (_I32, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                              ctypes.POINTER(ctypes.c_int32), _D]),
+    "gsph_set_stars": (_I32, [_P, _I64] + [_D] * 8),
+    "gsph_update_all_star_gas_forces": (_I32, [_P]),
+    "gsph_get_star_forces": (_I32, [_P] + [_D] * 7),
 }
+
+ABI_VERSION = 2
 
 _lib = None
 
@@ -103,7 +108,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.gsph_abi_version() != 1:
+    if lib.gsph_abi_version() != ABI_VERSION:
         raise RuntimeError("libgsph_gb300.so ABI version mismatch")
     if path is None:
         _lib = lib

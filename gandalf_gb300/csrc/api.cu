@@ -19,6 +19,7 @@
 #include "gsph_state.cuh"
 #include "kernels.cuh"
 #include "mixed_state.cuh"
+#include "stars.cuh"
 #include "tree.cuh"
 
 using namespace gsph;
@@ -50,7 +51,7 @@ struct gsph_ctx {
   int ltot = 0, ncell = 0, nleaf = 0, P = 0, lpg = 4;
   // device arrays
   double* in[9] = {};        // x y z vx vy vz m u h (input order)
-  double* f[26] = {};        // leaf-order fields (see kF* below)
+  double* f[27] = {};        // leaf-order fields (see kF* below)
   int* id = nullptr;
   int *cell_first = nullptr, *cell_n = nullptr, *cell_parent = nullptr, *leaf_cell = nullptr;
   unsigned char* cell_level = nullptr;
@@ -87,6 +88,10 @@ struct gsph_ctx {
   int* heavy_leaves = nullptr;
   int* heavy_count = nullptr;
   int max_leaf = 8;
+  // star particles: 8 input arrays (x y z vx vy vz m h) then 7 results (a, adot, gpot)
+  int nstar = 0, star_cap = 0;
+  double* star_buf = nullptr;
+  bool have_star_forces = false;
   // timing
   cudaEvent_t ev[5] = {};
   gsph_stats last{};
@@ -97,7 +102,7 @@ namespace {
 enum {
   kFX = 0, kFY, kFZ, kFVX, kFVY, kFVZ, kFM, kFU, kFH, kFH0, kFRho, kFInvOmega, kFZeta, kFHfactor,
   kFHrangesqd, kFPressure, kFSound, kFAX, kFAY, kFAZ, kFAGX, kFAGY, kFAGZ, kFGpot, kFDudt, kFDivV,
-  kNumFields
+  kFGpotHydro, kNumFields
 };
 
 int fail(gsph_ctx* c, int code, const std::string& msg) {
@@ -260,8 +265,24 @@ int ensure_capacity(gsph_ctx* c, int n) {
   return GSPH_OK;
 }
 
-SphParams make_params(const gsph_config& cfg) {
+StarSet make_stars(const gsph_ctx* c) {
+  StarSet s{};
+  s.n = c->nstar;
+  if (!c->nstar) return s;
+  const double* b = c->star_buf;
+  const size_t k = (size_t) c->star_cap;
+  s.x = b; s.y = b + k; s.z = b + 2 * k; s.vx = b + 3 * k; s.vy = b + 4 * k; s.vz = b + 5 * k;
+  s.m = b + 6 * k; s.h = b + 7 * k;
+  double* o = c->star_buf + 8 * k;
+  s.ax = o; s.ay = o + k; s.az = o + 2 * k; s.adotx = o + 3 * k; s.adoty = o + 4 * k; s.adotz = o + 5 * k;
+  s.gpot = o + 6 * k;
+  return s;
+}
+
+SphParams make_params(const gsph_ctx* c) {
   SphParams p{};
+  const gsph_config& cfg = c->cfg;
+  p.stars = make_stars(c);
   p.h_fac = cfg.h_fac; p.h_converge = cfg.h_converge; p.alpha_visc = cfg.alpha_visc;
   p.beta_visc = cfg.beta_visc; p.gamma_eos = cfg.gamma_eos; p.temp0 = cfg.temp0; p.mu_bar = cfg.mu_bar;
   p.thetamaxsqd = cfg.thetamaxsqd;
@@ -284,7 +305,7 @@ Particles make_particles(gsph_ctx* c) {
   p.rho = f[kFRho]; p.invomega = f[kFInvOmega]; p.zeta = f[kFZeta]; p.hfactor = f[kFHfactor];
   p.hrangesqd = f[kFHrangesqd]; p.pressure = f[kFPressure]; p.sound = f[kFSound];
   p.ax = f[kFAX]; p.ay = f[kFAY]; p.az = f[kFAZ]; p.agx = f[kFAGX]; p.agy = f[kFAGY]; p.agz = f[kFAGZ];
-  p.gpot = f[kFGpot]; p.dudt = f[kFDudt]; p.div_v = f[kFDivV];
+  p.gpot = f[kFGpot]; p.dudt = f[kFDudt]; p.div_v = f[kFDivV]; p.gpot_hydro = f[kFGpotHydro];
   return p;
 }
 
@@ -376,14 +397,14 @@ __global__ void k_unpack_aos(const unsigned char* base, int n, int64_t stride, g
 struct FieldPtrs { const double* f[kNumFields]; };
 
 __global__ void k_pack_aos(unsigned char* base, int n, int64_t stride, gsph_field_offsets off, FieldPtrs fp,
-                           const int* __restrict__ id) {
+                           const int* __restrict__ id, int gpot_hydro_field) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     unsigned char* r = base + (size_t) id[s] * stride;
     auto put = [&](int64_t o, int fld) { if (o >= 0) *reinterpret_cast<double*>(r + o) = fp.f[fld][s]; };
     put(off.h, kFH); put(off.u, kFU); put(off.rho, kFRho); put(off.invomega, kFInvOmega);
     put(off.zeta, kFZeta); put(off.hfactor, kFHfactor); put(off.hrangesqd, kFHrangesqd);
     put(off.pressure, kFPressure); put(off.sound, kFSound); put(off.div_v, kFDivV); put(off.dudt, kFDudt);
-    put(off.gpot, kFGpot); put(off.gpot_hydro, kFGpot);
+    put(off.gpot, kFGpot); put(off.gpot_hydro, gpot_hydro_field);
     if (off.a >= 0) { put(off.a, kFAX); put(off.a + 8, kFAY); put(off.a + 16, kFAZ); }
     if (off.atree >= 0) { put(off.atree, kFAGX); put(off.atree + 8, kFAGY); put(off.atree + 16, kFAGZ); }
   }
@@ -393,8 +414,9 @@ __global__ void k_scatter_field(const double* __restrict__ src, const int* __res
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) dst[id[s]] = src[s];
 }
 
-int field_index(int field) {
+int field_index(const gsph_ctx* c, int field) {
   switch (field) {
+    case GSPH_FIELD_GPOT_HYDRO: return c->nstar ? kFGpotHydro : kFGpot;
     case GSPH_FIELD_H: return kFH;
     case GSPH_FIELD_RHO: return kFRho;
     case GSPH_FIELD_INVOMEGA: return kFInvOmega;
@@ -479,10 +501,10 @@ int do_props(gsph_ctx* c) {
   if (mixed(c)) {
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count + 2, 0, 2 * sizeof(int), c->stream));
     c->launches += (unsigned) launch_density_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
-                                                   make_params(c->cfg), make_counters(c), heavy, c->lpg, c->max_leaf,
+                                                   make_params(c), make_counters(c), heavy, c->lpg, c->max_leaf,
                                                    c->stream);
   } else {
-    launch_density(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+    launch_density(t, p, make_params(c), make_counters(c), c->lpg, c->stream);
     c->launches += 1;
   }
   int rc = check_launch(c, "density");
@@ -514,20 +536,31 @@ int do_forces(gsph_ctx* c, bool gravity) {
   if (mixed(c)) {
     if (gravity) {
       c->launches += (unsigned) launch_all_forces_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
-                                                        make_params(c->cfg), make_counters(c), heavy, c->lpg,
+                                                        make_params(c), make_counters(c), heavy, c->lpg,
                                                         c->max_leaf, c->stream);
       GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 3, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
     }
     else
       c->launches += (unsigned) launch_hydro_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
-                                                   make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+                                                   make_params(c), make_counters(c), c->lpg, c->stream);
   } else {
-    if (gravity) launch_all_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
-    else launch_hydro_forces(t, p, make_params(c->cfg), make_counters(c), c->lpg, c->stream);
+    if (gravity) launch_all_forces(t, p, make_params(c), make_counters(c), c->lpg, c->stream);
+    else launch_hydro_forces(t, p, make_params(c), make_counters(c), c->lpg, c->stream);
     c->launches += 1;
   }
+  // star gravity on the gas, after gpot_hydro is taken (GradhSphTree.cpp:596-606)
+  c->launches += (unsigned) launch_gas_from_stars(p, make_stars(c), c->stream);
   c->have_forces = true;
+  c->have_star_forces = false;
   return check_launch(c, "forces");
+}
+
+int do_star_gas(gsph_ctx* c) {
+  if (!c->have_props) return fail(c, GSPH_ERR_STATE, "smoothing lengths not solved");
+  c->launches += (unsigned) launch_stars_from_gas(make_tree(c), make_particles(c), make_stars(c), make_params(c),
+                                                  make_counters(c), c->max_leaf, c->stream);
+  c->have_star_forces = true;
+  return check_launch(c, "star gas forces");
 }
 
 int begin_counters(gsph_ctx* c) {
@@ -613,6 +646,7 @@ void gsph_destroy(gsph_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_all(c);
   if (c->aos) cudaFree(c->aos);
+  if (c->star_buf) cudaFree(c->star_buf);
   for (int q = 0; q < 5; q++) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -757,6 +791,10 @@ int32_t gsph_step(gsph_ctx* c) {
   cudaEventRecord(c->ev[3], c->stream);
   rc = do_forces(c, c->cfg.self_gravity != 0);
   if (rc) return rc;
+  if (c->nstar && c->cfg.self_gravity) {
+    rc = do_star_gas(c);
+    if (rc) return rc;
+  }
   cudaEventRecord(c->ev[4], c->stream);
   rc = read_status(c);
   float ms[4] = {0, 0, 0, 0};
@@ -769,9 +807,67 @@ int32_t gsph_step(gsph_ctx* c) {
   return rc;
 }
 
+int32_t gsph_set_stars(gsph_ctx* c, int64_t nstar, const double* x, const double* y, const double* z,
+                       const double* vx, const double* vy, const double* vz, const double* m, const double* h) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (nstar < 0 || nstar > (1 << 20)) return fail(c, GSPH_ERR_INVALID, "star count out of range");
+  const double* a[8] = {x, y, z, vx, vy, vz, m, h};
+  if (nstar > 0) {
+    for (int q = 0; q < 8; q++) if (!a[q]) return fail(c, GSPH_ERR_INVALID, "star array is NULL");
+    for (int64_t i = 0; i < nstar; i++) {
+      for (int q = 0; q < 8; q++)
+        if (!std::isfinite(a[q][i])) return fail(c, GSPH_ERR_INVALID, "non-finite star data");
+      if (!(m[i] > 0.0) || !(h[i] > 0.0)) return fail(c, GSPH_ERR_INVALID, "star mass and h must be > 0");
+    }
+  }
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  if (nstar > c->star_cap) {
+    if (c->star_buf) cudaFree(c->star_buf);
+    c->star_buf = nullptr;
+    c->star_cap = 0;
+    GSPH_CUDA(cudaMalloc(&c->star_buf, sizeof(double) * 15 * (size_t) nstar));
+    c->star_cap = (int) nstar;
+  }
+  for (int q = 0; q < 8 && nstar > 0; q++)
+    GSPH_CUDA(cudaMemcpyAsync(c->star_buf + (size_t) q * c->star_cap, a[q], sizeof(double) * (size_t) nstar,
+                              cudaMemcpyHostToDevice, c->stream));
+  c->nstar = (int) nstar;
+  // the h solve (zeta term) and both force passes depend on the stars
+  c->have_props = c->have_forces = c->have_star_forces = false;
+  return GSPH_OK;
+}
+
+int32_t gsph_update_all_star_gas_forces(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->cfg.self_gravity) return fail(c, GSPH_ERR_STATE, "self_gravity is off in this context");
+  if (!c->nstar) return fail(c, GSPH_ERR_STATE, "no star particles set");
+  cudaSetDevice(c->device);
+  int rc = begin_counters(c);
+  if (rc) return rc;
+  rc = do_star_gas(c);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int32_t gsph_get_star_forces(gsph_ctx* c, double* ax, double* ay, double* az, double* adotx, double* adoty,
+                             double* adotz, double* gpot) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->have_star_forces) return fail(c, GSPH_ERR_STATE, "star <- gas forces not computed");
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  double* out[7] = {ax, ay, az, adotx, adoty, adotz, gpot};
+  const double* src = c->star_buf + 8 * (size_t) c->star_cap;
+  for (int q = 0; q < 7; q++)
+    if (out[q])
+      GSPH_CUDA(cudaMemcpy(out[q], src + (size_t) q * c->star_cap, sizeof(double) * (size_t) c->nstar,
+                           cudaMemcpyDeviceToHost));
+  return GSPH_OK;
+}
+
 int32_t gsph_get_field_device(gsph_ctx* c, int32_t field, double* out) {
   if (!c || !out) return GSPH_ERR_INVALID;
-  const int fi = field_index(field);
+  const int fi = field_index(c, field);
   if (fi < 0) return fail(c, GSPH_ERR_INVALID, "unknown field");
   if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "no results yet");
   cudaSetDevice(c->device);
@@ -802,7 +898,8 @@ int32_t gsph_get_particles_aos(gsph_ctx* c, void* base, int64_t n, int64_t strid
   cudaSetDevice(c->device);
   FieldPtrs fp;
   for (int q = 0; q < kNumFields; q++) fp.f[q] = c->f[q];
-  k_pack_aos<<<grid1(c->n), 256, 0, c->stream>>>(static_cast<unsigned char*>(c->aos), c->n, stride, *off, fp, c->id);
+  k_pack_aos<<<grid1(c->n), 256, 0, c->stream>>>(static_cast<unsigned char*>(c->aos), c->n, stride, *off, fp, c->id,
+                                                  c->nstar ? kFGpotHydro : kFGpot);
   int rc = check_launch(c, "pack");
   if (rc) return rc;
   GSPH_CUDA(cudaMemcpyAsync(base, c->aos, (size_t) n * (size_t) stride, cudaMemcpyDeviceToHost, c->stream));

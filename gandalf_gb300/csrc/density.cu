@@ -17,6 +17,7 @@
 #include "gsph_state.cuh"
 #include "gsph_walk.cuh"
 #include "kernels.cuh"
+#include "stars.cuh"
 
 namespace gsph {
 
@@ -239,7 +240,8 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
     const double drho = -(1.0 / 3.0) * hfin / rho_out;   // h_rho_deriv, src/Headers/Sph.h:264-268
     const double io = 1.0 / (1.0 - drho * om_out);
     p.invomega[slot] = io;
-    p.zeta[slot] = drho * zeta_out * io;
+    const double zsum = prm.stars.n ? zeta_out + star_zeta_sum(prm.stars, xi, yi, zi, hfin) : zeta_out;
+    p.zeta[slot] = drho * zsum * io;
     double u = p.u[slot];
     const double gm1 = prm.gamma_eos - 1.0;
     if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }

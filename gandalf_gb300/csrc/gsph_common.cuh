@@ -18,6 +18,7 @@ constexpr double kBig = 9.9e20;               // src/Headers/Constants.h:72
 constexpr double kKernRange = 2.0;            // M4 support, src/Hydrodynamics/M4Kernel.cpp:37-56
 constexpr double kKernRangeSqd = 4.0;
 constexpr double kGhostRange = 2.5;           // src/Headers/Hydrodynamics.h:52
+constexpr double kTwoPi = 6.28318530717959;   // src/Headers/Constants.h:62
 constexpr int kWarp = 32;
 constexpr unsigned kFull = 0xffffffffu;
 

@@ -4,6 +4,14 @@
 
 namespace gsph {
 
+// Star particles (NbodyParticle r, v, m, h; device arrays of n each) and the star <- gas
+// results the star walk writes.
+struct StarSet {
+  int n;
+  const double *x, *y, *z, *vx, *vy, *vz, *m, *h;
+  double *ax, *ay, *az, *adotx, *adoty, *adotz, *gpot;
+};
+
 struct SphParams {
   double h_fac, h_converge, alpha_visc, beta_visc, gamma_eos, temp0, mu_bar, thetamaxsqd;
   double boxmin[3], boxmax[3], boxsize[3], boxhalf[3];
@@ -11,6 +19,7 @@ struct SphParams {
   int periodic;     // 0 open, 1 periodic in x, y and z
   int multipole;    // 0 monopole, 1 quadrupole
   int self_gravity;
+  StarSet stars;    // n = 0: no stars
 };
 
 // Particles in leaf order (slot = position in the leaf-ordered arrays).
@@ -21,6 +30,7 @@ struct Particles {
   double* h0;                 // h when the tree was built (ghost ranges, cell stock)
   double *rho, *invomega, *zeta, *hfactor, *hrangesqd, *pressure, *sound;
   double *ax, *ay, *az, *agx, *agy, *agz, *gpot, *dudt, *div_v;
+  double* gpot_hydro;         // gpot before the star terms (written only with stars)
 };
 
 // Tree topology (static per N) and stocked cell data (depth-first ids).

@@ -18,6 +18,7 @@
 #include "gsph_walk.cuh"
 #include "kernels.cuh"
 #include "mixed_state.cuh"
+#include "stars.cuh"
 
 namespace gsph {
 
@@ -229,32 +230,78 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
       return true;
     };
 
+    // The candidate's position as a hi + lo float pair (its periodic image for code !=
+    // kNoShift); false: that image does not exist.  ch.w = mass.
+    auto cand_pos = [&](int j, int code, float4& ch, float4& cl) -> bool {
+      if (code == kNoShift) { ch = mp.pos_hi[j]; cl = mp.pos_lo[j]; return true; }
+      const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+      const double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+      const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+      bool ok = true;
+      if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
+      if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
+      if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
+      if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
+      if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
+      if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
+      if (!ok) return false;
+      const double X = __dadd_rn(xj, sx), Y = __dadd_rn(yj, sy), Z = __dadd_rn(zj, sz);
+      ch = make_float4((float) X, (float) Y, (float) Z, mp.pos_hi[j].w);
+      cl = make_float4((float) (X - (double) ch.x), (float) (Y - (double) ch.y), (float) (Z - (double) ch.z), 0.f);
+      return true;
+    };
+
     // Per-particle compact lists of (d^2, m) for the pairs inside 2 hmax_list (the
     // reference's own pre-filter, GradhSphTree.cpp:205-219), built once per attempt; a
-    // particle whose list does not fit loops over the candidates instead.
-    const unsigned gmask = LPG == 32 ? kFull : (((1u << LPG) - 1u) << (g * LPG));
+    // particle whose list does not fit loops over the candidates instead.  The build runs
+    // one candidate per lane (LPG leaves of up to 32/LPG particles per round, coalesced
+    // loads) against every particle of the cell, eight at a time from registers.
+    constexpr int G = 32 / LPG;
     const unsigned ltm = (1u << lane) - 1u;
     float2* clist = compact + g * kcap;
     int ccount = 0;
     const float lim2 = (float) (kKernRangeSqd * hmax_list * hmax_list) * (1.0f + kMargin);
     if (!overflow) {
-      for (int e = 0; e < ncached; e++) {
-        const int tagv = list[e];
-        const int node = tagv & ((1 << kNodeBits) - 1);
-        const int code = tagv >> kNodeBits;
-        const int f = t.cell_first[node], nn = t.cell_n[node];
-        for (int q0 = 0; q0 < nn; q0 += LPG) {
-          const int q = q0 + sl;
-          float d2 = 0.0f, mj = 0.0f;
-          bool keep = false;
-          if (mine && q < nn) keep = cand(f + q, code, d2, mj) && d2 <= lim2;
-          const unsigned b = __ballot_sync(kFull, keep);
-          if (keep) {
-            const int pos = ccount + __popc(b & gmask & ltm);
-            if (pos < kcap) clist[pos] = make_float2(d2, mj);
-          }
-          ccount += __popc(b & gmask);
+      const int ntgt = ncell < G ? ncell : G;
+      for (int gc = 0; gc < ntgt; gc += 8) {
+        float4 th[8], tl[8];
+        int tc[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int tg = gc + u < ntgt ? gc + u : ntgt - 1;
+          th[u] = mp.pos_hi[first + tg];
+          tl[u] = mp.pos_lo[first + tg];
+          tc[u] = 0;
         }
+        for (int e0 = 0; e0 < ncached; e0 += LPG) {
+          const int e = e0 + lane / G, q = lane % G;
+          bool valid = false;
+          float4 ch = make_float4(0.f, 0.f, 0.f, 0.f), cl = ch;
+          if (e < ncached) {
+            const int tagv = list[e];
+            const int node = tagv & ((1 << kNodeBits) - 1);
+            const int code = tagv >> kNodeBits;
+            if (q < t.cell_n[node]) valid = cand_pos(t.cell_first[node] + q, code, ch, cl);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; u++) {
+            if (gc + u >= ntgt) break;
+            const float dx = (ch.x - th[u].x) + (cl.x - tl[u].x);
+            const float dy = (ch.y - th[u].y) + (cl.y - tl[u].y);
+            const float dz = (ch.z - th[u].z) + (cl.z - tl[u].z);
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const bool keep = valid && d2 <= lim2;
+            const unsigned b = __ballot_sync(kFull, keep);
+            if (keep) {
+              const int pos = tc[u] + __popc(b & ltm);
+              if (pos < kcap) compact[(gc + u) * kcap + pos] = make_float2(d2, ch.w);
+            }
+            tc[u] += __popc(b);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          if (gc + u == g) ccount = tc[u];
       }
     }
     const bool use_compact = !overflow && ccount <= kcap;
@@ -400,7 +447,8 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     const double drho = -(1.0 / 3.0) * hfin / rho_out;
     const double io = 1.0 / (1.0 - drho * om_out);
     p.invomega[slot] = io;
-    p.zeta[slot] = drho * zeta_out * io;
+    const double zsum = prm.stars.n ? zeta_out + star_zeta_sum(prm.stars, xi, yi, zi, hfin) : zeta_out;
+    p.zeta[slot] = drho * zsum * io;
     double u = p.u[slot];
     const double gm1 = prm.gamma_eos - 1.0;
     if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
@@ -413,6 +461,15 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
 constexpr int kDensWarps = 4;
 constexpr int kCompactPerWarp = 1536;   // float2 entries shared by the warp's particle groups
 
+// Per-particle compact list capacity, also the stride between the lists of the particle
+// groups of a warp: congruent to LPG modulo 16 so that the groups' reads of 8-byte entries
+// (lane sl of group g reads entry sl + LPG k) fall in distinct shared-memory banks.
+template <int LPG>
+__host__ __device__ constexpr int compact_stride() {
+  return LPG >= 16 ? kCompactPerWarp / (32 / LPG)
+                   : ((kCompactPerWarp / (32 / LPG) - LPG) / 16) * 16 + LPG;
+}
+
 size_t dens_smem_normal() {
   return sizeof(float2) * kDensWarps * kCompactPerWarp + sizeof(int) * kDensWarps * (kDensStack + kDensListNormal);
 }
@@ -420,8 +477,10 @@ size_t dens_smem_wide() {
   return sizeof(float2) * 8 * kCompactPerWarp + sizeof(int) * 8 * (kDensStack + kDensListWide) + sizeof(DensSmem);
 }
 
+// Shared memory limits the warp-per-leaf density kernel to 3 blocks per SM, so the
+// register budget is set for 3 (168 registers a thread).
 template <int LPG>
-__global__ void __launch_bounds__(kDensWarps * 32)
+__global__ void __launch_bounds__(kDensWarps * 32, 3)
 k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
                 HeavyList heavy, bool handover) {
   extern __shared__ float2 s_dyn2[];
@@ -431,7 +490,7 @@ k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams
   const int wib = threadIdx.x >> 5;
   const int leaf = blockIdx.x * kDensWarps + wib;
   if (leaf >= t.nleaf) return;
-  const int kcap = kCompactPerWarp / (32 / LPG);
+  const int kcap = compact_stride<LPG>();
   const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack + wib * kDensStack,
                                        s_list + wib * kDensListNormal, kDensListNormal,
                                        s_compact + wib * kCompactPerWarp, kcap, handover, nullptr);
@@ -443,7 +502,7 @@ k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams
 
 // Heavy cells: 8 warps share each cell's candidates.
 template <int LPG>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 1)
 k_density_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
                      HeavyList heavy) {
   extern __shared__ float2 s_dyn2[];
@@ -452,7 +511,7 @@ k_density_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphP
   int* s_list = s_stack + 8 * kDensStack;
   DensSmem* sm = reinterpret_cast<DensSmem*>(s_list + 8 * kDensListWide);
   const int wib = threadIdx.x >> 5;
-  const int kcap = kCompactPerWarp / (32 / LPG);
+  const int kcap = compact_stride<LPG>();
   const int nh = *heavy.count;
   for (int k = blockIdx.x; k < nh; k += gridDim.x) {
     density_cell<LPG, 8>(t, p, mp, mc, prm, cnt, heavy.leaves[k], s_stack + wib * kDensStack,

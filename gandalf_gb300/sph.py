@@ -71,6 +71,7 @@ class GradhSphTree:
             code = self._lib.gsph_create_error()
             raise GandalfError(f"gsph_create failed: {_native.ERRORS.get(code, code)}")
         self.n = 0
+        self.nstar = 0
 
     def close(self):
         if getattr(self, "_ctx", None):
@@ -108,6 +109,31 @@ class GradhSphTree:
             rc = self._lib.gsph_set_particles(self._ctx, len(arrs[0]), *[_dp(a) for a in arrs])
             self.n = len(arrs[0])
         self._check(rc, "set_particles")
+        if ics.get("stars") is not None:
+            self.set_stars(ics["stars"])
+
+    # ---- star particles (Simulation::ImportArrayNbody) ---------------------------------
+    STAR_KEYS = ("x", "y", "z", "vx", "vy", "vz", "m", "h")
+    STAR_FIELDS = ("ax", "ay", "az", "adotx", "adoty", "adotz", "gpot")
+
+    def set_stars(self, stars: dict | None):
+        """Star particles x y z vx vy vz m h (host arrays); None or empty removes them."""
+        if stars is None or len(stars["x"]) == 0:
+            self._check(self._lib.gsph_set_stars(self._ctx, 0, *([None] * 8)), "set_stars")
+            self.nstar = 0
+            return
+        arrs = [np.ascontiguousarray(stars[k], dtype=np.float64) for k in self.STAR_KEYS]
+        self._check(self._lib.gsph_set_stars(self._ctx, len(arrs[0]), *[_dp(a) for a in arrs]), "set_stars")
+        self.nstar = len(arrs[0])
+
+    def UpdateAllStarGasForces(self):
+        self._check(self._lib.gsph_update_all_star_gas_forces(self._ctx), "UpdateAllStarGasForces")
+
+    def star_forces(self) -> dict:
+        """Gas <- star results of the last star pass: a, adot, gpot per star."""
+        outs = [np.zeros(self.nstar) for _ in self.STAR_FIELDS]
+        self._check(self._lib.gsph_get_star_forces(self._ctx, *[_dp(a) for a in outs]), "star_forces")
+        return dict(zip(self.STAR_FIELDS, outs))
 
     def set_particles_aos(self, records: np.ndarray, offsets: dict):
         """Import a structured array of particle records (byte offsets per field)."""
@@ -144,6 +170,7 @@ class GradhSphTree:
     update_all_sph_properties = UpdateAllSphProperties
     update_all_sph_hydro_forces = UpdateAllSphHydroForces
     update_all_sph_forces = UpdateAllSphForces
+    update_all_star_gas_forces = UpdateAllStarGasForces
 
     # ---- results --------------------------------------------------------------------------
     def field(self, name: str) -> np.ndarray:

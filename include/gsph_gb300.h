@@ -13,6 +13,7 @@
  *                                                                        src/GradhSph/GradhSphTree.cpp:82-271
  *   gsph_update_all_sph_hydro_forces  <- GradhSphTree::UpdateAllSphHydroForces  :279-435
  *   gsph_update_all_sph_forces        <- GradhSphTree::UpdateAllSphForces       :443-657
+ *   gsph_update_all_star_gas_forces   <- HydroTree::UpdateAllStarGasForces src/Tree/HydroTree.cpp:551-654
  *
  * Particles cross the boundary either as structure-of-arrays (plain double pointers) or
  * as the caller's array-of-structures (GradhSphParticle records, Particle.h:285-368)
@@ -32,7 +33,7 @@
 extern "C" {
 #endif
 
-#define GSPH_ABI_VERSION 1
+#define GSPH_ABI_VERSION 2
 
 #define GSPH_OK 0
 #define GSPH_ERR_INVALID -1        /* bad argument or particle data */
@@ -84,7 +85,7 @@ enum gsph_field {
   GSPH_FIELD_H = 0, GSPH_FIELD_RHO, GSPH_FIELD_INVOMEGA, GSPH_FIELD_ZETA, GSPH_FIELD_HFACTOR,
   GSPH_FIELD_PRESSURE, GSPH_FIELD_SOUND, GSPH_FIELD_U, GSPH_FIELD_DIV_V, GSPH_FIELD_DUDT,
   GSPH_FIELD_AX, GSPH_FIELD_AY, GSPH_FIELD_AZ, GSPH_FIELD_AGX, GSPH_FIELD_AGY, GSPH_FIELD_AGZ,
-  GSPH_FIELD_GPOT, GSPH_FIELD_HRANGESQD, GSPH_FIELD_COUNT
+  GSPH_FIELD_GPOT, GSPH_FIELD_HRANGESQD, GSPH_FIELD_GPOT_HYDRO, GSPH_FIELD_COUNT
 };
 
 /* Counters of the last step: interactions evaluated (used for the roofline), the
@@ -136,6 +137,25 @@ int32_t gsph_set_particles_device(gsph_ctx* ctx, int64_t n, const double* x, con
  * can write results back without touching other fields. */
 int32_t gsph_set_particles_aos(gsph_ctx* ctx, const void* base, int64_t n, int64_t stride,
                                const gsph_field_offsets* off);
+
+/* ---- star particles (Simulation::ImportArrayNbody, src/Common/Simulation.cpp:1325-1430;
+ *      the stars a Simulation keeps in Nbody::nbodydata) ---------------------------------- */
+/* Host structure-of-arrays of nstar stars: position, velocity, mass, softening length h.
+ * nstar = 0 removes them.  With stars set, the h solve adds the SPH-star zeta term
+ * (GradhSph::ComputeH, src/GradhSph/GradhSph.cpp:282-297), both gas force passes add the
+ * stars' softened gravity to a, atree and gpot after gpot_hydro is taken
+ * (GradhSph::ComputeStarGravForces, src/GradhSph/GradhSph.cpp:698-743), and gsph_step
+ * with self-gravity also computes the star <- gas forces.  Setting stars invalidates the
+ * solved smoothing lengths and forces. */
+int32_t gsph_set_stars(gsph_ctx* ctx, int64_t nstar, const double* x, const double* y, const double* z,
+                       const double* vx, const double* vy, const double* vz, const double* m,
+                       const double* h);
+/* Gravity of the gas on every star through the gas tree (a, adot and gpot of the gas
+ * alone; the caller adds star-star terms).  Needs self-gravity and a solved h. */
+int32_t gsph_update_all_star_gas_forces(gsph_ctx* ctx);
+/* The star <- gas results into host arrays of nstar doubles (any pointer may be NULL). */
+int32_t gsph_get_star_forces(gsph_ctx* ctx, double* ax, double* ay, double* az, double* adotx,
+                             double* adoty, double* adotz, double* gpot);
 
 /* ---- the step ---------------------------------------------------------------------------- */
 int32_t gsph_build_tree(gsph_ctx* ctx);

@@ -71,8 +71,10 @@ def check_fp64(got: dict, ref: dict, gravity: bool):
         assert_close("gpot", got["gpot"], ref["gpot"], FP64_TOL["gpot"])
 
 
-# Star <- gas results (FP64): summation order and rsqrt/pow differences only.
-STAR_TOL = {"a": 1e-12, "adot": 1e-11, "gpot": 1e-12}
+# Star <- gas results (FP64): summation order and rsqrt/pow differences only.  adot: the
+# reference weighs one of its terms with a single-precision powf (NbodyHermite4.cpp:194),
+# whose last float bit differs between math libraries.
+STAR_TOL = {"a": 1e-12, "adot": 1e-6, "gpot": 1e-12}
 
 
 def check_stars(got: dict, ref: dict):
