@@ -125,13 +125,81 @@ __device__ __forceinline__ double shift_of(int code, int k, const SphParams& prm
 // ==========================================================================================
 constexpr int kDensStack = 1024;
 constexpr int kDensListNormal = 256;    // leaves a warp handles alone
-constexpr int kDensListWide = 1024;     // per warp in the wide kernel
 constexpr int kMaxAttempts = 256;
 
 struct DensSmem {
   double part[8][8][3];   // [warp][group][rho, omega, zeta]
   int flag[8];
 };
+
+// One step of GradhSph::ComputeH's h iteration (src/GradhSph/GradhSph.cpp:206-254) from
+// the kernel sums of the current h (drho = sum m W, dom = sum m h^-1 Womega, dze = sum m
+// Wzeta, before the h^-3 / h^-2 factors): the density, the convergence test against
+// h_fac (m / rho)^(1/3), then a fixed-point step (iterations < 30) or bisection (up to
+// 150).  h_fac (m/rho)^(1/3) = h_fac h w^(-1/3) with w = rho h^3 / m: a float reciprocal
+// cube root refined by one fp64 Newton step (relative error ~1e-14).  Sets done when the
+// particle has finished (converged, left the bracket, aborted with h > hmax_list, or
+// failed to converge).
+__device__ __forceinline__ void h_update(double drho, double dom, double dze, double inv_m, double inv_hfac,
+                                         double invhsqd, double hmax_list, const SphParams& prm, int iteration,
+                                         double& hi, double& invh, double& h_lower, double& h_upper,
+                                         double& hrho_last, double& rho, double& om, double& zeta, double& mloc,
+                                         bool& done, bool& abort_cell, bool& fail) {
+  const double hfac3 = invh * invhsqd;
+  rho = drho * hfac3;
+  om = dom * hfac3;
+  zeta = dze * invhsqd;
+  const double w = drho * inv_m;
+  double r = (double) rcbrtf((float) w);
+  r = r * (4.0 / 3.0 - (w * (1.0 / 3.0)) * (r * r * r));
+  const double hrho = prm.h_fac * hi * r;
+  hrho_last = hrho;
+  if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
+    done = true;
+    return;
+  }
+  if (iteration < 30) {
+    invh = invh * (w * r * r) * inv_hfac;   // 1 / hrho
+    hi = hrho;
+  } else {
+    if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
+    else if (iteration < 150) {
+      if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
+      hi = 0.5 * (h_lower + h_upper);
+    } else {
+      fail = true;
+      done = true;
+      return;
+    }
+    invh = 1.0 / hi;
+  }
+  mloc = fmax(mloc, hi);
+  if (hi > hmax_list) { abort_cell = true; done = true; }
+  else if (!(hi > h_lower && hi < h_upper)) done = true;
+}
+
+// Final per-particle results of the h solve (GradhSph.cpp:262-317): h, rho, hfactor,
+// hrangesqd, invomega, zeta (with the SPH-star term), the EOS quantities.
+__device__ __forceinline__ void finish_density(const Particles& p, const SphParams& prm, int slot, double hfin,
+                                               double rho_out, double om_out, double zeta_out, double xi, double yi,
+                                               double zi) {
+  const double invh = 1.0 / hfin;
+  p.h[slot] = hfin;
+  p.rho[slot] = rho_out;
+  p.hfactor[slot] = invh * invh * invh * invh;
+  p.hrangesqd[slot] = __dmul_rn(__dmul_rn(kKernRangeSqd, hfin), hfin);
+  p.div_v[slot] = 0.0;
+  const double drho = -(1.0 / 3.0) * hfin / rho_out;
+  const double io = 1.0 / (1.0 - drho * om_out);
+  p.invomega[slot] = io;
+  const double zsum = prm.stars.n ? zeta_out + star_zeta_sum(prm.stars, xi, yi, zi, hfin) : zeta_out;
+  p.zeta[slot] = drho * zsum * io;
+  double u = p.u[slot];
+  const double gm1 = prm.gamma_eos - 1.0;
+  if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
+  p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
+  p.pressure[slot] = gm1 * rho_out * u;
+}
 
 template <int LPG, int WARPS>
 __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, const MixedParticles& mp,
@@ -368,42 +436,9 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         for (int w = 0; w < WARPS; w++) { drho += sm->part[w][g][0]; dom += sm->part[w][g][1]; dze += sm->part[w][g][2]; }
         __syncthreads();
       }
-      if (!done) {
-        const double hfac3 = invh * invhsqd;
-        rho = drho * hfac3;
-        om = dom * hfac3;
-        zeta = dze * invhsqd;
-        // h_fac (m/rho)^(1/3) = h_fac h w^(-1/3) with w = rho h^3 / m: float reciprocal
-        // cube root refined by one fp64 Newton step (relative error ~1e-14)
-        const double w = drho * inv_m;
-        double r = (double) rcbrtf((float) w);
-        r = r * (4.0 / 3.0 - (w * (1.0 / 3.0)) * (r * r * r));
-        const double hrho = prm.h_fac * hi * r;
-        hrho_last = hrho;
-        if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
-          done = true;
-        } else {
-          if (iteration < 30) {
-            invh = invh * (w * r * r) * inv_hfac;   // 1 / hrho
-            hi = hrho;
-          } else {
-            if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
-            else if (iteration < 150) {
-              if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
-              hi = 0.5 * (h_lower + h_upper);
-            } else {
-              fail = true;
-              done = true;
-            }
-            invh = 1.0 / hi;
-          }
-          if (!done) {
-            mloc = fmax(mloc, hi);
-            if (hi > hmax_list) { abort_cell = true; done = true; }
-            else if (!(hi > h_lower && hi < h_upper)) done = true;
-          }
-        }
-      }
+      if (!done)
+        h_update(drho, dom, dze, inv_m, inv_hfac, invhsqd, hmax_list, prm, iteration, hi, invh, h_lower, h_upper,
+                 hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
     }
     double mw = mloc;
     for (int o = 16; o > 0; o >>= 1) mw = fmax(mw, __shfl_xor_sync(kFull, mw, o));
@@ -436,26 +471,171 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   unsigned long long tot = pairs;
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
   if (lane == 0) atomicAdd(cnt.density_pairs, tot);
-  if (mine && sl == 0 && wib == 0) {
-    const double hfin = h_out;
-    const double invh = 1.0 / hfin;
-    p.h[slot] = hfin;
-    p.rho[slot] = rho_out;
-    p.hfactor[slot] = invh * invh * invh * invh;
-    p.hrangesqd[slot] = __dmul_rn(__dmul_rn(kKernRangeSqd, hfin), hfin);
-    p.div_v[slot] = 0.0;
-    const double drho = -(1.0 / 3.0) * hfin / rho_out;
-    const double io = 1.0 / (1.0 - drho * om_out);
-    p.invomega[slot] = io;
-    const double zsum = prm.stars.n ? zeta_out + star_zeta_sum(prm.stars, xi, yi, zi, hfin) : zeta_out;
-    p.zeta[slot] = drho * zsum * io;
-    double u = p.u[slot];
-    const double gm1 = prm.gamma_eos - 1.0;
-    if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
-    p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
-    p.pressure[slot] = gm1 * rho_out * u;
-  }
+  if (mine && sl == 0 && wib == 0) finish_density(p, prm, slot, h_out, rho_out, om_out, zeta_out, xi, yi, zi);
   return true;
+}
+
+
+// Heavy leaves: one block per leaf, one warp per particle (particles g, g + 8, ... of the
+// leaf).  Instead of scanning the leaf's whole gather list every iteration, each
+// iteration walks the tree for the particle's own search box r_i +- 2 h_i: every pair
+// inside the kernel support of the current h is inside the leaf's gather box (h stays
+// below hmax_list while the attempt runs), so the sums take the same pairs as the
+// gather-list form.  The cell-level attempt protocol (abort when some h exceeds
+// hmax_list, exact skip-ahead of the 1.05 sequence) is kept across the block.
+constexpr int kPPStack = 1024;
+constexpr int kPPList = 256;
+
+template <int LPG>
+__global__ void __launch_bounds__(256, 2)
+k_density_mixed_pp(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
+                   HeavyList heavy) {
+  __shared__ int s_stack[8][kPPStack];
+  __shared__ int s_list[8][kPPList];
+  __shared__ double s_h0[32];
+  __shared__ double s_mloc[8];
+  constexpr int G = 32 / LPG;   // lanes per leaf when scanning emitted leaves
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* stack = s_stack[wib];
+  int* list = s_list[wib];
+  const int nh = *heavy.count;
+  unsigned long long pairs = 0;
+  bool stack_ok = true, fail = false, unsolved = false;
+  for (int k = blockIdx.x; k < nh; k += gridDim.x) {
+    const int leaf = heavy.leaves[k];
+    const int c = t.leaf_cell[leaf];
+    const int first = t.cell_first[c], ncell = t.cell_n[c];
+    __syncthreads();
+    if (threadIdx.x < ncell) s_h0[threadIdx.x] = p.h[first + threadIdx.x];
+    __syncthreads();
+    double hk = __dmul_rn(1.05, t.geom[c].hmax);
+    bool solved = false;
+    for (int att = 0; att < kMaxAttempts && !solved; att++) {
+      double mloc = 0.0;
+      bool abort_any = false;
+      for (int g = wib; g < ncell; g += 8) {
+        const int slot = first + g;
+        const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
+        const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
+        double hi = s_h0[g], h_lower = 0.0, h_upper = hk;
+        double invh = 1.0 / hi, hrho_last = hi;
+        const double inv_m = 1.0 / mi, inv_hfac = 1.0 / prm.h_fac;
+        double rho = 0.0, om = 0.0, zeta = 0.0;
+        bool done = false, abort_cell = false;
+        int iteration = 0;
+        while (!done) {
+          iteration++;
+          const double invhsqd = invh * invh;
+          const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
+          float srho = 0.0f, som = 0.0f, sze = 0.0f;
+          // the particle's search box, rounded outwards, and its periodic images
+          const double rr = __dmul_rn(kKernRange * (1.0 + 1.0 / 1024.0), hi);
+          double gmin[3] = {xi - rr, yi - rr, zi - rr}, gmax[3] = {xi + rr, yi + rr, zi + rr};
+          int nsh[3] = {1, 1, 1}, sh[3][3];
+          for (int q = 0; q < 3; q++) {
+            sh[q][0] = 1;
+            if (prm.periodic) {
+              if (gmax[q] > prm.boxmax[q]) sh[q][nsh[q]++] = 2;
+              if (gmin[q] < prm.boxmin[q]) sh[q][nsh[q]++] = 0;
+            }
+          }
+          WarpLists L{list, list, list, 0, 0, 0, kPPList};
+          auto consume = [&]() {
+            for (int e0 = 0; e0 < L.na; e0 += LPG) {
+              const int e = e0 + lane / G, q = lane % G;
+              if (e >= L.na) continue;
+              const int tagv = list[e];
+              const int node = tagv & ((1 << kNodeBits) - 1);
+              const int code = tagv >> kNodeBits;
+              if (q >= t.cell_n[node]) continue;
+              const int j = t.cell_first[node] + q;
+              float dx, dy, dz, mj;
+              if (code == kNoShift) {
+                const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+                mj = pjh.w;
+                dx = (pjh.x - pih.x) + (pjl.x - pil.x);
+                dy = (pjh.y - pih.y) + (pjl.y - pil.y);
+                dz = (pjh.z - pih.z) + (pjl.z - pil.z);
+              } else {
+                const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+                const double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+                const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+                bool ok = true;
+                if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
+                if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
+                if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
+                if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
+                if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
+                if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
+                if (!ok) continue;
+                mj = mp.pos_hi[j].w;
+                dx = (float) (__dadd_rn(xj, sx) - xi);
+                dy = (float) (__dadd_rn(yj, sy) - yi);
+                dz = (float) (__dadd_rn(zj, sz) - zi);
+              }
+              const float ssqd = (dx * dx + dy * dy + dz * dz) * invhsqd_f;
+              if (ssqd < 4.0f) {
+                const float sv = fsqrt_pos(ssqd);
+                srho = fmaf(mj, m4f_w0(sv), srho);
+                som = fmaf(mj * invh_f, m4f_womega(sv), som);
+                sze = fmaf(mj, m4f_wzeta(sv), sze);
+                pairs++;
+              }
+            }
+            __syncwarp();
+          };
+          for (int a0 = 0; a0 < nsh[0]; a0++)
+            for (int a1 = 0; a1 < nsh[1]; a1++)
+              for (int a2 = 0; a2 < nsh[2]; a2++) {
+                const int code = sh[0][a0] + 3 * sh[1][a1] + 9 * sh[2][a2];
+                float bmin[3], bmax[3];
+                for (int q = 0; q < 3; q++) {
+                  const double sft = shift_of(code, q, prm);
+                  bmin[q] = __double2float_rd(gmin[q] - sft);
+                  bmax[q] = __double2float_ru(gmax[q] - sft);
+                }
+                auto decide = [&](int node, int level) -> int {
+                  if (t.cell_n[node] == 0) return kSkip;
+                  if (!fbox_overlap(bmin, bmax, mc.bbmin[node], mc.bbmax[node])) return kSkip;
+                  return level == t.ltot ? kEmitA : kOpen;
+                };
+                auto tag = [&](int node, int) { return node | (code << kNodeBits); };
+                stack_ok = warp_walk(0, t.ltot, t.cell_level, stack, kPPStack, L, decide, tag, consume) && stack_ok;
+                consume();
+                L.na = 0;
+              }
+          for (int o = 16; o > 0; o >>= 1) {
+            srho += __shfl_xor_sync(kFull, srho, o);
+            som += __shfl_xor_sync(kFull, som, o);
+            sze += __shfl_xor_sync(kFull, sze, o);
+          }
+          h_update(srho, som, sze, inv_m, inv_hfac, invhsqd, hk, prm, iteration, hi, invh, h_lower, h_upper,
+                   hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
+          if (!stack_ok) done = true;
+        }
+        abort_any = abort_any || abort_cell;
+        if (!abort_cell && lane == 0)
+          finish_density(p, prm, slot, fmax(hrho_last, h_lower), rho, om, zeta, xi, yi, zi);
+      }
+      if (lane == 0) s_mloc[wib] = mloc;
+      abort_any = __syncthreads_or(abort_any);
+      if (!abort_any) { solved = true; break; }
+      double mc_ = 0.0;
+      for (int w = 0; w < 8; w++) mc_ = fmax(mc_, s_mloc[w]);
+      __syncthreads();
+      int guard = 0;
+      do { hk = __dmul_rn(1.05, hk); } while (hk < mc_ && ++guard < 100000);
+    }
+    if (!solved) unsolved = true;
+  }
+  unsigned long long tot = pairs;
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
+  if (lane == 0) {
+    atomicAdd(cnt.density_pairs, tot);
+    if (!stack_ok) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
+    if (fail) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
+    if (unsolved) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
+  }
 }
 
 constexpr int kDensWarps = 4;
@@ -472,9 +652,6 @@ __host__ __device__ constexpr int compact_stride() {
 
 size_t dens_smem_normal() {
   return sizeof(float2) * kDensWarps * kCompactPerWarp + sizeof(int) * kDensWarps * (kDensStack + kDensListNormal);
-}
-size_t dens_smem_wide() {
-  return sizeof(float2) * 8 * kCompactPerWarp + sizeof(int) * 8 * (kDensStack + kDensListWide) + sizeof(DensSmem);
 }
 
 // Shared memory limits the warp-per-leaf density kernel to 3 blocks per SM, so the
@@ -500,26 +677,6 @@ k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams
   }
 }
 
-// Heavy cells: 8 warps share each cell's candidates.
-template <int LPG>
-__global__ void __launch_bounds__(256, 1)
-k_density_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
-                     HeavyList heavy) {
-  extern __shared__ float2 s_dyn2[];
-  float2* s_compact = s_dyn2;
-  int* s_stack = reinterpret_cast<int*>(s_dyn2 + 8 * kCompactPerWarp);
-  int* s_list = s_stack + 8 * kDensStack;
-  DensSmem* sm = reinterpret_cast<DensSmem*>(s_list + 8 * kDensListWide);
-  const int wib = threadIdx.x >> 5;
-  const int kcap = compact_stride<LPG>();
-  const int nh = *heavy.count;
-  for (int k = blockIdx.x; k < nh; k += gridDim.x) {
-    density_cell<LPG, 8>(t, p, mp, mc, prm, cnt, heavy.leaves[k], s_stack + wib * kDensStack,
-                         s_list + wib * kDensListWide, kDensListWide, s_compact + wib * kCompactPerWarp, kcap,
-                         false, sm);
-    __syncthreads();
-  }
-}
 
 // ==========================================================================================
 // Forces, mixed form.
@@ -1099,11 +1256,7 @@ int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles
   (void) max_leaf;
   GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, blocks, kDensWarps * 32, smem_n, t, p, mp, mc, prm, cnt, heavy,
                  true)
-  const size_t smem = dens_smem_wide();
-  for (auto f : {k_density_mixed_wide<1>, k_density_mixed_wide<2>, k_density_mixed_wide<4>,
-                 k_density_mixed_wide<8>, k_density_mixed_wide<16>, k_density_mixed_wide<32>})
-    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-  GSPH_MIXED_LPG(k_density_mixed_wide, lanes_per_particle, 152, 256, smem, t, p, mp, mc, prm, cnt, heavy)
+  GSPH_MIXED_LPG(k_density_mixed_pp, lanes_per_particle, 2 * 152, 256, 0, t, p, mp, mc, prm, cnt, heavy)
   return 2;
 }
 
