@@ -45,6 +45,10 @@ UNIT = "particle updates/s"
 #   monopole cell term                  NeighbourSearch.h:359-373     24
 FLOPS = dict(density=42, hydro=80, hydro_grav=145, direct=24, quad=82, mono=24)
 
+# DRAM bytes (read + write) per force pass, from one-pass ncu captures of the force kernels
+# (profiles/forces_density_mixed_plummer262k_dram.md): (workload, n, form) -> bytes.
+FORCE_TRAFFIC = {("plummer_sphere", 262144, "mixed"): 49.09e6 + 0.697e6 + 5.79e6}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -57,6 +61,8 @@ def parse():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="launch each step's kernels on the stream "
+                    "instead of replaying the captured CUDA graph")
     return ap.parse_args()
 
 
@@ -176,7 +182,7 @@ def algorithmic_flops(st, gravity, quad=True):
     return fk, st["density_pairs"] * FLOPS["density"]
 
 
-def run_form(c, params, precision, steps, warmup, flush):
+def run_form(c, params, precision, steps, warmup, flush, graph=True):
     import torch
     from gandalf_gb300.sph import GradhSphTree
 
@@ -187,7 +193,7 @@ def run_form(c, params, precision, steps, warmup, flush):
     t.set_stream(stream.cuda_stream)
     for _ in range(warmup):
         t.set_particles(dev)
-        t.step()
+        t.step(graph=graph)
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     per = {"ms_build": 0.0, "ms_density": 0.0, "ms_hmax": 0.0, "ms_forces": 0.0}
@@ -197,7 +203,7 @@ def run_form(c, params, precision, steps, warmup, flush):
         flush.zero_()                      # L2 flush, outside the timed pair
         ev[k][0].record(stream)
         t.set_particles(dev)
-        t.step()
+        t.step(graph=graph)
         ev[k][1].record(stream)
         st = t.stats()
         for key in per:
@@ -211,7 +217,7 @@ def run_form(c, params, precision, steps, warmup, flush):
             "launches": launches, "results": out}
 
 
-def run_e2e(c, params, precision, steps, warmup):
+def run_e2e(c, params, precision, steps, warmup, graph=True):
     """Records in, step, records out through the C ABI; separate pinned input and output
     record buffers so every step starts from the same inputs, as the device-resident
     loop does."""
@@ -222,13 +228,13 @@ def run_e2e(c, params, precision, steps, warmup):
     t = GradhSphTree(params, precision=precision, device=torch.cuda.current_device())
     for _ in range(max(1, warmup)):
         t.set_particles_aos(rec, off)
-        t.step()
+        t.step(graph=graph)
         t.get_particles_aos(orec, off)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         t.set_particles_aos(rec, off)
-        t.step()
+        t.step(graph=graph)
         t.get_particles_aos(orec, off)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -310,7 +316,7 @@ def main():
                 if world > 1:
                     dist.barrier()
                 torch.cuda.synchronize()
-                results[form] = run_form(c, params, form, args.steps, args.warmup, flush)
+                results[form] = run_form(c, params, form, args.steps, args.warmup, flush, not args.no_graph)
                 if world > 1:
                     dist.barrier()
                 torch.cuda.synchronize()
@@ -330,7 +336,7 @@ def main():
     value = world * n * args.steps / (ms * 1e-3)
     e2e = None
     if not args.no_e2e:
-        E = run_e2e(c, params, head, max(1, min(args.steps, 5)), 1)
+        E = run_e2e(c, params, head, max(1, min(args.steps, 5)), 1, not args.no_graph)
         k = max(1, min(args.steps, 5))
         e2e = {"value": n * k / E["wall"] * world, "unit": UNIT, "h2d_bytes_per_step": E["bytes"],
                "d2h_bytes_per_step": E["bytes"], "path": "gsph_set_particles_aos + gsph_step + "
@@ -342,7 +348,8 @@ def main():
     achieved = f_force / (R["per"]["ms_forces"] * 1e-3) / 1e12
     roof = {"bound": "fp64" if fp64 else "fp32", "kernel": "all-forces" if gravity else "hydro-forces",
             "achieved": achieved, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
-            "frac": achieved / (peak_gf / 1e3) if peak_gf > 0 else None, "traffic": None,
+            "frac": achieved / (peak_gf / 1e3) if peak_gf > 0 else None,
+            "traffic": FORCE_TRAFFIC.get((args.workload, n, head)),
             "peak_source": "measured FMA-loop throughput of this GPU (gsph_fma_peak_gflops); "
                            "MEASURED_PEAKS.json holds HBM and bf16 figures only",
             "flops_per_launch": f_force, "ms_per_launch": R["per"]["ms_forces"]}
@@ -372,7 +379,7 @@ def main():
         forms_out["mixed_vs_fp64_rel_err"] = errs
         forms_out["speedup_mixed_over_fp64"] = results["fp64"]["ms_total"] / results["mixed"]["ms_total"]
     cfg = workload_config(args.workload, c)
-    cfg.update(precision=head, l2="flushed between timed steps (256 MiB write, outside the timed span)",
+    cfg.update(precision=head, cuda_graph=not args.no_graph, l2="flushed between timed steps (256 MiB write, outside the timed span)",
                parallelism=f"replicas{world}")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,

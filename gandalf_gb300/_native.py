@@ -71,6 +71,7 @@ SIGNATURES = {
     "gsph_update_all_sph_hydro_forces": (_I32, [_P]),
     "gsph_update_all_sph_forces": (_I32, [_P]),
     "gsph_step": (_I32, [_P]),
+    "gsph_step_graph": (_I32, [_P]),
     "gsph_get_field": (_I32, [_P, _I32, _D]),
     "gsph_get_field_device": (_I32, [_P, _I32, _P]),
     "gsph_get_particles_aos": (_I32, [_P, _P, _I64, _I64, ctypes.POINTER(FieldOffsets)]),

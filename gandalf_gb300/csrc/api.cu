@@ -92,6 +92,12 @@ struct gsph_ctx {
   int nstar = 0, star_cap = 0;
   double* star_buf = nullptr;
   bool have_star_forces = false;
+  // CUDA graph of the whole step (gsph_step_graph), valid for one capture key
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_valid = false;
+  bool capturing = false;
+  unsigned graph_launches = 0;
   // timing
   cudaEvent_t ev[5] = {};
   gsph_stats last{};
@@ -125,6 +131,14 @@ void free_all(gsph_ctx* c) {
   c->bufs.clear();
   c->cap = 0;
   c->cap_ncell = 0;
+}
+
+void drop_graph(gsph_ctx* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+  c->graph_valid = false;
 }
 
 template <class T>
@@ -236,6 +250,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
     c->rec_bytes = 0;   // recording buffers were freed with the rest
     c->rec_sph_cnt = nullptr;
   }
+  if (fresh || n != c->n || ltot != c->ltot) drop_graph(c);
   if (fresh || n != c->n || ltot != c->ltot || !c->have_particles) {
     Shape s;
     make_shape(n, ltot, s);
@@ -471,6 +486,12 @@ int read_status(gsph_ctx* c) {
   return GSPH_OK;
 }
 
+// Phase timestamps; inside a graph capture they become event-record nodes of the graph.
+void mark(gsph_ctx* c, int q) {
+  if (c->capturing) cudaEventRecordWithFlags(c->ev[q], c->stream, cudaEventRecordExternal);
+  else cudaEventRecord(c->ev[q], c->stream);
+}
+
 int do_build(gsph_ctx* c) {
   if (!c->have_particles) return fail(c, GSPH_ERR_STATE, "no particles imported");
   BuildArgs a{};
@@ -510,7 +531,7 @@ int do_props(gsph_ctx* c) {
   int rc = check_launch(c, "density");
   if (rc) return rc;
   if (mixed(c)) GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
-  cudaEventRecord(c->ev[2], c->stream);
+  mark(c, 2);
   launch_update_hmax(t, p, c->stream);
   c->launches += 1;
   if (mixed(c)) {
@@ -574,6 +595,7 @@ int ensure_recording(gsph_ctx* c) {
   const size_t need = (size_t) c->n * (sizeof(int) * (1 + c->rec_max) + 2 * sizeof(unsigned long long)) +
                       (size_t) c->nleaf * 2 * sizeof(unsigned long long);
   if (c->rec_sph_cnt && c->rec_bytes >= need) return GSPH_OK;
+  drop_graph(c);   // a captured step holds the old recording buffers
   int rc = alloc(c, c->rec_sph_cnt, c->n);
   if (!rc) rc = alloc(c, c->rec_sph_ids, (size_t) c->n * c->rec_max);
   if (!rc) rc = alloc(c, c->rec_dir_cnt, c->n);
@@ -644,6 +666,7 @@ void gsph_destroy(gsph_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
   free_all(c);
   if (c->aos) cudaFree(c->aos);
   if (c->star_buf) cudaFree(c->star_buf);
@@ -775,36 +798,87 @@ int32_t gsph_update_all_sph_forces(gsph_ctx* c) {
   return read_status(c);
 }
 
-int32_t gsph_step(gsph_ctx* c) {
-  if (!c) return GSPH_ERR_INVALID;
-  cudaSetDevice(c->device);
-  int rc = ensure_recording(c);
+namespace {
+
+// Everything one step launches, in stream order, with no host synchronisation (so that it
+// can also be captured into a graph).
+int step_body(gsph_ctx* c) {
+  int rc = begin_counters(c);
   if (rc) return rc;
-  rc = begin_counters(c);
-  if (rc) return rc;
-  cudaEventRecord(c->ev[0], c->stream);
+  mark(c, 0);
   rc = do_build(c);
   if (rc) return rc;
-  cudaEventRecord(c->ev[1], c->stream);
+  mark(c, 1);
   rc = do_props(c);
   if (rc) return rc;
-  cudaEventRecord(c->ev[3], c->stream);
+  mark(c, 3);
   rc = do_forces(c, c->cfg.self_gravity != 0);
   if (rc) return rc;
   if (c->nstar && c->cfg.self_gravity) {
     rc = do_star_gas(c);
     if (rc) return rc;
   }
-  cudaEventRecord(c->ev[4], c->stream);
-  rc = read_status(c);
+  mark(c, 4);
+  return GSPH_OK;
+}
+
+int finish_step(gsph_ctx* c) {
+  const int rc = read_status(c);
   float ms[4] = {0, 0, 0, 0};
-  cudaEventElapsedTime(&ms[0], c->ev[0], c->ev[1]);
-  cudaEventElapsedTime(&ms[1], c->ev[1], c->ev[2]);
-  cudaEventElapsedTime(&ms[2], c->ev[2], c->ev[3]);
-  cudaEventElapsedTime(&ms[3], c->ev[3], c->ev[4]);
+  for (int q = 0; q < 4; q++) {
+    const int a = q, b = q + 1;
+    if (cudaEventElapsedTime(&ms[q], c->ev[a], c->ev[b]) != cudaSuccess) ms[q] = 0.0f;
+  }
+  (void) cudaGetLastError();   // a phase event that was not recorded leaves no error behind
   c->last.ms_build = ms[0]; c->last.ms_density = ms[1]; c->last.ms_hmax = ms[2]; c->last.ms_forces = ms[3];
   c->last.ms_total = ms[0] + ms[1] + ms[2] + ms[3];
   return rc;
+}
+
+}  // namespace
+
+int32_t gsph_step(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  cudaSetDevice(c->device);
+  int rc = ensure_recording(c);
+  if (rc) return rc;
+  rc = step_body(c);
+  if (rc) return rc;
+  return finish_step(c);
+}
+
+int32_t gsph_step_graph(gsph_ctx* c) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->have_particles) return fail(c, GSPH_ERR_STATE, "no particles imported");
+  cudaSetDevice(c->device);
+  int rc = ensure_recording(c);
+  if (rc) return rc;
+  if (!c->graph_valid) {
+    drop_graph(c);
+    // capture on the context's own stream (a caller's stream may be the legacy default
+    // stream, which cannot be captured); the graph is launched on the current stream
+    GSPH_CUDA(cudaStreamSynchronize(c->stream));
+    cudaStream_t saved = c->stream;
+    c->stream = c->own_stream;
+    GSPH_CUDA(cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeRelaxed));
+    c->capturing = true;
+    rc = step_body(c);
+    c->capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->own_stream, &g);
+    c->stream = saved;
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    c->graph = g;
+    GSPH_CUDA(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+    c->graph_launches = c->launches;
+    c->graph_valid = true;
+  }
+  GSPH_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
+  c->launches = c->graph_launches;
+  c->have_tree = c->have_props = c->have_forces = true;
+  c->have_star_forces = c->nstar && c->cfg.self_gravity;
+  return finish_step(c);
 }
 
 int32_t gsph_set_stars(gsph_ctx* c, int64_t nstar, const double* x, const double* y, const double* z,
@@ -823,6 +897,7 @@ int32_t gsph_set_stars(gsph_ctx* c, int64_t nstar, const double* x, const double
   cudaSetDevice(c->device);
   GSPH_CUDA(cudaStreamSynchronize(c->stream));
   if (nstar > c->star_cap) {
+    drop_graph(c);
     if (c->star_buf) cudaFree(c->star_buf);
     c->star_buf = nullptr;
     c->star_cap = 0;
@@ -832,6 +907,7 @@ int32_t gsph_set_stars(gsph_ctx* c, int64_t nstar, const double* x, const double
   for (int q = 0; q < 8 && nstar > 0; q++)
     GSPH_CUDA(cudaMemcpyAsync(c->star_buf + (size_t) q * c->star_cap, a[q], sizeof(double) * (size_t) nstar,
                               cudaMemcpyHostToDevice, c->stream));
+  if ((int) nstar != c->nstar || nstar > c->star_cap) drop_graph(c);
   c->nstar = (int) nstar;
   // the h solve (zeta term) and both force passes depend on the stars
   c->have_props = c->have_forces = c->have_star_forces = false;
@@ -917,6 +993,7 @@ int32_t gsph_get_stats(gsph_ctx* c, gsph_stats* out) {
 int32_t gsph_set_recording(gsph_ctx* c, int32_t enable, int32_t max_sph) {
   if (!c) return GSPH_ERR_INVALID;
   if (enable && (max_sph < 1 || max_sph > 4096)) return fail(c, GSPH_ERR_INVALID, "max_sph must be 1..4096");
+  if ((enable ? 1 : 0) != c->record || (enable && max_sph != c->rec_max)) drop_graph(c);
   c->record = enable ? 1 : 0;
   if (enable && max_sph != c->rec_max) { c->rec_sph_cnt = nullptr; c->rec_bytes = 0; }
   c->rec_max = enable ? max_sph : 0;

@@ -162,9 +162,13 @@ class GradhSphTree:
     def UpdateAllSphForces(self):
         self._check(self._lib.gsph_update_all_sph_forces(self._ctx), "UpdateAllSphForces")
 
-    def step(self):
-        """BuildTree + UpdateAllSphProperties + the configured force pass."""
-        self._check(self._lib.gsph_step(self._ctx), "step")
+    def step(self, graph: bool = False):
+        """BuildTree + UpdateAllSphProperties + the configured force pass (graph=True:
+        replayed from a captured CUDA graph)."""
+        if graph:
+            self._check(self._lib.gsph_step_graph(self._ctx), "step_graph")
+        else:
+            self._check(self._lib.gsph_step(self._ctx), "step")
 
     build_tree = BuildTree
     update_all_sph_properties = UpdateAllSphProperties

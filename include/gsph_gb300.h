@@ -164,6 +164,11 @@ int32_t gsph_update_all_sph_hydro_forces(gsph_ctx* ctx);
 int32_t gsph_update_all_sph_forces(gsph_ctx* ctx);        /* hydro + self-gravity */
 /* build + properties + forces (hydro only or hydro + gravity, as configured) */
 int32_t gsph_step(gsph_ctx* ctx);
+/* The same step replayed from a CUDA graph: the step's launches are captured once and
+ * re-captured automatically when the particle count, the stars or the recording setting
+ * change (the particle values may change freely between calls).  Results are identical
+ * to gsph_step's. */
+int32_t gsph_step_graph(gsph_ctx* ctx);
 
 /* ---- results ----------------------------------------------------------------------------- */
 /* One field for all particles in input order into host memory (n doubles). */
