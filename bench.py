@@ -66,6 +66,106 @@ def parse():
     return ap.parse_args()
 
 
+def ensemble_main(args, rank, world, local):
+    """64 periodic KH boxes of log-uniform N (4,096..131,072), hydro only, mixed form:
+    one batched step (persistent launches over all boxes' leaf cells, one CUDA graph)
+    against the same 64 simulations stepped one after another (each from its own graph)."""
+    import torch
+    from gandalf_gb300 import ics as ics_mod
+    from gandalf_gb300 import _native
+    from gandalf_gb300 import build as gbuild
+    from gandalf_gb300.sph import GradhSphBatch, GradhSphTree
+    gbuild.build()
+    lib = _native.load()
+    boxes = ics_mod.kh_ensemble(64, 4096, 131072, seed=2024 + rank)
+    ntot = sum(len(b["x"]) for b in boxes)
+    trees = []
+    for c in boxes:
+        c = dict(c)
+        params = c.pop("params")
+        t = GradhSphTree(params, precision="mixed", device=local)
+        t.set_particles(c)
+        trees.append(t)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    batch = GradhSphBatch(trees)
+    with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            batch.step()
+        ms_batch = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            batch.step()
+            ms_batch += batch.stats()["ms"]
+        # the same simulations one after another, each replayed from its own graph
+        for t in trees:
+            t.step(graph=True)
+        torch.cuda.synchronize()
+        ms_seq = 0.0
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream = torch.cuda.current_stream()
+        for t in trees:
+            t.set_stream(stream.cuda_stream)
+        for _ in range(args.steps):
+            flush.zero_()
+            ev0.record(stream)
+            for t in trees:
+                t.step(graph=True)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms_seq += ev0.elapsed_time(ev1)
+    clocks = clk.summary()
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms_batch], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_batch = float(tt.item())
+    counts = {k: sum(t.stats()[k] for t in trees) for k in ("density_pairs", "hydro_pairs", "exact_checks")}
+    flops = counts["density_pairs"] * FLOPS["density"] + counts["hydro_pairs"] * FLOPS["hydro"]
+    peak_gf = lib.gsph_fma_peak_gflops(local, 0)
+    achieved = flops / (ms_batch / args.steps * 1e-3) / 1e12
+    # end to end: host SoA in, batch step, per-box results out
+    keys = ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")
+    hbytes = 0
+    t0 = time.perf_counter()
+    k_e2e = max(1, min(args.steps, 3))
+    for _ in range(k_e2e):
+        for t, c in zip(trees, boxes):
+            t.set_particles({k: c[k] for k in keys})
+        batch.step()
+        for t in trees:
+            for f in ("h", "rho", "ax", "ay", "az", "dudt"):
+                t.field(f)
+    wall = time.perf_counter() - t0
+    hbytes_in = ntot * 8 * len(keys)
+    hbytes_out = ntot * 8 * 6
+    launches = batch.stats()["launches"]
+    batch.close()
+    for t in trees:
+        t.close()
+    value = world * ntot * args.steps / (ms_batch * 1e-3)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_batch / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pairs / f64 positions", "data": "synthetic",
+            "config": {"workload": "kh_ensemble", "boxes": 64, "n_total": ntot,
+                       "n_per_box": [min(len(b["x"]) for b in boxes), max(len(b["x"]) for b in boxes)],
+                       "box": [1.0, 1.0, 0.25], "boundaries": "periodic", "nleafmax": 8, "precision": "mixed",
+                       "cuda_graph": True, "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": world * ntot * k_e2e / wall, "unit": UNIT, "h2d_bytes_per_step": hbytes_in,
+                    "d2h_bytes_per_step": hbytes_out,
+                    "path": "gsph_set_particles + gsph_batch_step + gsph_get_field per box"},
+            "gpu_launches": launches * args.steps,
+            "roofline": {"bound": "fp32", "kernel": "whole batch step (density + hydro)", "achieved": achieved,
+                         "peak": peak_gf / 1e3, "unit": "TFLOP/s", "frac": achieved / (peak_gf / 1e3),
+                         "traffic": None, "peak_source": "measured FMA-loop throughput (gsph_fma_peak_gflops)"},
+            "sequential": {"value": world * ntot * args.steps / (ms_seq * 1e-3), "ms_per_step": ms_seq / args.steps,
+                           "how": "the 64 simulations stepped one after another, each from its own CUDA graph"},
+            "speedup_batch_over_sequential": ms_seq / ms_batch, "counts": counts, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def workload(name, n):
     from gandalf_gb300 import ics
     if name == "plummer_sphere":
@@ -299,6 +399,11 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.workload == "kh_ensemble":
+        ensemble_main(args, rank, world, local)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     from gandalf_gb300 import _native
     from gandalf_gb300 import build as gbuild
     gbuild.build()

@@ -89,6 +89,11 @@ SIGNATURES = {
     "gsph_set_stars": (_I32, [_P, _I64] + [_D] * 8),
     "gsph_update_all_star_gas_forces": (_I32, [_P]),
     "gsph_get_star_forces": (_I32, [_P] + [_D] * 7),
+    "gsph_batch_create": (_P, [ctypes.POINTER(_P), _I32]),
+    "gsph_batch_destroy": (None, [_P]),
+    "gsph_batch_step": (_I32, [_P]),
+    "gsph_batch_last_error": (ctypes.c_char_p, [_P]),
+    "gsph_batch_stats": (_I32, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)]),
 }
 
 ABI_VERSION = 2

@@ -18,6 +18,7 @@
 #include "../../include/gsph_gb300.h"
 #include "gsph_state.cuh"
 #include "kernels.cuh"
+#include "batch.cuh"
 #include "mixed_state.cuh"
 #include "stars.cuh"
 #include "tree.cuh"
@@ -1088,6 +1089,260 @@ int32_t gsph_get_tree(gsph_ctx* c, int32_t* cell_n, int32_t* cell_first, int32_t
       r[29] = cf[q]; r[30] = 0;
     }
   }
+  return GSPH_OK;
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// Batches of simulations (gsph_batch_*): one persistent launch per pass over the leaf
+// cells of all simulations, the per-simulation tree builds and cell updates as parallel
+// branches of one CUDA graph.
+// ======================================================================================
+struct gsph_batch {
+  std::vector<gsph_ctx*> ctx;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  SimDesc* d_sims = nullptr;
+  int *d_start = nullptr, *d_hstart = nullptr, *d_next = nullptr;
+  std::vector<int> key_n, key_cap, key_rec;
+  std::vector<const void*> key_ptr;
+  bool prepared = false, gravity = false;
+  int lpg = 4;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t fork[3] = {};
+  std::vector<cudaEvent_t> join;   // 3 per simulation
+  cudaEvent_t ev[2] = {};
+  unsigned launches = 0;
+  float ms = 0.0f;
+  std::string err;
+};
+
+namespace {
+
+int bfail(gsph_batch* b, int code, const std::string& msg) {
+  b->err = msg;
+  return code;
+}
+
+void batch_drop_graph(gsph_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+bool batch_stale(const gsph_batch* b) {
+  if (!b->prepared) return true;
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    const gsph_ctx* c = b->ctx[i];
+    if (c->n != b->key_n[i] || c->cap != b->key_cap[i] || c->record != b->key_rec[i] ||
+        (const void*) c->rec_sph_cnt != b->key_ptr[i])
+      return true;
+  }
+  return false;
+}
+
+// Upload the simulations' descriptors and leaf prefix sums (host-synchronous).
+int batch_prepare(gsph_batch* b) {
+  const int ns = (int) b->ctx.size();
+  std::vector<SimDesc> d(ns);
+  std::vector<int> start(ns + 1, 0);
+  b->lpg = 32;
+  b->key_n.assign(ns, 0); b->key_cap.assign(ns, 0); b->key_rec.assign(ns, 0); b->key_ptr.assign(ns, nullptr);
+  for (int i = 0; i < ns; i++) {
+    gsph_ctx* c = b->ctx[i];
+    if (!c->have_particles) return bfail(b, GSPH_ERR_STATE, "a simulation of the batch has no particles");
+    if (c->nstar) return bfail(b, GSPH_ERR_UNSUPPORTED, "star particles are not supported in batches");
+    int rc = ensure_recording(c);
+    if (rc) return bfail(b, rc, c->err);
+    d[i] = SimDesc{make_tree(c), make_particles(c), make_mixed_particles(c), make_mixed_cells(c), make_params(c),
+                   make_counters(c), HeavyList{c->heavy_leaves, c->heavy_count}};
+    start[i + 1] = start[i] + c->nleaf;
+    b->lpg = std::min(b->lpg, c->lpg);
+    b->key_n[i] = c->n; b->key_cap[i] = c->cap; b->key_rec[i] = c->record; b->key_ptr[i] = c->rec_sph_cnt;
+  }
+  cudaError_t e = cudaMemcpy(b->d_sims, d.data(), sizeof(SimDesc) * ns, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_start, start.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bfail(b, GSPH_ERR_CUDA, std::string("batch upload: ") + cudaGetErrorString(e));
+  batch_drop_graph(b);
+  b->prepared = true;
+  return GSPH_OK;
+}
+
+// The batch step in stream order (captured into the graph): per-simulation branches
+// fork from and join the batch stream around each batched pass.
+int batch_body(gsph_batch* b) {
+  const int ns = (int) b->ctx.size();
+  BatchQueue q{ns, b->d_sims, b->d_start, b->d_hstart, b->d_next};
+  cudaStream_t o = b->stream;
+  b->launches = 0;
+  cudaEventRecordWithFlags(b->ev[0], o, cudaEventRecordExternal);
+  auto branches = [&](int phase, auto&& work) -> int {
+    cudaEventRecord(b->fork[phase], o);
+    for (int i = 0; i < ns; i++) {
+      gsph_ctx* c = b->ctx[i];
+      c->stream = c->own_stream;
+      cudaStreamWaitEvent(c->stream, b->fork[phase], 0);
+      const int rc = work(c);
+      if (rc) return bfail(b, rc, c->err);
+      cudaEventRecord(b->join[3 * i + phase], c->stream);
+      cudaStreamWaitEvent(o, b->join[3 * i + phase], 0);
+    }
+    return GSPH_OK;
+  };
+  int rc = branches(0, [&](gsph_ctx* c) -> int {
+    int r = begin_counters(c);
+    if (!r) r = do_build(c);
+    if (!r && cudaMemsetAsync(c->heavy_count, 0, 4 * sizeof(int), c->stream) != cudaSuccess) r = GSPH_ERR_CUDA;
+    return r;
+  });
+  if (rc) return rc;
+  b->launches += (unsigned) launch_batch_density(q, b->lpg, o);
+  rc = branches(1, [&](gsph_ctx* c) -> int {
+    const Tree t = make_tree(c);
+    const Particles p = make_particles(c);
+    GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    GSPH_CUDA(cudaMemsetAsync(c->heavy_count, 0, sizeof(int), c->stream));
+    launch_update_hmax(t, p, c->stream);
+    launch_mixed_prep_hydro(t, p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
+    c->launches += 3;
+    if (c->record && c->rec_sph_cnt) {
+      GSPH_CUDA(cudaMemsetAsync(c->rec_sph_cnt, 0, sizeof(int) * (size_t) c->n, c->stream));
+      GSPH_CUDA(cudaMemsetAsync(c->rec_dir_cnt, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));
+      GSPH_CUDA(cudaMemsetAsync(c->rec_dir_hash, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));
+      GSPH_CUDA(cudaMemsetAsync(c->rec_cell_cnt, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
+      GSPH_CUDA(cudaMemsetAsync(c->rec_cell_hash, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
+    }
+    return check_launch(c, "batch hmax update");
+  });
+  if (rc) return rc;
+  b->launches += (unsigned) launch_batch_forces(q, b->gravity, b->lpg, o);
+  rc = branches(2, [&](gsph_ctx* c) -> int {
+    GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 3, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    return GSPH_OK;
+  });
+  if (rc) return rc;
+  cudaEventRecordWithFlags(b->ev[1], o, cudaEventRecordExternal);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return bfail(b, GSPH_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  return GSPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gsph_batch* gsph_batch_create(gsph_ctx* const* ctxs, int32_t nsim) {
+  if (!ctxs || nsim < 1 || nsim > 4096) { g_create_error = GSPH_ERR_INVALID; return nullptr; }
+  for (int i = 0; i < nsim; i++) {
+    const gsph_ctx* c = ctxs[i];
+    if (!c || c->device != ctxs[0]->device || c->cfg.precision != GSPH_PRECISION_MIXED ||
+        c->cfg.self_gravity != ctxs[0]->cfg.self_gravity) {
+      g_create_error = c && c->cfg.precision != GSPH_PRECISION_MIXED ? GSPH_ERR_UNSUPPORTED : GSPH_ERR_INVALID;
+      return nullptr;
+    }
+    for (int j = 0; j < i; j++)
+      if (ctxs[j] == c) { g_create_error = GSPH_ERR_INVALID; return nullptr; }
+  }
+  gsph_batch* b = new gsph_batch();
+  b->ctx.assign(ctxs, ctxs + nsim);
+  b->device = ctxs[0]->device;
+  b->gravity = ctxs[0]->cfg.self_gravity != 0;
+  cudaSetDevice(b->device);
+  bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_sims, sizeof(SimDesc) * (size_t) nsim) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_start, sizeof(int) * (size_t) (nsim + 1)) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_hstart, sizeof(int) * (size_t) (nsim + 1)) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_next, sizeof(int) * 4) == cudaSuccess;
+  for (int q = 0; q < 3 && ok; q++) ok = cudaEventCreateWithFlags(&b->fork[q], cudaEventDisableTiming) == cudaSuccess;
+  b->join.assign(3 * (size_t) nsim, nullptr);
+  for (auto& ev : b->join)
+    if (ok) ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+  for (int q = 0; q < 2 && ok; q++) ok = cudaEventCreate(&b->ev[q]) == cudaSuccess;
+  if (!ok) {
+    gsph_batch_destroy(b);
+    g_create_error = GSPH_ERR_CUDA;
+    return nullptr;
+  }
+  g_create_error = GSPH_OK;
+  return b;
+}
+
+void gsph_batch_destroy(gsph_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_drop_graph(b);
+  if (b->d_sims) cudaFree(b->d_sims);
+  if (b->d_start) cudaFree(b->d_start);
+  if (b->d_hstart) cudaFree(b->d_hstart);
+  if (b->d_next) cudaFree(b->d_next);
+  for (cudaEvent_t e : b->fork) if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->join) if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->ev) if (e) cudaEventDestroy(e);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+const char* gsph_batch_last_error(const gsph_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int32_t gsph_batch_step(gsph_batch* b) {
+  if (!b) return GSPH_ERR_INVALID;
+  cudaSetDevice(b->device);
+  for (gsph_ctx* c : b->ctx) {
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bfail(b, GSPH_ERR_CUDA, "simulation stream");
+  }
+  int rc = GSPH_OK;
+  if (batch_stale(b)) {
+    rc = batch_prepare(b);
+    if (rc) return rc;
+  }
+  std::vector<cudaStream_t> saved;
+  for (gsph_ctx* c : b->ctx) saved.push_back(c->stream);
+  if (!b->exec) {
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+      return bfail(b, GSPH_ERR_CUDA, "cudaStreamBeginCapture");
+    for (gsph_ctx* c : b->ctx) c->capturing = true;
+    rc = batch_body(b);
+    for (gsph_ctx* c : b->ctx) c->capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    for (size_t i = 0; i < b->ctx.size(); i++) b->ctx[i]->stream = saved[i];
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return bfail(b, GSPH_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    b->graph = g;
+    if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
+      batch_drop_graph(b);
+      return bfail(b, GSPH_ERR_CUDA, "cudaGraphInstantiate");
+    }
+  }
+  if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess) return bfail(b, GSPH_ERR_CUDA, "cudaGraphLaunch");
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, GSPH_ERR_CUDA, "batch step");
+  if (cudaEventElapsedTime(&b->ms, b->ev[0], b->ev[1]) != cudaSuccess) b->ms = 0.0f;
+  (void) cudaGetLastError();
+  int first = GSPH_OK;
+  for (gsph_ctx* c : b->ctx) {
+    c->have_tree = c->have_props = c->have_forces = true;
+    c->have_star_forces = false;
+    const int r = read_status(c);
+    c->last.ms_build = c->last.ms_density = c->last.ms_hmax = c->last.ms_forces = 0.0f;
+    c->last.ms_total = 0.0f;
+    if (r && !first) {
+      first = r;
+      b->err = c->err;
+    }
+  }
+  return first;
+}
+
+int32_t gsph_batch_stats(const gsph_batch* b, float* ms, int32_t* launches) {
+  if (!b) return GSPH_ERR_INVALID;
+  unsigned total = b->launches;
+  for (const gsph_ctx* c : b->ctx) total += c->launches;
+  if (ms) *ms = b->ms;
+  if (launches) *launches = (int32_t) total;
   return GSPH_OK;
 }
 

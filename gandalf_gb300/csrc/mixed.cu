@@ -18,6 +18,7 @@
 #include "gsph_walk.cuh"
 #include "kernels.cuh"
 #include "mixed_state.cuh"
+#include "batch.cuh"
 #include "stars.cuh"
 
 namespace gsph {
@@ -486,156 +487,166 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
 constexpr int kPPStack = 1024;
 constexpr int kPPList = 256;
 
+struct PPShared {
+  int stack[8][kPPStack];
+  int list[8][kPPList];
+  double h0[32];
+  double mloc[8];
+};
+
+// One heavy leaf, solved by the whole block (256 threads); interaction counts and status
+// go to cnt when the leaf is done.
 template <int LPG>
-__global__ void __launch_bounds__(256, 2)
-k_density_mixed_pp(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
-                   HeavyList heavy) {
-  __shared__ int s_stack[8][kPPStack];
-  __shared__ int s_list[8][kPPList];
-  __shared__ double s_h0[32];
-  __shared__ double s_mloc[8];
+__device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& p, const MixedParticles& mp,
+                                                const MixedCells& mc, const SphParams& prm,
+                                                const DeviceCounters& cnt, int leaf, PPShared& sm) {
   constexpr int G = 32 / LPG;   // lanes per leaf when scanning emitted leaves
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int* stack = s_stack[wib];
-  int* list = s_list[wib];
-  const int nh = *heavy.count;
+  int* stack = sm.stack[wib];
+  int* list = sm.list[wib];
   unsigned long long pairs = 0;
-  bool stack_ok = true, fail = false, unsolved = false;
-  for (int k = blockIdx.x; k < nh; k += gridDim.x) {
-    const int leaf = heavy.leaves[k];
-    const int c = t.leaf_cell[leaf];
-    const int first = t.cell_first[c], ncell = t.cell_n[c];
-    __syncthreads();
-    if (threadIdx.x < ncell) s_h0[threadIdx.x] = p.h[first + threadIdx.x];
-    __syncthreads();
-    double hk = __dmul_rn(1.05, t.geom[c].hmax);
-    bool solved = false;
-    for (int att = 0; att < kMaxAttempts && !solved; att++) {
-      double mloc = 0.0;
-      bool abort_any = false;
-      for (int g = wib; g < ncell; g += 8) {
-        const int slot = first + g;
-        const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
-        const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
-        double hi = s_h0[g], h_lower = 0.0, h_upper = hk;
-        double invh = 1.0 / hi, hrho_last = hi;
-        const double inv_m = 1.0 / mi, inv_hfac = 1.0 / prm.h_fac;
-        double rho = 0.0, om = 0.0, zeta = 0.0;
-        bool done = false, abort_cell = false;
-        int iteration = 0;
-        while (!done) {
-          iteration++;
-          const double invhsqd = invh * invh;
-          const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
-          float srho = 0.0f, som = 0.0f, sze = 0.0f;
-          // the particle's search box, rounded outwards, and its periodic images
-          const double rr = __dmul_rn(kKernRange * (1.0 + 1.0 / 1024.0), hi);
-          double gmin[3] = {xi - rr, yi - rr, zi - rr}, gmax[3] = {xi + rr, yi + rr, zi + rr};
-          int nsh[3] = {1, 1, 1}, sh[3][3];
-          for (int q = 0; q < 3; q++) {
-            sh[q][0] = 1;
-            if (prm.periodic) {
-              if (gmax[q] > prm.boxmax[q]) sh[q][nsh[q]++] = 2;
-              if (gmin[q] < prm.boxmin[q]) sh[q][nsh[q]++] = 0;
-            }
+  bool stack_ok = true, fail = false;
+  const int c = t.leaf_cell[leaf];
+  const int first = t.cell_first[c], ncell = t.cell_n[c];
+  __syncthreads();
+  if (threadIdx.x < ncell) sm.h0[threadIdx.x] = p.h[first + threadIdx.x];
+  __syncthreads();
+  double hk = __dmul_rn(1.05, t.geom[c].hmax);
+  bool solved = false;
+  for (int att = 0; att < kMaxAttempts && !solved; att++) {
+    double mloc = 0.0;
+    bool abort_any = false;
+    for (int g = wib; g < ncell; g += 8) {
+      const int slot = first + g;
+      const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
+      const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
+      double hi = sm.h0[g], h_lower = 0.0, h_upper = hk;
+      double invh = 1.0 / hi, hrho_last = hi;
+      const double inv_m = 1.0 / mi, inv_hfac = 1.0 / prm.h_fac;
+      double rho = 0.0, om = 0.0, zeta = 0.0;
+      bool done = false, abort_cell = false;
+      int iteration = 0;
+      while (!done) {
+        iteration++;
+        const double invhsqd = invh * invh;
+        const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
+        float srho = 0.0f, som = 0.0f, sze = 0.0f;
+        // the particle's search box, rounded outwards, and its periodic images
+        const double rr = __dmul_rn(kKernRange * (1.0 + 1.0 / 1024.0), hi);
+        double gmin[3] = {xi - rr, yi - rr, zi - rr}, gmax[3] = {xi + rr, yi + rr, zi + rr};
+        int nsh[3] = {1, 1, 1}, sh[3][3];
+        for (int q = 0; q < 3; q++) {
+          sh[q][0] = 1;
+          if (prm.periodic) {
+            if (gmax[q] > prm.boxmax[q]) sh[q][nsh[q]++] = 2;
+            if (gmin[q] < prm.boxmin[q]) sh[q][nsh[q]++] = 0;
           }
-          WarpLists L{list, list, list, 0, 0, 0, kPPList};
-          auto consume = [&]() {
-            for (int e0 = 0; e0 < L.na; e0 += LPG) {
-              const int e = e0 + lane / G, q = lane % G;
-              if (e >= L.na) continue;
-              const int tagv = list[e];
-              const int node = tagv & ((1 << kNodeBits) - 1);
-              const int code = tagv >> kNodeBits;
-              if (q >= t.cell_n[node]) continue;
-              const int j = t.cell_first[node] + q;
-              float dx, dy, dz, mj;
-              if (code == kNoShift) {
-                const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
-                mj = pjh.w;
-                dx = (pjh.x - pih.x) + (pjl.x - pil.x);
-                dy = (pjh.y - pih.y) + (pjl.y - pil.y);
-                dz = (pjh.z - pih.z) + (pjl.z - pil.z);
-              } else {
-                const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
-                const double xj = p.x[j], yj = p.y[j], zj = p.z[j];
-                const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
-                bool ok = true;
-                if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
-                if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
-                if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
-                if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
-                if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
-                if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
-                if (!ok) continue;
-                mj = mp.pos_hi[j].w;
-                dx = (float) (__dadd_rn(xj, sx) - xi);
-                dy = (float) (__dadd_rn(yj, sy) - yi);
-                dz = (float) (__dadd_rn(zj, sz) - zi);
-              }
-              const float ssqd = (dx * dx + dy * dy + dz * dz) * invhsqd_f;
-              if (ssqd < 4.0f) {
-                const float sv = fsqrt_pos(ssqd);
-                srho = fmaf(mj, m4f_w0(sv), srho);
-                som = fmaf(mj * invh_f, m4f_womega(sv), som);
-                sze = fmaf(mj, m4f_wzeta(sv), sze);
-                pairs++;
-              }
-            }
-            __syncwarp();
-          };
-          for (int a0 = 0; a0 < nsh[0]; a0++)
-            for (int a1 = 0; a1 < nsh[1]; a1++)
-              for (int a2 = 0; a2 < nsh[2]; a2++) {
-                const int code = sh[0][a0] + 3 * sh[1][a1] + 9 * sh[2][a2];
-                float bmin[3], bmax[3];
-                for (int q = 0; q < 3; q++) {
-                  const double sft = shift_of(code, q, prm);
-                  bmin[q] = __double2float_rd(gmin[q] - sft);
-                  bmax[q] = __double2float_ru(gmax[q] - sft);
-                }
-                auto decide = [&](int node, int level) -> int {
-                  if (t.cell_n[node] == 0) return kSkip;
-                  if (!fbox_overlap(bmin, bmax, mc.bbmin[node], mc.bbmax[node])) return kSkip;
-                  return level == t.ltot ? kEmitA : kOpen;
-                };
-                auto tag = [&](int node, int) { return node | (code << kNodeBits); };
-                stack_ok = warp_walk(0, t.ltot, t.cell_level, stack, kPPStack, L, decide, tag, consume) && stack_ok;
-                consume();
-                L.na = 0;
-              }
-          for (int o = 16; o > 0; o >>= 1) {
-            srho += __shfl_xor_sync(kFull, srho, o);
-            som += __shfl_xor_sync(kFull, som, o);
-            sze += __shfl_xor_sync(kFull, sze, o);
-          }
-          h_update(srho, som, sze, inv_m, inv_hfac, invhsqd, hk, prm, iteration, hi, invh, h_lower, h_upper,
-                   hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
-          if (!stack_ok) done = true;
         }
-        abort_any = abort_any || abort_cell;
-        if (!abort_cell && lane == 0)
-          finish_density(p, prm, slot, fmax(hrho_last, h_lower), rho, om, zeta, xi, yi, zi);
+        WarpLists L{list, list, list, 0, 0, 0, kPPList};
+        auto consume = [&]() {
+          for (int e0 = 0; e0 < L.na; e0 += LPG) {
+            const int e = e0 + lane / G, q = lane % G;
+            if (e >= L.na) continue;
+            const int tagv = list[e];
+            const int node = tagv & ((1 << kNodeBits) - 1);
+            const int code = tagv >> kNodeBits;
+            if (q >= t.cell_n[node]) continue;
+            const int j = t.cell_first[node] + q;
+            float dx, dy, dz, mj;
+            if (code == kNoShift) {
+              const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+              mj = pjh.w;
+              dx = (pjh.x - pih.x) + (pjl.x - pil.x);
+              dy = (pjh.y - pih.y) + (pjl.y - pil.y);
+              dz = (pjh.z - pih.z) + (pjl.z - pil.z);
+            } else {
+              const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+              const double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+              const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+              bool ok = true;
+              if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
+              if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
+              if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
+              if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
+              if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
+              if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
+              if (!ok) continue;
+              mj = mp.pos_hi[j].w;
+              dx = (float) (__dadd_rn(xj, sx) - xi);
+              dy = (float) (__dadd_rn(yj, sy) - yi);
+              dz = (float) (__dadd_rn(zj, sz) - zi);
+            }
+            const float ssqd = (dx * dx + dy * dy + dz * dz) * invhsqd_f;
+            if (ssqd < 4.0f) {
+              const float sv = fsqrt_pos(ssqd);
+              srho = fmaf(mj, m4f_w0(sv), srho);
+              som = fmaf(mj * invh_f, m4f_womega(sv), som);
+              sze = fmaf(mj, m4f_wzeta(sv), sze);
+              pairs++;
+            }
+          }
+          __syncwarp();
+        };
+        for (int a0 = 0; a0 < nsh[0]; a0++)
+          for (int a1 = 0; a1 < nsh[1]; a1++)
+            for (int a2 = 0; a2 < nsh[2]; a2++) {
+              const int code = sh[0][a0] + 3 * sh[1][a1] + 9 * sh[2][a2];
+              float bmin[3], bmax[3];
+              for (int q = 0; q < 3; q++) {
+                const double sft = shift_of(code, q, prm);
+                bmin[q] = __double2float_rd(gmin[q] - sft);
+                bmax[q] = __double2float_ru(gmax[q] - sft);
+              }
+              auto decide = [&](int node, int level) -> int {
+                if (t.cell_n[node] == 0) return kSkip;
+                if (!fbox_overlap(bmin, bmax, mc.bbmin[node], mc.bbmax[node])) return kSkip;
+                return level == t.ltot ? kEmitA : kOpen;
+              };
+              auto tag = [&](int node, int) { return node | (code << kNodeBits); };
+              stack_ok = warp_walk(0, t.ltot, t.cell_level, stack, kPPStack, L, decide, tag, consume) && stack_ok;
+              consume();
+              L.na = 0;
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+          srho += __shfl_xor_sync(kFull, srho, o);
+          som += __shfl_xor_sync(kFull, som, o);
+          sze += __shfl_xor_sync(kFull, sze, o);
+        }
+        h_update(srho, som, sze, inv_m, inv_hfac, invhsqd, hk, prm, iteration, hi, invh, h_lower, h_upper,
+                 hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
+        if (!stack_ok) done = true;
       }
-      if (lane == 0) s_mloc[wib] = mloc;
-      abort_any = __syncthreads_or(abort_any);
-      if (!abort_any) { solved = true; break; }
-      double mc_ = 0.0;
-      for (int w = 0; w < 8; w++) mc_ = fmax(mc_, s_mloc[w]);
-      __syncthreads();
-      int guard = 0;
-      do { hk = __dmul_rn(1.05, hk); } while (hk < mc_ && ++guard < 100000);
+      abort_any = abort_any || abort_cell;
+      if (!abort_cell && lane == 0)
+        finish_density(p, prm, slot, fmax(hrho_last, h_lower), rho, om, zeta, xi, yi, zi);
     }
-    if (!solved) unsolved = true;
+    if (lane == 0) sm.mloc[wib] = mloc;
+    abort_any = __syncthreads_or(abort_any);
+    if (!abort_any) { solved = true; break; }
+    double mc_ = 0.0;
+    for (int w = 0; w < 8; w++) mc_ = fmax(mc_, sm.mloc[w]);
+    __syncthreads();
+    int guard = 0;
+    do { hk = __dmul_rn(1.05, hk); } while (hk < mc_ && ++guard < 100000);
   }
   unsigned long long tot = pairs;
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
   if (lane == 0) {
-    atomicAdd(cnt.density_pairs, tot);
+    if (tot) atomicAdd(cnt.density_pairs, tot);
     if (!stack_ok) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
     if (fail) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
-    if (unsolved) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
+    if (!solved && wib == 0) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
   }
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(256, 2)
+k_density_mixed_pp(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
+                   HeavyList heavy) {
+  __shared__ PPShared sm;
+  const int nh = *heavy.count;
+  for (int k = blockIdx.x; k < nh; k += gridDim.x)
+    density_pp_leaf<LPG>(t, p, mp, mc, prm, cnt, heavy.leaves[k], sm);
 }
 
 constexpr int kDensWarps = 4;
@@ -1129,14 +1140,12 @@ k_all_forces_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, S
 }
 
 // ---- hydro only (periodic or open), warp per leaf ----------------------------------------
+constexpr int kHListA = 512;
+
 template <int LPG>
-__global__ void __launch_bounds__(kForceWarps * 32)
-k_hydro_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt) {
-  __shared__ int s_stack[kForceWarps][kFStack];
-  __shared__ int s_list[kForceWarps][512];
-  const int wib = threadIdx.x >> 5;
-  const int leaf = blockIdx.x * kForceWarps + wib;
-  if (leaf >= t.nleaf) return;
+__device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, const MixedParticles& mp,
+                                           const MixedCells& mc, const SphParams& prm, const DeviceCounters& cnt,
+                                           int leaf, int* stack, int* list) {
   const int lane = threadIdx.x & 31;
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
@@ -1147,7 +1156,7 @@ k_hydro_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams p
   load_target_f(p, mp, slot, T);
   AccF A = {};
   unsigned long long npairs = 0, exact = 0;
-  WarpLists L{s_list[wib], s_list[wib], s_list[wib], 0, 0, 0, 512};
+  WarpLists L{list, list, list, 0, 0, 0, kHListA};
   const float4 bmin_f = mc.bbmin[c], bmax_f = mc.bbmax[c], hmin_f = mc.hbmin[c], hmax_f = mc.hbmax[c];
   const float half[3] = {(float) prm.boxhalf[0], (float) prm.boxhalf[1], (float) prm.boxhalf[2]};
   const float size[3] = {(float) prm.boxsize[0], (float) prm.boxsize[1], (float) prm.boxsize[2]};
@@ -1209,13 +1218,157 @@ k_hydro_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams p
       }
     }
   };
-  const bool ok = warp_walk(0, t.ltot, t.cell_level, s_stack[wib], kFStack, L, decide, tag, consume);
+  const bool ok = warp_walk(0, t.ltot, t.cell_level, stack, kFStack, L, decide, tag, consume);
   consume();
   if (!ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
   unsigned long long a1 = npairs, a4 = exact;
   for (int o = 16; o > 0; o >>= 1) { a1 += __shfl_xor_sync(kFull, a1, o); a4 += __shfl_xor_sync(kFull, a4, o); }
   if (lane == 0) { atomicAdd(cnt.hydro_pairs, a1); atomicAdd(cnt.exact_checks, a4); }
   finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, 0.0, 0, 0, false);
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(kForceWarps * 32)
+k_hydro_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt) {
+  __shared__ int s_stack[kForceWarps][kFStack];
+  __shared__ int s_list[kForceWarps][kHListA];
+  const int wib = threadIdx.x >> 5;
+  const int leaf = blockIdx.x * kForceWarps + wib;
+  if (leaf >= t.nleaf) return;
+  hydro_leaf<LPG>(t, p, mp, mc, prm, cnt, leaf, s_stack[wib], s_list[wib]);
+}
+
+// ==========================================================================================
+// Batched passes over many simulations (batch.cuh).
+// ==========================================================================================
+// Largest s with start[s] <= item (start has nsim + 1 nondecreasing entries).
+__device__ __forceinline__ int find_sim(const int* start, int nsim, int item) {
+  int lo = 0, hi = nsim - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int warp_take(int* counter) {
+  int item = 0;
+  if ((threadIdx.x & 31) == 0) item = atomicAdd(counter, 1);
+  return __shfl_sync(kFull, item, 0);
+}
+
+__device__ __forceinline__ int block_take(int* counter, int* s_item) {
+  __syncthreads();
+  if (threadIdx.x == 0) *s_item = atomicAdd(counter, 1);
+  __syncthreads();
+  return *s_item;
+}
+
+__global__ void k_batch_heavy_prefix(BatchQueue q) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int acc = 0;
+  for (int s = 0; s < q.nsim; s++) {
+    q.heavy_start[s] = acc;
+    acc += *q.sims[s].heavy.count;
+  }
+  q.heavy_start[q.nsim] = acc;
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(kDensWarps * 32, 3) k_batch_density(BatchQueue q) {
+  extern __shared__ float2 s_dyn2[];
+  float2* s_compact = s_dyn2;
+  int* s_stack = reinterpret_cast<int*>(s_dyn2 + kDensWarps * kCompactPerWarp);
+  int* s_list = s_stack + kDensWarps * kDensStack;
+  const int wib = threadIdx.x >> 5;
+  const int kcap = compact_stride<LPG>();
+  const int total = q.leaf_start[q.nsim];
+  for (;;) {
+    const int item = warp_take(&q.next[0]);
+    if (item >= total) break;
+    const int s = find_sim(q.leaf_start, q.nsim, item);
+    const SimDesc& d = q.sims[s];
+    const int leaf = item - q.leaf_start[s];
+    const bool ok = density_cell<LPG, 1>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, leaf, s_stack + wib * kDensStack,
+                                         s_list + wib * kDensListNormal, kDensListNormal,
+                                         s_compact + wib * kCompactPerWarp, kcap, true, nullptr);
+    if (!ok && (threadIdx.x & 31) == 0) {
+      const int k = atomicAdd(d.heavy.count, 1);
+      d.heavy.leaves[k] = leaf;
+    }
+  }
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(256, 2) k_batch_density_pp(BatchQueue q) {
+  __shared__ PPShared sm;
+  __shared__ int s_item;
+  const int total = q.heavy_start[q.nsim];
+  for (;;) {
+    const int item = block_take(&q.next[1], &s_item);
+    if (item >= total) break;
+    const int s = find_sim(q.heavy_start, q.nsim, item);
+    const SimDesc& d = q.sims[s];
+    density_pp_leaf<LPG>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, d.heavy.leaves[item - q.heavy_start[s]], sm);
+  }
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(kForceWarps * 32) k_batch_hydro(BatchQueue q) {
+  __shared__ int s_stack[kForceWarps][kFStack];
+  __shared__ int s_list[kForceWarps][kHListA];
+  const int wib = threadIdx.x >> 5;
+  const int total = q.leaf_start[q.nsim];
+  for (;;) {
+    const int item = warp_take(&q.next[2]);
+    if (item >= total) break;
+    const int s = find_sim(q.leaf_start, q.nsim, item);
+    const SimDesc& d = q.sims[s];
+    hydro_leaf<LPG>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, item - q.leaf_start[s], s_stack[wib], s_list[wib]);
+  }
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(kForceWarps * 32) k_batch_forces(BatchQueue q) {
+  __shared__ int s_stack[kForceWarps][kFStack];
+  __shared__ int s_a[kForceWarps][kFListA];
+  __shared__ int s_b[kForceWarps][kFListB];
+  __shared__ int s_c[kForceWarps][kFListC];
+  const int wib = threadIdx.x >> 5;
+  const int total = q.leaf_start[q.nsim];
+  for (;;) {
+    const int item = warp_take(&q.next[2]);
+    if (item >= total) break;
+    const int s = find_sim(q.leaf_start, q.nsim, item);
+    const SimDesc& d = q.sims[s];
+    const int leaf = item - q.leaf_start[s];
+    const bool ok = all_forces_leaf<LPG, 1>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, leaf, 0, s_stack[wib], s_a[wib],
+                                            s_b[wib], s_c[wib], kFListA, kFListB, kFListC, true);
+    if (!ok && (threadIdx.x & 31) == 0) {
+      const int k = atomicAdd(d.heavy.count, 1);
+      d.heavy.leaves[k] = leaf;
+    }
+  }
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(256) k_batch_forces_wide(BatchQueue q) {
+  extern __shared__ int s_dyn[];
+  __shared__ int s_item;
+  const int wib = threadIdx.x >> 5;
+  const int per = kFStack + kWListA + kWListB + kWListC;
+  int* base = s_dyn + wib * per;
+  ForceSmem* fs = reinterpret_cast<ForceSmem*>(s_dyn + 8 * per);
+  const int total = q.heavy_start[q.nsim];
+  for (;;) {
+    const int item = block_take(&q.next[3], &s_item);
+    if (item >= total) break;
+    const int s = find_sim(q.heavy_start, q.nsim, item);
+    const SimDesc& d = q.sims[s];
+    all_forces_leaf<LPG, 8>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, d.heavy.leaves[item - q.heavy_start[s]], 0, base,
+                            base + kFStack, base + kFStack + kWListA, base + kFStack + kWListA + kWListB, kWListA,
+                            kWListB, kWListC, false, wib, fs);
+  }
 }
 
 int grid1(int n) { return n < 1 ? 1 : (n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8; }
@@ -1281,5 +1434,33 @@ int launch_hydro_mixed(const Tree& t, const Particles& p, const MixedParticles& 
   GSPH_MIXED_LPG(k_hydro_mixed, lanes_per_particle, blocks, kForceWarps * 32, 0, t, p, mp, mc, prm, cnt)
   return 1;
 }
+
+int launch_batch_density(const BatchQueue& q, int lpg, cudaStream_t st) {
+  cudaMemsetAsync(q.next, 0, 4 * sizeof(int), st);
+  const size_t smem_n = dens_smem_normal();
+  for (auto f : {k_batch_density<1>, k_batch_density<2>, k_batch_density<4>, k_batch_density<8>,
+                 k_batch_density<16>, k_batch_density<32>})
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_n);
+  GSPH_MIXED_LPG(k_batch_density, lpg, 152 * 3, kDensWarps * 32, smem_n, q)
+  k_batch_heavy_prefix<<<1, 32, 0, st>>>(q);
+  GSPH_MIXED_LPG(k_batch_density_pp, lpg, 152 * 2, 256, 0, q)
+  return 3;
+}
+
+int launch_batch_forces(const BatchQueue& q, bool gravity, int lpg, cudaStream_t st) {
+  if (!gravity) {
+    GSPH_MIXED_LPG(k_batch_hydro, lpg, 152 * 4, kForceWarps * 32, 0, q)
+    return 1;
+  }
+  GSPH_MIXED_LPG(k_batch_forces, lpg, 152 * 4, kForceWarps * 32, 0, q)
+  k_batch_heavy_prefix<<<1, 32, 0, st>>>(q);
+  const size_t smem = sizeof(int) * 8 * (kFStack + kWListA + kWListB + kWListC) + sizeof(ForceSmem);
+  for (auto f : {k_batch_forces_wide<1>, k_batch_forces_wide<2>, k_batch_forces_wide<4>,
+                 k_batch_forces_wide<8>, k_batch_forces_wide<16>, k_batch_forces_wide<32>})
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  GSPH_MIXED_LPG(k_batch_forces_wide, lpg, 152 * 2, 256, smem, q)
+  return 3;
+}
+
 
 }  // namespace gsph

@@ -77,6 +77,45 @@ def plummer_sphere(n: int = 262144, seed: int = 4321, rtrunc: float = 10.0) -> d
     return ics
 
 
+def kh_box(n: int = 32768, seed: int = 7, pressure: float = 2.5) -> dict:
+    """Periodic 3-D Kelvin-Helmholtz box [0,1) x [0,1) x [0,0.25) (hydro only).
+
+    Equal-mass particles, density 2 in the band |y - 0.5| < 0.25 and 1 outside (2:1 in
+    number density, uniform random positions in each region); shear vx = -0.5 inside and
+    +0.5 outside the band; vy = 0.01 sin(4 pi x); uniform pressure P (u = P / ((gamma-1)
+    rho)); gamma = 5/3.
+    """
+    rng = np.random.default_rng(seed)
+    gamma = 5.0 / 3.0
+    nd = int(round(2.0 * n / 3.0))
+    nl = n - nd
+    xd = np.stack([rng.random(nd), 0.25 + 0.5 * rng.random(nd), 0.25 * rng.random(nd)], 1)
+    yl = 0.5 * rng.random(nl)
+    yl = np.where(yl < 0.25, yl, yl + 0.5)
+    xl = np.stack([rng.random(nl), yl, 0.25 * rng.random(nl)], 1)
+    x = np.concatenate([xd, xl])
+    dense = np.concatenate([np.ones(nd, bool), np.zeros(nl, bool)])
+    rho = np.where(dense, 2.0, 1.0)
+    v = np.zeros((n, 3))
+    v[:, 0] = np.where(dense, -0.5, 0.5)
+    v[:, 1] = 0.01 * np.sin(4.0 * math.pi * x[:, 0])
+    mtot = 2.0 * 0.5 * 0.25 + 1.0 * 0.5 * 0.25
+    m = np.full(n, mtot / n)
+    u = pressure / ((gamma - 1.0) * rho)
+    h = H_FAC * (m / rho) ** (1.0 / 3.0)
+    ics = _pack(x, v, m, u, h)
+    ics["params"] = dict(self_gravity=0, eos=0, periodic=1, boxmin=(0.0, 0.0, 0.0),
+                         boxmax=(1.0, 1.0, 0.25), gamma_eos=gamma, thetamaxsqd=0.25)
+    return ics
+
+
+def kh_ensemble(nbox: int = 64, nmin: int = 4096, nmax: int = 131072, seed: int = 2024) -> list:
+    """``nbox`` independent KH boxes with particle counts log-uniform in [nmin, nmax]."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(nmin), math.log(nmax), nbox)).astype(int)
+    return [kh_box(int(nb), seed=seed + 1 + i) for i, nb in enumerate(sizes)]
+
+
 def with_stars(ics: dict, nstar: int = 64, rmax: float = 0.5, mass: float = 1.0e-3, h: float = 0.01,
                sigma_v: float = 0.0, seed: int = 99) -> dict:
     """Add ``nstar`` star particles, uniform in the sphere r < rmax, to a particle set.
@@ -105,4 +144,5 @@ def _unit_vectors(rng, n):
 WORKLOADS = {
     "periodic_cube": periodic_cube,
     "plummer_sphere": plummer_sphere,
+    "kh_box": kh_box,
 }

@@ -262,3 +262,37 @@ def list_hash(ids) -> np.uint64:
         return np.uint64(0)
     with np.errstate(over="ignore"):
         return np.sum(mix64(ids), dtype=np.uint64)
+
+
+class GradhSphBatch:
+    """Many independent simulations (mixed-precision GradhSphTree objects) stepped together:
+    one persistent launch per pass over all their leaf cells, replayed from one CUDA graph."""
+
+    def __init__(self, trees: list):
+        self._lib = _native.load()
+        self.trees = list(trees)
+        arr = (ctypes.c_void_p * len(self.trees))(*[t._ctx for t in self.trees])
+        self._b = self._lib.gsph_batch_create(arr, len(self.trees))
+        if not self._b:
+            code = self._lib.gsph_create_error()
+            raise GandalfError(f"gsph_batch_create failed: {_native.ERRORS.get(code, code)}")
+
+    def step(self):
+        rc = self._lib.gsph_batch_step(self._b)
+        if rc != _native.GSPH_OK:
+            msg = self._lib.gsph_batch_last_error(self._b)
+            raise GandalfError(f"batch step: {_native.ERRORS.get(rc, rc)}: {msg.decode() if msg else ''}")
+
+    def stats(self) -> dict:
+        ms = ctypes.c_float()
+        nl = ctypes.c_int32()
+        self._lib.gsph_batch_stats(self._b, ctypes.byref(ms), ctypes.byref(nl))
+        return {"ms": ms.value, "launches": nl.value}
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._lib.gsph_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        self.close()

@@ -170,6 +170,23 @@ int32_t gsph_step(gsph_ctx* ctx);
  * to gsph_step's. */
 int32_t gsph_step_graph(gsph_ctx* ctx);
 
+/* ---- batches of independent simulations ------------------------------------------------
+ * No counterpart in the reference (which steps one simulation per process).  A batch
+ * steps many mixed-precision contexts at once: each of the density and force passes is one
+ * persistent launch whose warps pull leaf cells of all simulations from a device work
+ * queue, and the per-simulation tree builds and cell updates run as parallel branches of
+ * one CUDA graph.  Results per context are identical to gsph_step on that context; read
+ * them with the per-context calls.  All contexts must be mixed precision on one device,
+ * share the self_gravity setting and have no stars; a context may belong to one batch at a
+ * time and must not be stepped on its own while the batch step runs. */
+typedef struct gsph_batch gsph_batch;
+gsph_batch* gsph_batch_create(gsph_ctx* const* ctxs, int32_t nsim);   /* NULL: see gsph_create_error */
+void gsph_batch_destroy(gsph_batch* batch);
+int32_t gsph_batch_step(gsph_batch* batch);
+const char* gsph_batch_last_error(const gsph_batch* batch);
+/* Device time of the last batch step (ms) and the kernels one batch step launches. */
+int32_t gsph_batch_stats(const gsph_batch* batch, float* ms, int32_t* launches);
+
 /* ---- results ----------------------------------------------------------------------------- */
 /* One field for all particles in input order into host memory (n doubles). */
 int32_t gsph_get_field(gsph_ctx* ctx, int32_t field, double* out);
