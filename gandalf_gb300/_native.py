@@ -21,6 +21,21 @@ FIELDS = ["h", "rho", "invomega", "zeta", "hfactor", "pressure", "sound", "u", "
 FIELD_ID = {k: i for i, k in enumerate(FIELDS)}
 
 
+class KdkConfig(ctypes.Structure):
+    _fields_ = [("nlevels", ctypes.c_int32), ("level_diff_max", ctypes.c_int32), ("courant_mult", ctypes.c_double),
+                ("accel_mult", ctypes.c_double), ("energy_mult", ctypes.c_double)]
+
+
+class KdkStatus(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("nresync", ctypes.c_int64), ("level_max", ctypes.c_int64),
+                ("level_step", ctypes.c_int64), ("nsteps", ctypes.c_int64), ("t", ctypes.c_double),
+                ("timestep", ctypes.c_double), ("dt_max", ctypes.c_double), ("active_updates", ctypes.c_int64),
+                ("status", ctypes.c_uint32)]
+
+
+KDK_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "u", "dt", "tlast", "level", "nstep", "nlast", "levelneib"]
+
+
 class Config(ctypes.Structure):
     _fields_ = [("ndim", ctypes.c_int32), ("nleafmax", ctypes.c_int32),
                 ("hydro_forces", ctypes.c_int32), ("self_gravity", ctypes.c_int32),
@@ -89,6 +104,11 @@ SIGNATURES = {
     "gsph_set_stars": (_I32, [_P, _I64] + [_D] * 8),
     "gsph_update_all_star_gas_forces": (_I32, [_P]),
     "gsph_get_star_forces": (_I32, [_P] + [_D] * 7),
+    "gsph_kdk_config_defaults": (None, [ctypes.POINTER(KdkConfig)]),
+    "gsph_kdk_setup": (_I32, [_P, ctypes.POINTER(KdkConfig)]),
+    "gsph_kdk_steps": (_I32, [_P, _I32, _I32]),
+    "gsph_kdk_get_status": (_I32, [_P, ctypes.POINTER(KdkStatus)]),
+    "gsph_kdk_get_state": (_I32, [_P, _I32, _D]),
     "gsph_batch_create": (_P, [ctypes.POINTER(_P), _I32]),
     "gsph_batch_destroy": (None, [_P]),
     "gsph_batch_step": (_I32, [_P]),

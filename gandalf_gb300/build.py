@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libgsph_gb300.so")
-SOURCES = ["tree.cu", "density.cu", "forces.cu", "mixed.cu", "stars.cu", "peak.cu", "api.cu"]
+SOURCES = ["tree.cu", "density.cu", "forces.cu", "mixed.cu", "stars.cu", "integrate.cu", "peak.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -19,6 +19,7 @@
 #include "gsph_state.cuh"
 #include "kernels.cuh"
 #include "batch.cuh"
+#include "integrate.cuh"
 #include "mixed_state.cuh"
 #include "stars.cuh"
 #include "tree.cuh"
@@ -93,6 +94,20 @@ struct gsph_ctx {
   int nstar = 0, star_cap = 0;
   double* star_buf = nullptr;
   bool have_star_forces = false;
+  // KDK integration with block timesteps (gsph_kdk_*)
+  bool kdk = false;
+  KdkParams kp{};
+  KdkGlobal* kg = nullptr;
+  double* kdk_buf = nullptr;          // r0 v0 a0 (9), u0 dudt0 dt dt_next tlast (5), keep (17): x cap
+  int* kdk_ibuf = nullptr;            // nlast nstep level levelneib: x cap
+  unsigned char* kdk_flags = nullptr;
+  unsigned char* leaf_active = nullptr;
+  int *leaf_level = nullptr, *leaf_lvn = nullptr;
+  int kdk_cap = 0;
+  cudaGraph_t kdk_graph = nullptr;
+  cudaGraphExec_t kdk_exec = nullptr;
+  int kdk_graph_steps = 0;
+  unsigned kdk_graph_launches = 0;
   // CUDA graph of the whole step (gsph_step_graph), valid for one capture key
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -133,6 +148,8 @@ void free_all(gsph_ctx* c) {
   c->cap = 0;
   c->cap_ncell = 0;
 }
+
+void kdk_free(gsph_ctx* c);
 
 void drop_graph(gsph_ctx* c) {
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
@@ -252,6 +269,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
     c->rec_sph_cnt = nullptr;
   }
   if (fresh || n != c->n || ltot != c->ltot) drop_graph(c);
+  if (fresh || n != c->n) c->kdk = false;   // a new particle set restarts any integration
   if (fresh || n != c->n || ltot != c->ltot || !c->have_particles) {
     Shape s;
     make_shape(n, ltot, s);
@@ -322,6 +340,7 @@ Particles make_particles(gsph_ctx* c) {
   p.hrangesqd = f[kFHrangesqd]; p.pressure = f[kFPressure]; p.sound = f[kFSound];
   p.ax = f[kFAX]; p.ay = f[kFAY]; p.az = f[kFAZ]; p.agx = f[kFAGX]; p.agy = f[kFAGY]; p.agz = f[kFAGZ];
   p.gpot = f[kFGpot]; p.dudt = f[kFDudt]; p.div_v = f[kFDivV]; p.gpot_hydro = f[kFGpotHydro];
+  if (c->kdk) { p.active = c->leaf_active; p.level = c->leaf_level; p.lvn = c->leaf_lvn; }
   return p;
 }
 
@@ -535,6 +554,10 @@ int do_props(gsph_ctx* c) {
   mark(c, 2);
   launch_update_hmax(t, p, c->stream);
   c->launches += 1;
+  if (c->kdk) {   // every particle's thermal properties before the force pass
+    launch_kdk_thermal(p, make_params(c), c->stream);
+    c->launches += 1;
+  }
   if (mixed(c)) {
     launch_mixed_prep_hydro(t, p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
     c->launches += 2;
@@ -668,6 +691,7 @@ void gsph_destroy(gsph_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   drop_graph(c);
+  kdk_free(c);
   free_all(c);
   if (c->aos) cudaFree(c->aos);
   if (c->star_buf) cudaFree(c->star_buf);
@@ -1343,6 +1367,287 @@ int32_t gsph_batch_stats(const gsph_batch* b, float* ms, int32_t* launches) {
   for (const gsph_ctx* c : b->ctx) total += c->launches;
   if (ms) *ms = b->ms;
   if (launches) *launches = (int32_t) total;
+  return GSPH_OK;
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// KDK leapfrog with block timesteps (gsph_kdk_*): SphSimulation::PostInitialConditionsSetup
+// and MainLoop (src/Hydrodynamics/SphSimulation.cpp:203-565, :573-880) for the gas, on the
+// device.
+// ======================================================================================
+namespace {
+
+// keep[] order of integrate.cuh: the leaf-order fields they mirror
+const int kKeepField[kKeep] = {kFRho, kFInvOmega, kFZeta, kFHfactor, kFHrangesqd, kFPressure, kFSound,
+                               kFAX, kFAY, kFAZ, kFAGX, kFAGY, kFAGZ, kFGpot, kFDudt, kFDivV, kFGpotHydro};
+
+void kdk_free(gsph_ctx* c) {
+  if (c->kdk_exec) cudaGraphExecDestroy(c->kdk_exec);
+  if (c->kdk_graph) cudaGraphDestroy(c->kdk_graph);
+  c->kdk_exec = nullptr;
+  c->kdk_graph = nullptr;
+  c->kdk_graph_steps = 0;
+  for (void* q : {(void*) c->kg, (void*) c->kdk_buf, (void*) c->kdk_ibuf, (void*) c->kdk_flags,
+                  (void*) c->leaf_active, (void*) c->leaf_level, (void*) c->leaf_lvn})
+    if (q) cudaFree(q);
+  c->kg = nullptr; c->kdk_buf = nullptr; c->kdk_ibuf = nullptr; c->kdk_flags = nullptr;
+  c->leaf_active = nullptr; c->leaf_level = nullptr; c->leaf_lvn = nullptr;
+  c->kdk_cap = 0;
+  c->kdk = false;
+}
+
+KdkState make_kdk_state(gsph_ctx* c) {
+  KdkState s{};
+  const size_t k = (size_t) c->kdk_cap;
+  s.n = c->n;
+  s.x = c->in[0]; s.y = c->in[1]; s.z = c->in[2]; s.vx = c->in[3]; s.vy = c->in[4]; s.vz = c->in[5];
+  s.u = c->in[7]; s.h = c->in[8];
+  double* b = c->kdk_buf;
+  for (int q = 0; q < 3; q++) { s.r0[q] = b + q * k; s.v0[q] = b + (3 + q) * k; s.a0[q] = b + (6 + q) * k; }
+  s.u0 = b + 9 * k; s.dudt0 = b + 10 * k; s.dt = b + 11 * k; s.dt_next = b + 12 * k; s.tlast = b + 13 * k;
+  for (int q = 0; q < kKeep; q++) s.keep[q] = b + (14 + q) * k;
+  int* ib = c->kdk_ibuf;
+  s.nlast = ib; s.nstep = ib + k; s.level = ib + 2 * k; s.levelneib = ib + 3 * k;
+  s.flags = c->kdk_flags;
+  return s;
+}
+
+KdkLeaf make_kdk_leaf(gsph_ctx* c) {
+  KdkLeaf l{};
+  l.n = c->n;
+  l.id = c->id;
+  for (int q = 0; q < kKeep; q++) l.f[q] = c->f[kKeepField[q]];
+  l.h = c->f[kFH];
+  l.u = c->f[kFU];
+  l.active = c->leaf_active;
+  l.level = c->leaf_level;
+  l.lvn = c->leaf_lvn;
+  return l;
+}
+
+// One h solve + force pass over the active particles of the current tree.
+int kdk_pass(gsph_ctx* c, bool forces) {
+  const KdkState s = make_kdk_state(c);
+  const KdkLeaf l = make_kdk_leaf(c);
+  launch_kdk_gather(s, l, c->kg, c->stream);
+  c->launches += 1;
+  int rc = do_props(c);
+  if (rc) return rc;
+  if (forces) {
+    rc = do_forces(c, c->cfg.self_gravity != 0);
+    if (rc) return rc;
+  }
+  launch_kdk_scatter(s, l, c->stream);
+  c->launches += 1;
+  return check_launch(c, "kdk pass");
+}
+
+constexpr int kKdkPasses = 3;   // the first force pass and up to two CheckTimesteps repeats
+
+int kdk_step_body(gsph_ctx* c) {
+  const KdkState s = make_kdk_state(c);
+  launch_kdk_begin(c->kg, c->stream);
+  launch_kdk_advance(s, c->kp, c->kg, c->stream);
+  c->launches += 2;
+  int rc = do_build(c);
+  if (rc) return rc;
+  for (int pass = 0; pass < kKdkPasses; pass++) {
+    rc = kdk_pass(c, true);
+    if (rc) return rc;
+    launch_kdk_check(s, c->kp, c->kg, pass == kKdkPasses - 1, c->stream);
+    c->launches += pass == kKdkPasses - 1 ? 3 : 2;
+  }
+  launch_kdk_timesteps(s, c->kp, c->kg, c->stream);
+  launch_kdk_end(s, c->kp, c->kg, c->stream);
+  c->launches += 5;
+  return check_launch(c, "kdk step");
+}
+
+int kdk_read(gsph_ctx* c) {
+  int rc = read_status(c);
+  KdkGlobal g{};
+  GSPH_CUDA(cudaMemcpy(&g, c->kg, sizeof(g), cudaMemcpyDeviceToHost));
+  if (!rc && (g.status & kKdkTimestepInvalid)) rc = fail(c, GSPH_ERR_INVALID, "Hydro timestep too large or non-positive");
+  if (!rc && (g.status & kKdkNotSettled))
+    rc = fail(c, GSPH_ERR_CAPACITY, "neighbour timestep checks still activating particles after the last pass");
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gsph_kdk_config_defaults(gsph_kdk_config* k) {
+  if (!k) return;
+  std::memset(k, 0, sizeof(*k));
+  k->nlevels = 1;            // Parameters.cpp:244-245, :239-240, :263
+  k->level_diff_max = 1;
+  k->courant_mult = 0.15;
+  k->accel_mult = 0.3;
+  k->energy_mult = 0.4;
+}
+
+int32_t gsph_kdk_setup(gsph_ctx* c, const gsph_kdk_config* k) {
+  if (!c || !k) return GSPH_ERR_INVALID;
+  if (!c->have_particles) return fail(c, GSPH_ERR_STATE, "no particles imported");
+  if (k->nlevels < 1 || k->nlevels > 20 || k->level_diff_max < 1 || !(k->courant_mult > 0) ||
+      !(k->accel_mult > 0) || !(k->energy_mult > 0))
+    return fail(c, GSPH_ERR_INVALID, "bad KDK parameters");
+  if (c->nstar) return fail(c, GSPH_ERR_UNSUPPORTED, "star particles need the N-body integrator (not implemented)");
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->kdk_cap < c->cap) {
+    kdk_free(c);
+    const size_t k2 = (size_t) c->cap;
+    GSPH_CUDA(cudaMalloc(&c->kg, sizeof(KdkGlobal)));
+    GSPH_CUDA(cudaMalloc(&c->kdk_buf, sizeof(double) * (14 + kKeep) * k2));
+    GSPH_CUDA(cudaMalloc(&c->kdk_ibuf, sizeof(int) * 4 * k2));
+    GSPH_CUDA(cudaMalloc(&c->kdk_flags, k2));
+    GSPH_CUDA(cudaMalloc(&c->leaf_active, k2));
+    GSPH_CUDA(cudaMalloc(&c->leaf_level, sizeof(int) * k2));
+    GSPH_CUDA(cudaMalloc(&c->leaf_lvn, sizeof(int) * k2));
+    c->kdk_cap = c->cap;
+  }
+  if (c->kdk_exec) cudaGraphExecDestroy(c->kdk_exec);
+  if (c->kdk_graph) cudaGraphDestroy(c->kdk_graph);
+  c->kdk_exec = nullptr;
+  c->kdk_graph = nullptr;
+  c->kdk_graph_steps = 0;
+  drop_graph(c);   // the single-step graph was captured without the active flags
+  KdkParams& kp = c->kp;
+  kp = KdkParams{};
+  kp.nlevels = k->nlevels;
+  kp.level_diff_max = k->level_diff_max;
+  kp.energy_integration = c->cfg.eos == GSPH_EOS_ENERGY_EQN;
+  kp.periodic = c->cfg.periodic;
+  kp.courant_mult = k->courant_mult;
+  kp.accel_mult = k->accel_mult;
+  kp.energy_mult = k->energy_mult;
+  for (int q = 0; q < 3; q++) {
+    kp.boxmin[q] = c->cfg.boxmin[q];
+    kp.boxmax[q] = c->cfg.boxmax[q];
+    kp.boxsize[q] = c->cfg.boxmax[q] - c->cfg.boxmin[q];
+  }
+  c->kdk = true;
+  const KdkState s = make_kdk_state(c);
+  int rc = begin_counters(c);
+  if (rc) return rc;
+  launch_kdk_setup_state(s, c->kg, c->stream);
+  // h solve on the initial tree, then a new tree with the solved h, a second h solve and
+  // the force pass (SphSimulation.cpp:305-466 with initial h provided)
+  rc = do_build(c);
+  if (!rc) rc = kdk_pass(c, false);
+  if (!rc) rc = do_build(c);
+  if (!rc) rc = kdk_pass(c, true);
+  if (rc) { c->kdk = false; return rc; }
+  launch_kdk_setup_finish(s, c->stream);
+  launch_kdk_timesteps(s, c->kp, c->kg, c->stream);
+  launch_kdk_end(s, c->kp, c->kg, c->stream);
+  rc = check_launch(c, "kdk setup");
+  if (rc) { c->kdk = false; return rc; }
+  rc = kdk_read(c);
+  if (rc) c->kdk = false;
+  return rc;
+}
+
+int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->kdk) return fail(c, GSPH_ERR_STATE, "gsph_kdk_setup has not been run for these particles");
+  if (nsteps < 1 || nsteps > 100000) return fail(c, GSPH_ERR_INVALID, "nsteps out of range");
+  cudaSetDevice(c->device);
+  int rc = begin_counters(c);
+  if (rc) return rc;
+  mark(c, 0);
+  if (!use_graph) {
+    for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c);
+    if (rc) return rc;
+  } else {
+    if (!c->kdk_exec || c->kdk_graph_steps != nsteps) {
+      if (c->kdk_exec) cudaGraphExecDestroy(c->kdk_exec);
+      if (c->kdk_graph) cudaGraphDestroy(c->kdk_graph);
+      c->kdk_exec = nullptr;
+      c->kdk_graph = nullptr;
+      GSPH_CUDA(cudaStreamSynchronize(c->stream));
+      cudaStream_t saved = c->stream;
+      c->stream = c->own_stream;
+      const unsigned before = c->launches;
+      GSPH_CUDA(cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeRelaxed));
+      c->capturing = true;
+      for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c);
+      c->capturing = false;
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(c->own_stream, &g);
+      c->stream = saved;
+      if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+      if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+      c->kdk_graph = g;
+      GSPH_CUDA(cudaGraphInstantiate(&c->kdk_exec, c->kdk_graph, 0));
+      c->kdk_graph_steps = nsteps;
+      c->kdk_graph_launches = c->launches - before;
+    }
+    // the counters were zeroed by begin_counters outside the graph
+    GSPH_CUDA(cudaGraphLaunch(c->kdk_exec, c->stream));
+    c->launches += c->kdk_graph_launches;
+  }
+  mark(c, 4);
+  rc = kdk_read(c);
+  float ms = 0.0f;
+  if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]) != cudaSuccess) ms = 0.0f;
+  (void) cudaGetLastError();
+  c->last.ms_build = c->last.ms_density = c->last.ms_hmax = c->last.ms_forces = 0.0f;
+  c->last.ms_total = ms;
+  c->have_tree = c->have_props = c->have_forces = true;
+  return rc;
+}
+
+int32_t gsph_kdk_get_status(gsph_ctx* c, gsph_kdk_status* out) {
+  if (!c || !out) return GSPH_ERR_INVALID;
+  if (!c->kdk) return fail(c, GSPH_ERR_STATE, "no KDK integration in this context");
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  KdkGlobal g{};
+  GSPH_CUDA(cudaMemcpy(&g, c->kg, sizeof(g), cudaMemcpyDeviceToHost));
+  out->n = g.n; out->nresync = g.nresync; out->level_max = g.level_max; out->level_step = g.level_step;
+  out->nsteps = g.Nsteps; out->t = g.t; out->timestep = g.timestep; out->dt_max = g.dt_max;
+  out->active_updates = (int64_t) g.active_updates;
+  out->status = g.status;
+  return GSPH_OK;
+}
+
+int32_t gsph_kdk_get_state(gsph_ctx* c, int32_t which, double* out) {
+  if (!c || !out) return GSPH_ERR_INVALID;
+  if (!c->kdk) return fail(c, GSPH_ERR_STATE, "no KDK integration in this context");
+  if (which < 0 || which >= GSPH_KDK_COUNT) return fail(c, GSPH_ERR_INVALID, "unknown KDK state field");
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  const KdkState s = make_kdk_state(c);
+  const size_t n = (size_t) c->n;
+  const double* src = nullptr;
+  const int* isrc = nullptr;
+  switch (which) {
+    case GSPH_KDK_X: src = s.x; break;
+    case GSPH_KDK_Y: src = s.y; break;
+    case GSPH_KDK_Z: src = s.z; break;
+    case GSPH_KDK_VX: src = s.vx; break;
+    case GSPH_KDK_VY: src = s.vy; break;
+    case GSPH_KDK_VZ: src = s.vz; break;
+    case GSPH_KDK_U: src = s.u; break;
+    case GSPH_KDK_DT: src = s.dt; break;
+    case GSPH_KDK_TLAST: src = s.tlast; break;
+    case GSPH_KDK_LEVEL: isrc = s.level; break;
+    case GSPH_KDK_NSTEP: isrc = s.nstep; break;
+    case GSPH_KDK_NLAST: isrc = s.nlast; break;
+    default: isrc = s.levelneib; break;
+  }
+  if (src) {
+    GSPH_CUDA(cudaMemcpy(out, src, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<int> v(n);
+    GSPH_CUDA(cudaMemcpy(v.data(), isrc, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) out[i] = (double) v[i];
+  }
   return GSPH_OK;
 }
 

@@ -54,8 +54,9 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
   const int first = t.cell_first[c], ncell = t.cell_n[c];
-  const bool mine = g < ncell;
-  const int slot = first + (mine ? g : 0);
+  const bool mine = g < ncell && is_active(p, first + g);
+  if (!__any_sync(kFull, mine)) return;   // no active particle in this leaf
+  const int slot = first + (g < ncell ? g : 0);
   const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
   const double h_start = p.h[slot];
   const CellBox bb = t.bb[c];

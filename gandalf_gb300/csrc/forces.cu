@@ -199,8 +199,10 @@ k_hydro_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
   const int first = t.cell_first[c], ncell = t.cell_n[c];
-  const bool mine = g < ncell;
-  const int slot = first + (mine ? g : 0);
+  const bool mine = g < ncell && is_active(p, first + g);
+  if (!__any_sync(kFull, mine)) return;   // no active particle in this leaf
+  const int slot = first + (g < ncell ? g : 0);
+  int lvn_own = 0;
   Target T;
   load_target(p, slot, T);
   const CellGeom G = t.geom[c];
@@ -224,14 +226,15 @@ k_hydro_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
       for (int q = sl; q < nn; q += LPG) {
         const int j = f + q;
         double r[3] = {p.x[j], p.y[j], p.z[j]};
+        int sh[3] = {0, 0, 0};   // image of j, in box lengths
         if (prm.periodic) {
           // GhostNeighbourFinder::_MakePeriodicGhost: image nearest the leaf centre
           double d[3];
           bool any = false;
           for (int k = 0; k < 3; k++) {
             d[k] = __dsub_rn(r[k], G.rcell[k]);
-            if (d[k] > prm.boxhalf[k]) { d[k] = __dsub_rn(d[k], prm.boxsize[k]); any = true; }
-            else if (d[k] < -prm.boxhalf[k]) { d[k] = __dadd_rn(d[k], prm.boxsize[k]); any = true; }
+            if (d[k] > prm.boxhalf[k]) { d[k] = __dsub_rn(d[k], prm.boxsize[k]); any = true; sh[k] = -1; }
+            else if (d[k] < -prm.boxhalf[k]) { d[k] = __dadd_rn(d[k], prm.boxsize[k]); any = true; sh[k] = 1; }
           }
           if (any) for (int k = 0; k < 3; k++) r[k] = __dadd_rn(G.rcell[k], d[k]);
         }
@@ -240,13 +243,15 @@ k_hydro_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
           // GhostNeighbourFinder::ApplyPeriodicDistanceCorrection relative to the particle
           double* dd[3] = {&dx, &dy, &dz};
           for (int k = 0; k < 3; k++) {
-            if (*dd[k] > prm.boxhalf[k]) *dd[k] = __dsub_rn(*dd[k], prm.boxsize[k]);
-            else if (*dd[k] < -prm.boxhalf[k]) *dd[k] = __dadd_rn(*dd[k], prm.boxsize[k]);
+            if (*dd[k] > prm.boxhalf[k]) { *dd[k] = __dsub_rn(*dd[k], prm.boxsize[k]); sh[k]--; }
+            else if (*dd[k] < -prm.boxhalf[k]) { *dd[k] = __dadd_rn(*dd[k], prm.boxsize[k]); sh[k]++; }
           }
+          if ((sh[0] | sh[1] | sh[2]) && !ghost_exists(prm, p, j, sh)) continue;
         }
         const double drsqd = dot3_rn(dx, dy, dz);
         if (drsqd >= T.hrangesqd && drsqd >= p.hrangesqd[j]) continue;
         hydro_pair(prm, p, T, j, dx, dy, dz, drsqd, A);
+        lvn_pair(p, slot, j, lvn_own);
         npairs++;
         if (cnt.record) {
           const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
@@ -261,6 +266,7 @@ k_hydro_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
   reduce_acc<LPG>(A);
   const unsigned long long tot = warp_total(npairs);
   if (lane == 0) atomicAdd(cnt.hydro_pairs, tot);
+  lvn_finish(p, slot, mine, lvn_own);
   if (mine && sl == 0) finish_particle(prm, p, slot, T, A, false);
 }
 
@@ -279,8 +285,10 @@ k_all_forces_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
   const int first = t.cell_first[c], ncell = t.cell_n[c];
-  const bool mine = g < ncell;
-  const int slot = first + (mine ? g : 0);
+  const bool mine = g < ncell && is_active(p, first + g);
+  if (!__any_sync(kFull, mine)) return;   // no active particle in this leaf
+  const int slot = first + (g < ncell ? g : 0);
+  int lvn_own = 0;
   Target T;
   load_target(p, slot, T);
   const CellGeom G = t.geom[c];
@@ -325,6 +333,7 @@ k_all_forces_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
           if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
         } else {
           hydro_grav_pair(prm, p, T, j, dx, dy, dz, drsqd, A);
+          lvn_pair(p, slot, j, lvn_own);
           nsph++;
           if (cnt.record) {
             const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
@@ -371,6 +380,7 @@ k_all_forces_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
     const unsigned long long cc = warp_total(ccount), ch = warp_total(chash);
     if (lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
   }
+  lvn_finish(p, slot, mine, lvn_own);
   if (mine && sl == 0) finish_particle(prm, p, slot, T, A, true);
 }
 

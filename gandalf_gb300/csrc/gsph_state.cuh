@@ -31,7 +31,39 @@ struct Particles {
   double *rho, *invomega, *zeta, *hfactor, *hrangesqd, *pressure, *sound;
   double *ax, *ay, *az, *agx, *agy, *agz, *gpot, *dudt, *div_v;
   double* gpot_hydro;         // gpot before the star terms (written only with stars)
+  // block timesteps (nullptr when every particle is active and levels are not tracked)
+  const unsigned char* active;   // per slot: 1 = the h solve and forces are computed
+  const int* level;              // per slot: timestep level
+  int* lvn;                      // per slot: max level of its SPH neighbours (atomicMax)
 };
+
+__device__ __forceinline__ bool is_active(const Particles& p, int slot) { return !p.active || p.active[slot]; }
+
+// Whether the periodic image of particle j shifted by (sx, sy, sz) box lengths exists as a
+// ghost: the reference makes ghosts only of particles within ghost_range * kernrange * h of
+// the boundary they are copied across, with h as at the tree build (HydroTree.cpp:494-543).
+__device__ __forceinline__ bool ghost_exists(const SphParams& prm, const Particles& p, int j, const int* sh) {
+  const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+  const double r[3] = {p.x[j], p.y[j], p.z[j]};
+  for (int k = 0; k < 3; k++) {
+    if (sh[k] > 1 || sh[k] < -1) return false;
+    if (sh[k] > 0 && !(r[k] < __dadd_rn(prm.boxmin[k], lim))) return false;
+    if (sh[k] < 0 && !(r[k] > __dsub_rn(prm.boxmax[k], lim))) return false;
+  }
+  return true;
+}
+
+// levelneib bookkeeping of one SPH pair (i active, j its neighbour; GradhSph.cpp:445-446):
+// i takes the largest neighbour level and j the level of i (for a periodic image j is the
+// real particle, as NeighbourManager::GetNeibI maps ghosts back, NeighbourManager.h:296-302).
+__device__ __forceinline__ void lvn_pair(const Particles& p, int slot_i, int j, int& own) {
+  if (!p.level) return;
+  own = max(own, p.level[j]);
+  atomicMax(&p.lvn[j], p.level[slot_i]);
+}
+__device__ __forceinline__ void lvn_finish(const Particles& p, int slot, bool mine, int own) {
+  if (p.level && mine && own > 0) atomicMax(&p.lvn[slot], own);
+}
 
 // Tree topology (static per N) and stocked cell data (depth-first ids).
 struct Tree {

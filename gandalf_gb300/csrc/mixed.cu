@@ -214,8 +214,9 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
   const int first = t.cell_first[c], ncell = t.cell_n[c];
-  const bool mine = g < ncell;
-  const int slot = first + (mine ? g : 0);
+  const bool mine = g < ncell && is_active(p, first + g);
+  if (!__any_sync(kFull, mine)) return true;   // no active particle in this leaf
+  const int slot = first + (g < ncell ? g : 0);
   const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
   const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
   const double h_start = p.h[slot];
@@ -518,6 +519,7 @@ __device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& 
     bool abort_any = false;
     for (int g = wib; g < ncell; g += 8) {
       const int slot = first + g;
+      if (!is_active(p, slot)) continue;
       const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
       const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
       double hi = sm.h0[g], h_lower = 0.0, h_upper = hk;
@@ -922,8 +924,10 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   const int c = t.leaf_cell[leaf];
   const int first = t.cell_first[c], ncell = t.cell_n[c];
   const int pidx = pfirst + g;
-  const bool mine = pidx < ncell;
-  const int slot = first + (mine ? pidx : 0);
+  const bool mine = pidx < ncell && is_active(p, first + pidx);
+  if (SLICES == 1 && !__any_sync(kFull, mine)) return true;   // no active particle in this leaf
+  const int slot = first + (pidx < ncell ? pidx : 0);
+  int lvn_own = 0;
   TargetF T;
   load_target_f(p, mp, slot, T);
   LeafGeo G;
@@ -956,6 +960,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         const float d2 = dx * dx + dy * dy + dz * dz;
         if (sph_member(p, T, j, d2, mp.aux[j].z, prm, exact)) {
           hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
+          lvn_pair(p, slot, j, lvn_own);
           nsph++;
           if (cnt.record) {
             const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
@@ -1032,6 +1037,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   if (gave_up) return false;
   consume_ab();
   consume_c();
+  lvn_finish(p, slot, mine, lvn_own);
   if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
   unsigned long long a1 = nsph, a2 = ndir, a3 = ncellp, a4 = exact;
   for (int o = 16; o > 0; o >>= 1) {
@@ -1150,12 +1156,14 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
   const int first = t.cell_first[c], ncell = t.cell_n[c];
-  const bool mine = g < ncell;
-  const int slot = first + (mine ? g : 0);
+  const bool mine = g < ncell && is_active(p, first + g);
+  if (!__any_sync(kFull, mine)) return;   // no active particle in this leaf
+  const int slot = first + (g < ncell ? g : 0);
   TargetF T;
   load_target_f(p, mp, slot, T);
   AccF A = {};
   unsigned long long npairs = 0, exact = 0;
+  int lvn_own = 0;
   WarpLists L{list, list, list, 0, 0, 0, kHListA};
   const float4 bmin_f = mc.bbmin[c], bmax_f = mc.bbmax[c], hmin_f = mc.hbmin[c], hmax_f = mc.hbmax[c];
   const float half[3] = {(float) prm.boxhalf[0], (float) prm.boxhalf[1], (float) prm.boxhalf[2]};
@@ -1198,18 +1206,21 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
                       (pjh.z - T.ph.z) + (pjl.z - T.pl.z)};
         if (prm.periodic) {
           const double xj[3] = {p.x[j], p.y[j], p.z[j]}, xi[3] = {T.x, T.y, T.z};
+          int sh[3] = {0, 0, 0};   // image of j, in box lengths
           for (int k = 0; k < 3; k++) {
             if (fabsf(d[k]) > half[k] * 0.5f) {
               double dd = xj[k] - xi[k];
-              if (dd > prm.boxhalf[k]) dd -= prm.boxsize[k];
-              else if (dd < -prm.boxhalf[k]) dd += prm.boxsize[k];
+              if (dd > prm.boxhalf[k]) { dd -= prm.boxsize[k]; sh[k] = -1; }
+              else if (dd < -prm.boxhalf[k]) { dd += prm.boxsize[k]; sh[k] = 1; }
               d[k] = (float) dd;
             }
           }
+          if ((sh[0] | sh[1] | sh[2]) && !ghost_exists(prm, p, j, sh)) continue;
         }
         const float d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!sph_member(p, T, j, d2, mp.aux[j].z, prm, exact)) continue;
         hydro_pair_f(prm, mp, T, j, d[0], d[1], d[2], d2, pjh.w, A);
+        lvn_pair(p, slot, j, lvn_own);
         npairs++;
         if (cnt.record) {
           const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
@@ -1224,6 +1235,7 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
   unsigned long long a1 = npairs, a4 = exact;
   for (int o = 16; o > 0; o >>= 1) { a1 += __shfl_xor_sync(kFull, a1, o); a4 += __shfl_xor_sync(kFull, a4, o); }
   if (lane == 0) { atomicAdd(cnt.hydro_pairs, a1); atomicAdd(cnt.exact_checks, a4); }
+  lvn_finish(p, slot, mine, lvn_own);
   finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, 0.0, 0, 0, false);
 }
 

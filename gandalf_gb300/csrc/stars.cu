@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(256) k_gas_from_stars(Particles p, StarSet s) 
   const int n = p.n;
   for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const int slot = base + threadIdx.x;
-    const bool mine = slot < n;
+    const bool mine = slot < n && is_active(p, slot);
     double xi = 0, yi = 0, zi = 0, hi = 1;
     if (mine) { xi = p.x[slot]; yi = p.y[slot]; zi = p.z[slot]; hi = p.h[slot]; }
     double ax = 0.0, ay = 0.0, az = 0.0, pot = 0.0;

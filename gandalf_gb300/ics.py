@@ -77,6 +77,41 @@ def plummer_sphere(n: int = 262144, seed: int = 4321, rtrunc: float = 10.0) -> d
     return ics
 
 
+def rotating_cloud(n: int = 1048576, seed: int = 31, amp: float = 0.1, erot: float = 0.16,
+                   etherm: float = 0.26) -> dict:
+    """Uniform rotating sphere (R = M = G = 1) with an m = 2 density perturbation.
+
+    rho ~ 1 + amp cos(2 phi), imposed by displacing the azimuth of a uniform sphere:
+    phi + (amp/2) sin(2 phi) = phi_uniform, solved by Newton iteration.  Solid-body rotation
+    about z with E_rot / |E_grav| = erot (E_grav = -3/5, I = 2/5: omega^2 = erot 0.6 / 0.2);
+    isothermal gas with E_therm / |E_grav| = etherm, E_therm = (3/2) M c_s^2, c_s^2 = temp0 /
+    mu_bar (mu_bar = 1).
+    """
+    rng = np.random.default_rng(seed)
+    r = rng.random(n) ** (1.0 / 3.0)
+    cost = 2.0 * rng.random(n) - 1.0
+    phi0 = 2.0 * math.pi * rng.random(n)
+    phi = phi0.copy()
+    for _ in range(30):
+        f = phi + 0.5 * amp * np.sin(2.0 * phi) - phi0
+        phi -= f / (1.0 + amp * np.cos(2.0 * phi))
+    sint = np.sqrt(1.0 - cost * cost)
+    x = np.stack([r * sint * np.cos(phi), r * sint * np.sin(phi), r * cost], 1)
+    omega = math.sqrt(erot * 0.6 / 0.2)
+    v = np.stack([-omega * x[:, 1], omega * x[:, 0], np.zeros(n)], 1)
+    m = np.full(n, 1.0 / n)
+    cs2 = etherm * 0.6 / 1.5
+    gamma = 5.0 / 3.0
+    u = np.full(n, cs2 / (gamma - 1.0))
+    rho = 3.0 / (4.0 * math.pi) * (1.0 + amp * np.cos(2.0 * phi))
+    h = H_FAC * (m / rho) ** (1.0 / 3.0)
+    ics = _pack(x, v, m, u, h)
+    ics["params"] = dict(self_gravity=1, eos=1, periodic=0, thetamaxsqd=0.25, gamma_eos=gamma,
+                         temp0=cs2, mu_bar=1.0)
+    ics["kdk"] = dict(nlevels=4, level_diff_max=1, courant_mult=0.15, accel_mult=0.3, energy_mult=0.4)
+    return ics
+
+
 def kh_box(n: int = 32768, seed: int = 7, pressure: float = 2.5) -> dict:
     """Periodic 3-D Kelvin-Helmholtz box [0,1) x [0,1) x [0,0.25) (hydro only).
 
@@ -145,4 +180,5 @@ WORKLOADS = {
     "periodic_cube": periodic_cube,
     "plummer_sphere": plummer_sphere,
     "kh_box": kh_box,
+    "rotating_cloud": rotating_cloud,
 }

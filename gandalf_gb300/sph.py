@@ -176,6 +176,29 @@ class GradhSphTree:
     update_all_sph_forces = UpdateAllSphForces
     update_all_star_gas_forces = UpdateAllStarGasForces
 
+    # ---- KDK integration with block timesteps (SphSimulation::MainLoop) -------------------
+    def kdk_setup(self, **kw):
+        """PostInitialConditionsSetup: nlevels, level_diff_max, courant_mult, accel_mult,
+        energy_mult as the reference's parameters."""
+        k = _native.KdkConfig()
+        self._lib.gsph_kdk_config_defaults(ctypes.byref(k))
+        for name, val in kw.items():
+            setattr(k, name, type(getattr(k, name))(val))
+        self._check(self._lib.gsph_kdk_setup(self._ctx, ctypes.byref(k)), "kdk_setup")
+
+    def kdk_steps(self, nsteps: int, graph: bool = True):
+        self._check(self._lib.gsph_kdk_steps(self._ctx, int(nsteps), int(graph)), "kdk_steps")
+
+    def kdk_status(self) -> dict:
+        st = _native.KdkStatus()
+        self._check(self._lib.gsph_kdk_get_status(self._ctx, ctypes.byref(st)), "kdk_status")
+        return {k: getattr(st, k) for k, _ in _native.KdkStatus._fields_}
+
+    def kdk_state(self, name: str) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.float64)
+        self._check(self._lib.gsph_kdk_get_state(self._ctx, _native.KDK_FIELDS.index(name), _dp(out)), "kdk_state")
+        return out
+
     # ---- results --------------------------------------------------------------------------
     def field(self, name: str) -> np.ndarray:
         out = np.empty(self.n, dtype=np.float64)

@@ -170,6 +170,41 @@ int32_t gsph_step(gsph_ctx* ctx);
  * to gsph_step's. */
 int32_t gsph_step_graph(gsph_ctx* ctx);
 
+/* ---- KDK leapfrog with block timesteps --------------------------------------------------
+ * The gas part of SphSimulation::PostInitialConditionsSetup and MainLoop
+ * (src/Hydrodynamics/SphSimulation.cpp:203-565, :573-880) with SphLeapfrogKDK
+ * (src/Hydrodynamics/SphLeapfrogKDK.cpp) and Simulation::ComputeBlockTimesteps
+ * (src/Common/Simulation.cpp:1764-2190), run on the device: every step drifts all
+ * particles, rebuilds the tree, solves h and the forces of the active particles (those at
+ * the end of their step), repeats for particles the neighbour-timestep check activates,
+ * assigns new timestep levels and closes the steps that end.  The integer-time state stays
+ * on the device, so a sequence of steps needs no host round trip and can run as one CUDA
+ * graph.  Parameters as the reference's Nlevels, level_diff_max, courant_mult, accel_mult,
+ * energy_mult (Parameters.cpp:239-263); the energy equation is integrated for gas_eos =
+ * energy_eqn.  Stars are not supported here. */
+typedef struct gsph_kdk_config {
+  int32_t nlevels, level_diff_max;
+  double courant_mult, accel_mult, energy_mult;
+} gsph_kdk_config;
+void gsph_kdk_config_defaults(gsph_kdk_config* cfg);
+/* Initial h solves, forces and timesteps for the imported particles (time 0). */
+int32_t gsph_kdk_setup(gsph_ctx* ctx, const gsph_kdk_config* cfg);
+/* nsteps main-loop steps; use_graph = 1 replays them from one captured CUDA graph. */
+int32_t gsph_kdk_steps(gsph_ctx* ctx, int32_t nsteps, int32_t use_graph);
+typedef struct gsph_kdk_status {
+  int64_t n, nresync, level_max, level_step, nsteps;   /* integer time (Simulation.h:187-215) */
+  double t, timestep, dt_max;
+  int64_t active_updates;     /* active particles summed over all force passes since setup */
+  uint32_t status;            /* 1: invalid timestep, 2: timestep checks did not settle */
+} gsph_kdk_status;
+int32_t gsph_kdk_get_status(gsph_ctx* ctx, gsph_kdk_status* out);
+enum gsph_kdk_field {
+  GSPH_KDK_X = 0, GSPH_KDK_Y, GSPH_KDK_Z, GSPH_KDK_VX, GSPH_KDK_VY, GSPH_KDK_VZ, GSPH_KDK_U, GSPH_KDK_DT,
+  GSPH_KDK_TLAST, GSPH_KDK_LEVEL, GSPH_KDK_NSTEP, GSPH_KDK_NLAST, GSPH_KDK_LEVELNEIB, GSPH_KDK_COUNT
+};
+/* One integration field for all particles, input order, as doubles (n values). */
+int32_t gsph_kdk_get_state(gsph_ctx* ctx, int32_t which, double* out);
+
 /* ---- batches of independent simulations ------------------------------------------------
  * No counterpart in the reference (which steps one simulation per process).  A batch
  * steps many mixed-precision contexts at once: each of the density and force passes is one

@@ -46,9 +46,16 @@ struct InHeader {
   int32_t nleafmax;
   int32_t multipole;      // 0 monopole, 1 quadrupole
   int32_t nstar;          // star particles following the gas arrays
-  int32_t pad1;
+  int32_t kdk;            // 1: a KdkBlock follows the header (multi-step run)
   double h_fac, h_converge, alpha_visc, beta_visc, gamma_eos, thetamaxsqd, temp0, mu_bar;
   double boxmin[3], boxmax[3];
+};
+
+// Multi-step run: SetupSimulation then nsteps SphSimulation::MainLoop calls
+// (src/Hydrodynamics/SphSimulation.cpp:573-880) with the KDK leapfrog and block timesteps.
+struct KdkBlock {
+  int32_t nsteps, nlevels, level_diff_max, pad;
+  double courant_mult, accel_mult, energy_mult, pad2;
 };
 
 void die(const char* msg) { std::fprintf(stderr, "gsph_ref_harness: %s\n", msg); std::exit(2); }
@@ -76,6 +83,8 @@ int main(int argc, char** argv) {
   InHeader hd;
   if (std::fread(&hd, sizeof(hd), 1, fin) != 1) die("short header");
   if (std::memcmp(hd.magic, "GSPHIN01", 8) != 0) die("bad magic");
+  KdkBlock kb{};
+  if (hd.kdk && std::fread(&kb, sizeof(kb), 1, fin) != 1) die("short kdk block");
   const int N = hd.n;
   std::vector<double> arr[9];
   for (int a = 0; a < 9; a++) {
@@ -113,7 +122,11 @@ int main(int argc, char** argv) {
   S("multipole", hd.multipole == 1 ? "quadrupole" : "monopole");
   I("Nleafmax", hd.nleafmax); F("thetamaxsqd", hd.thetamaxsqd);
   I("ntreebuildstep", 1); I("ntreestockstep", 1);
-  I("Nlevels", 1); I("sink_particles", 0);
+  I("Nlevels", hd.kdk ? kb.nlevels : 1); I("sink_particles", 0);
+  if (hd.kdk) {
+    I("level_diff_max", kb.level_diff_max);
+    F("courant_mult", kb.courant_mult); F("accel_mult", kb.accel_mult); F("energy_mult", kb.energy_mult);
+  }
   S("sph_integration", "lfkdk");
   const char* bl[3] = {"boundary_lhs[0]", "boundary_lhs[1]", "boundary_lhs[2]"};
   const char* br[3] = {"boundary_rhs[0]", "boundary_rhs[1]", "boundary_rhs[2]"};
@@ -138,6 +151,34 @@ int main(int argc, char** argv) {
   const double t_setup = now_s() - t_setup0;
 
   GradhSphSimulation<3>* sim = static_cast<GradhSphSimulation<3>*>(base);
+  if (hd.kdk) {
+    // ---- multi-step run: the reference's own main loop ----------------------------------
+    const double tk0 = now_s();
+    for (int s = 0; s < kb.nsteps; s++) sim->MainLoop();
+    const double tk = now_s() - tk0;
+    Sph<3>* sp = sim->sph;
+    const int NK = 24;
+    std::vector<double> kout((size_t) N * NK);
+    for (int i = 0; i < N; i++) {
+      GradhSphParticle<3>& p = static_cast<GradhSphParticle<3>&>(sp->GetSphParticlePointer(i));
+      if (p.iorig != i) die("particle order changed");
+      double* o = &kout[(size_t) i * NK];
+      for (int k = 0; k < 3; k++) { o[k] = p.r[k]; o[3 + k] = p.v[k]; o[6 + k] = p.a[k]; }
+      o[9] = p.h; o[10] = p.rho; o[11] = p.u; o[12] = p.level; o[13] = p.nstep; o[14] = p.nlast;
+      o[15] = p.levelneib; o[16] = p.dt; o[17] = p.tlast; o[18] = p.dudt; o[19] = p.div_v;
+      o[20] = p.gpot; o[21] = p.invomega; o[22] = p.pressure; o[23] = p.sound;
+    }
+    std::vector<double> g = {(double) sim->n, sim->t, sim->timestep, (double) sim->level_max,
+                             (double) sim->level_step, (double) sim->nresync, (double) sim->Nsteps, sim->dt_max};
+    FILE* fk = std::fopen("kdk.bin", "wb");
+    write_block(fk, kout);
+    write_block(fk, g);
+    std::fclose(fk);
+    fk = std::fopen("timing.txt", "w");
+    std::fprintf(fk, "setup %.6f\nkdk_steps %.6f\n", t_setup, tk);
+    std::fclose(fk);
+    return 0;
+  }
   Sph<3>* sph = sim->sph;
   typedef GradhSphTree<3, GradhSphParticle> TreeType;
   TreeType* neib = reinterpret_cast<TreeType*>(sim->sphneib);

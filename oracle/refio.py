@@ -36,11 +36,16 @@ def available() -> bool:
 
 
 STAR_KEYS = ("x", "y", "z", "vx", "vy", "vz", "m", "h")
+KDK_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "h", "rho", "u", "level", "nstep", "nlast",
+              "levelneib", "dt", "tlast", "dudt", "div_v", "gpot", "invomega", "pressure", "sound"]
+KDK_GLOBAL = ["n", "t", "timestep", "level_max", "level_step", "nresync", "Nsteps", "dt_max"]
+KDK_DEFAULTS = dict(nsteps=1, nlevels=1, level_diff_max=1, courant_mult=0.15, accel_mult=0.3, energy_mult=0.4)
 STAR_FIELDS = ["ax", "ay", "az", "adotx", "adoty", "adotz", "gpot"]
 
 
-def write_input(path: str, ics: dict, params: dict) -> None:
-    """ics may carry ``stars``: a dict of star arrays (STAR_KEYS)."""
+def write_input(path: str, ics: dict, params: dict, kdk: dict | None = None) -> None:
+    """ics may carry ``stars``: a dict of star arrays (STAR_KEYS); kdk: a multi-step run
+    (KDK_DEFAULTS keys)."""
     p = dict(DEFAULTS)
     p.update(params)
     n = len(ics["x"])
@@ -49,10 +54,15 @@ def write_input(path: str, ics: dict, params: dict) -> None:
     with open(path, "wb") as f:
         f.write(b"GSPHIN01")
         f.write(struct.pack("<8i", n, int(p["self_gravity"]), int(p["eos"]), int(p["periodic"]),
-                            int(p["nleafmax"]), int(p["multipole"]), nstar, 0))
+                            int(p["nleafmax"]), int(p["multipole"]), nstar, 1 if kdk else 0))
         f.write(struct.pack("<8d", p["h_fac"], p["h_converge"], p["alpha_visc"], p["beta_visc"],
                             p["gamma_eos"], p["thetamaxsqd"], p["temp0"], p["mu_bar"]))
         f.write(struct.pack("<6d", *p["boxmin"], *p["boxmax"]))
+        if kdk:
+            k = dict(KDK_DEFAULTS)
+            k.update(kdk)
+            f.write(struct.pack("<4i", int(k["nsteps"]), int(k["nlevels"]), int(k["level_diff_max"]), 0))
+            f.write(struct.pack("<4d", k["courant_mult"], k["accel_mult"], k["energy_mult"], 0.0))
         for key in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h"):
             f.write(np.ascontiguousarray(ics[key], dtype="<f8").tobytes())
         for key in STAR_KEYS if nstar else ():
@@ -75,6 +85,31 @@ def _blocks(path, dtype):
 
 def _csr(off, ids):
     return [ids[off[i]:off[i + 1]] for i in range(len(off) - 1)]
+
+
+def run_kdk(ics: dict, params: dict, kdk: dict, workdir: str | None = None) -> dict:
+    """SetupSimulation + kdk["nsteps"] reference main-loop steps; per-particle state
+    (KDK_FIELDS, input order) and the integer-time globals (KDK_GLOBAL)."""
+    if not available():
+        raise RuntimeError("upstream harness not built (make -f oracle/Makefile.ref)")
+    tmp = os.path.abspath(workdir) if workdir else tempfile.mkdtemp(prefix="gsph_kdk_")
+    os.makedirs(tmp, exist_ok=True)
+    inp = os.path.join(tmp, "input.bin")
+    write_input(inp, ics, params, kdk)
+    res = subprocess.run([HARNESS, inp, tmp], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"reference harness failed ({res.returncode}): {res.stdout[-2000:]}"
+                           f"{res.stderr[-2000:]}")
+    n = len(ics["x"])
+    kb, gb = _blocks(os.path.join(tmp, "kdk.bin"), "<f8")
+    kb = kb.reshape(n, len(KDK_FIELDS))
+    timing = {}
+    with open(os.path.join(tmp, "timing.txt")) as f:
+        for line in f:
+            k, v = line.split()
+            timing[k] = float(v)
+    return {"particles": {k: kb[:, i].copy() for i, k in enumerate(KDK_FIELDS)},
+            "global": {k: float(gb[i]) for i, k in enumerate(KDK_GLOBAL)}, "timing": timing}
 
 
 def run(ics: dict, params: dict, workdir: str | None = None) -> dict:

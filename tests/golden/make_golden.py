@@ -13,6 +13,10 @@ oracle/Makefile.ref) on small seeded particle sets and stores, per case:
                 star <- gas results (oracle/refio.STAR_FIELDS order)
 Hashes are sums of splitmix64(id) (gandalf_gb300.sph.list_hash).
 
+KDK cases (multi-step runs of the reference's main loop with block timesteps) store the
+inputs, the integrator parameters (kdk_*), the final per-particle state
+(oracle/refio.KDK_FIELDS order) and the integer-time globals (oracle/refio.KDK_GLOBAL).
+
     python tests/golden/make_golden.py     # needs oracle/_ref built
 """
 from __future__ import annotations
@@ -35,6 +39,37 @@ CASES = {
     "plummer_stars2048": lambda: ics_mod.with_stars(ics_mod.plummer_sphere(2048, seed=13), 16, h=0.05,
                                                     sigma_v=0.1, seed=14),
 }
+
+
+def _cube_adiabatic(n, seed):
+    c = ics_mod.periodic_cube(n, seed=seed)
+    c["kdk"] = dict(nlevels=3, level_diff_max=1, courant_mult=0.15, accel_mult=0.3, energy_mult=0.4)
+    return c
+
+
+KDK_CASES = {
+    "rotating_kdk2048": (lambda: ics_mod.rotating_cloud(2048, seed=41), 8),
+    "cube_kdk2048": (lambda: _cube_adiabatic(2048, 42), 6),
+}
+
+
+def make_kdk(name):
+    fn, nsteps = KDK_CASES[name]
+    c = fn()
+    prm = dict(c["params"])
+    kdk = dict(c["kdk"])
+    kdk["nsteps"] = nsteps
+    r = refio.run_kdk(c, prm, kdk)
+    out = {k: c[k] for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")}
+    out["state"] = np.stack([r["particles"][k] for k in refio.KDK_FIELDS], axis=1)
+    out["global"] = np.array([r["global"][k] for k in refio.KDK_GLOBAL])
+    for k, v in prm.items():
+        out["param_" + k] = np.asarray(v)
+    for k, v in kdk.items():
+        out["kdk_" + k] = np.asarray(v)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")
 
 
 def csr(lists):
@@ -72,5 +107,8 @@ def make(name):
 
 
 if __name__ == "__main__":
-    for name in (sys.argv[1:] or CASES):
-        make(name)
+    for name in (sys.argv[1:] or list(CASES) + list(KDK_CASES)):
+        if name in KDK_CASES:
+            make_kdk(name)
+        else:
+            make(name)
