@@ -166,6 +166,109 @@ def ensemble_main(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def kdk_main(args, rank, world, local):
+    """Rotating isothermal cloud (uniform sphere, m = 2 perturbation, solid-body rotation),
+    N = 1,048,576, self-gravity theta = 0.5 quadrupole, 4 block-timestep levels: K KDK main
+    loop steps (default 20) replayed from one CUDA graph, FP64 and mixed forms.  The unit
+    of work is one active particle through one force pass (SURVEY metric for block-timestep
+    configurations)."""
+    import torch
+    from gandalf_gb300 import ics as ics_mod
+    from gandalf_gb300 import _native
+    from gandalf_gb300 import build as gbuild
+    from gandalf_gb300.sph import GradhSphTree
+    gbuild.build()
+    lib = _native.load()
+    n = args.n or 1048576
+    c = ics_mod.rotating_cloud(n, seed=31 + rank)
+    params = c.pop("params")
+    kdk = c.pop("kdk")
+    K = args.steps if args.steps != 10 else 20
+    stream = torch.cuda.current_stream()
+    forms = ["fp64", "mixed"] if args.precision == "auto" else [args.precision]
+    out, finals = {}, {}
+    with ClockSampler(local) as clk:
+        for form in forms:
+            t = GradhSphTree(params, precision=form, device=local)
+            t.set_stream(stream.cuda_stream)
+            t.set_particles(c)
+            t.kdk_setup(**kdk)
+            t.kdk_steps(K, graph=True)          # capture + warm-up run of the K-step graph
+            torch.cuda.synchronize()
+            u0 = t.kdk_status()["active_updates"]
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            t.kdk_steps(K, graph=True)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            st = t.kdk_status()
+            upd = st["active_updates"] - u0
+            s2 = t.stats()
+            out[form] = {"value": upd / (ms * 1e-3), "ms_total": ms, "ms_per_step": ms / K, "active_updates": upd,
+                         "active_fraction_per_step": upd / (K * n), "particle_steps_per_s": n * K / (ms * 1e-3),
+                         "level_max": st["level_max"], "t_end": st["t"],
+                         "counts": {k: s2[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs", "cell_pairs")},
+                         "launches": s2["launches"]}
+            finals[form] = t.results()
+            t.close()
+    clocks = clk.summary()
+    head = "mixed" if "mixed" in out else forms[0]
+    R = out[head]
+    line = {"metric": METRIC, "value": world * R["value"], "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": 1, "ms_per_step": R["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 pairs / f64 positions" if head == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": "rotating_cloud", "n": n, "nlevels": kdk["nlevels"], "kdk_steps": K,
+                       "level_diff_max": kdk["level_diff_max"], "courant_mult": kdk["courant_mult"],
+                       "accel_mult": kdk["accel_mult"], "eos": "isothermal", "thetamaxsqd": 0.25,
+                       "multipole": "quadrupole", "precision": head, "cuda_graph": "K steps in one graph",
+                       "unit_of_work": "active particle per force pass", "parallelism": f"replicas{world}",
+                       "l2": "working set (1M particles) larger than L2"},
+            "gpu_launches": R["launches"], "forms": out, "clocks": clocks}
+    if "fp64" in out and "mixed" in out:
+        line["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+        a, b = finals["mixed"], finals["fp64"]
+        errs = {}
+        for k in ("rho", "h"):
+            e = np.abs(a[k] - b[k]) / np.abs(b[k])
+            errs[k] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
+        A = np.stack([a["ax"], a["ay"], a["az"]], 1)
+        B = np.stack([b["ax"], b["ay"], b["az"]], 1)
+        nb = np.linalg.norm(B, axis=1)
+        e = np.linalg.norm(A - B, axis=1) / nb
+        errs["a"] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
+        line["mixed_vs_fp64_rel_err_after_all_steps"] = errs
+    st = out[head]["counts"]
+    flops = (st["density_pairs"] * FLOPS["density"] + st["hydro_pairs"] * FLOPS["hydro_grav"] +
+             st["direct_pairs"] * FLOPS["direct"] + st["cell_pairs"] * FLOPS["quad"])
+    peak_gf = lib.gsph_fma_peak_gflops(local, 1 if head == "fp64" else 0)
+    achieved = flops / (R["ms_total"] * 1e-3) / 1e12
+    line["roofline"] = {"bound": "fp32" if head == "mixed" else "fp64", "kernel": "whole K-step sequence",
+                        "achieved": achieved, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
+                        "frac": achieved / (peak_gf / 1e3), "traffic": None,
+                        "peak_source": "measured FMA-loop throughput (gsph_fma_peak_gflops)"}
+    if not args.no_e2e:
+        # host particles in, setup, K steps, results out, through the C ABI
+        t = GradhSphTree(params, precision=head, device=local)
+        t0 = time.perf_counter()
+        t.set_particles(c)
+        t.kdk_setup(**kdk)
+        u0 = t.kdk_status()["active_updates"]
+        t.kdk_steps(K, graph=True)
+        res = {k: t.kdk_state(k) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        res.update(t.results())
+        wall = time.perf_counter() - t0
+        upd = t.kdk_status()["active_updates"] - u0
+        t.close()
+        line["e2e"] = {"value": world * upd / wall, "unit": UNIT, "h2d_bytes_per_step": n * 9 * 8 / K,
+                       "d2h_bytes_per_step": n * 8 * (6 + len(res) - 6) / K,
+                       "path": "gsph_set_particles + gsph_kdk_setup + gsph_kdk_steps(K, graph) + field reads; "
+                               "setup (two h solves and a force pass) inside the timed span"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def workload(name, n):
     from gandalf_gb300 import ics
     if name == "plummer_sphere":
@@ -399,6 +502,11 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.workload == "rotating_cloud":
+        kdk_main(args, rank, world, local)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     if args.workload == "kh_ensemble":
         ensemble_main(args, rank, world, local)
         if world > 1:
