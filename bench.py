@@ -166,6 +166,72 @@ def ensemble_main(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def evrard_main(args, rank, world, local):
+    """Evrard sphere, N = 8,388,608 gas particles, self-gravity theta = 0.5 quadrupole, plus 64
+    stars coupled by FP64 direct sums (gas <- stars, star <- gas tree walk) in every step;
+    mixed form with the leaf size chosen by the autotuner, one graph-replayed step per
+    timed iteration."""
+    import torch
+    from gandalf_gb300 import ics as ics_mod
+    from gandalf_gb300 import _native
+    from gandalf_gb300 import build as gbuild
+    from gandalf_gb300.autotune import tune_leaf_size
+    from gandalf_gb300.sph import GradhSphTree
+    gbuild.build()
+    lib = _native.load()
+    n = args.n or 8388608
+    c = ics_mod.evrard_sphere(n, seed=51 + rank)
+    params = c.pop("params")
+    form = "mixed" if args.precision == "auto" else args.precision
+    steps = args.steps if args.steps != 10 else 3
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    with ClockSampler(local) as clk:
+        tune = tune_leaf_size(c, params, precision=form, steps=1, device=local)
+        t = GradhSphTree(params, precision=form, nleafmax=tune["nleafmax"], device=local)
+        stream = torch.cuda.current_stream()
+        t.set_stream(stream.cuda_stream)
+        t.set_particles(c)
+        for _ in range(max(1, args.warmup)):
+            t.step(graph=True)
+        torch.cuda.synchronize()
+        ms = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            t.step(graph=True)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        st = t.stats()
+        sf = t.star_forces()
+    clocks = clk.summary()
+    t.close()
+    value = world * n * steps / (ms * 1e-3)
+    flops = (st["density_pairs"] * FLOPS["density"] + st["hydro_pairs"] * FLOPS["hydro_grav"] +
+             st["direct_pairs"] * FLOPS["direct"] + st["cell_pairs"] * FLOPS["quad"])
+    peak_gf = lib.gsph_fma_peak_gflops(local, 0 if form == "mixed" else 1)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 pairs / f64 positions" if form == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": "evrard_sphere", "n": n, "nstar": 64, "star_mass": 1e-3, "star_h": 0.01,
+                       "thetamaxsqd": 0.25, "multipole": "quadrupole", "precision": form,
+                       "nleafmax_autotuned": tune, "cuda_graph": True, "parallelism": f"replicas{world}",
+                       "l2": "flushed between timed steps (256 MiB write)"},
+            "gpu_launches": st["launches"],
+            "counts": {k: st[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs", "cell_pairs")},
+            "phases_ms_last_step": {k: st[k] for k in ("ms_build", "ms_density", "ms_hmax", "ms_forces")},
+            "star_gpot_mean": float(np.mean(sf["gpot"])),
+            "roofline": {"bound": "fp32" if form == "mixed" else "fp64", "kernel": "whole step",
+                         "achieved": flops / (ms / steps * 1e-3) / 1e12, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
+                         "frac": flops / (ms / steps * 1e-3) / 1e12 / (peak_gf / 1e3), "traffic": None,
+                         "peak_source": "measured FMA-loop throughput (gsph_fma_peak_gflops)"},
+            "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def kdk_main(args, rank, world, local):
     """Rotating isothermal cloud (uniform sphere, m = 2 perturbation, solid-body rotation),
     N = 1,048,576, self-gravity theta = 0.5 quadrupole, 4 block-timestep levels: K KDK main
@@ -502,6 +568,11 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.workload == "evrard_sphere":
+        evrard_main(args, rank, world, local)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     if args.workload == "rotating_cloud":
         kdk_main(args, rank, world, local)
         if world > 1:

@@ -77,6 +77,25 @@ def plummer_sphere(n: int = 262144, seed: int = 4321, rtrunc: float = 10.0) -> d
     return ics
 
 
+def evrard_sphere(n: int = 8388608, seed: int = 51, nstar: int = 64) -> dict:
+    """Evrard collapse initial state: gas sphere R = M = G = 1 with rho ~ 1/r (r = R sqrt(U),
+    isotropic directions), u = 0.05 G M / R, at rest; plus ``nstar`` stars of mass 1e-3,
+    uniform in r < 0.5, at rest, softening length h = 0.01 (with_stars)."""
+    rng = np.random.default_rng(seed)
+    r = np.sqrt(rng.random(n))
+    x = r[:, None] * _unit_vectors(rng, n)
+    v = np.zeros((n, 3))
+    m = np.full(n, 1.0 / n)
+    u = np.full(n, 0.05)
+    rho = 1.0 / (2.0 * math.pi * np.maximum(r, 1e-6))
+    h = H_FAC * (m / rho) ** (1.0 / 3.0)
+    ics = _pack(x, v, m, u, h)
+    ics["params"] = dict(self_gravity=1, eos=0, periodic=0, thetamaxsqd=0.25, gamma_eos=5.0 / 3.0)
+    if nstar:
+        ics = with_stars(ics, nstar, rmax=0.5, mass=1.0e-3, h=0.01, seed=seed + 1)
+    return ics
+
+
 def rotating_cloud(n: int = 1048576, seed: int = 31, amp: float = 0.1, erot: float = 0.16,
                    etherm: float = 0.26) -> dict:
     """Uniform rotating sphere (R = M = G = 1) with an m = 2 density perturbation.
@@ -181,4 +200,5 @@ WORKLOADS = {
     "plummer_sphere": plummer_sphere,
     "kh_box": kh_box,
     "rotating_cloud": rotating_cloud,
+    "evrard_sphere": evrard_sphere,
 }
