@@ -50,6 +50,22 @@ FLOPS = dict(density=42, hydro=80, hydro_grav=145, direct=24, quad=82, mono=24)
 FORCE_TRAFFIC = {("plummer_sphere", 262144, "mixed"): 49.09e6 + 0.697e6 + 5.79e6}
 
 
+def max_over_ranks(ms, world, device="cuda"):
+    """The job's time for replicas on several GPUs: the slowest rank's (all-reduce MAX)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_throughput(units_per_rank, ms, world):
+    """Whole-job units per second: every rank processes units_per_rank in (at most) ms."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -115,11 +131,7 @@ def ensemble_main(args, rank, world, local):
             torch.cuda.synchronize()
             ms_seq += ev0.elapsed_time(ev1)
     clocks = clk.summary()
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms_batch], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_batch = float(tt.item())
+    ms_batch = max_over_ranks(ms_batch, world)
     counts = {k: sum(t.stats()[k] for t in trees) for k in ("density_pairs", "hydro_pairs", "exact_checks")}
     flops = counts["density_pairs"] * FLOPS["density"] + counts["hydro_pairs"] * FLOPS["hydro"]
     peak_gf = lib.gsph_fma_peak_gflops(local, 0)
@@ -143,7 +155,7 @@ def ensemble_main(args, rank, world, local):
     batch.close()
     for t in trees:
         t.close()
-    value = world * ntot * args.steps / (ms_batch * 1e-3)
+    value = job_throughput(ntot * args.steps, ms_batch, world)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batch / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 pairs / f64 positions", "data": "synthetic",
@@ -207,7 +219,8 @@ def evrard_main(args, rank, world, local):
         sf = t.star_forces()
     clocks = clk.summary()
     t.close()
-    value = world * n * steps / (ms * 1e-3)
+    ms = max_over_ranks(ms, world)
+    value = job_throughput(n * steps, ms, world)
     flops = (st["density_pairs"] * FLOPS["density"] + st["hydro_pairs"] * FLOPS["hydro_grav"] +
              st["direct_pairs"] * FLOPS["direct"] + st["cell_pairs"] * FLOPS["quad"])
     peak_gf = lib.gsph_fma_peak_gflops(local, 0 if form == "mixed" else 1)
@@ -281,7 +294,10 @@ def kdk_main(args, rank, world, local):
     clocks = clk.summary()
     head = "mixed" if "mixed" in out else forms[0]
     R = out[head]
-    line = {"metric": METRIC, "value": world * R["value"], "unit": UNIT, "n_gpus": world, "steps": K,
+    R["ms_total"] = max_over_ranks(R["ms_total"], world)
+    R["value"] = R["active_updates"] / (R["ms_total"] * 1e-3)
+    line = {"metric": METRIC, "value": job_throughput(R["active_updates"], R["ms_total"], world), "unit": UNIT,
+            "n_gpus": world, "steps": K,
             "warmup": 1, "ms_per_step": R["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 pairs / f64 positions" if head == "mixed" else "f64",
             "data": "synthetic",
@@ -612,12 +628,8 @@ def main():
     ok = [f for f in forms if "error" not in results[f]]
     head = "mixed" if "mixed" in ok else ok[0]
     R = results[head]
-    ms = R["ms_total"]
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * n * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(R["ms_total"], world)
+    value = job_throughput(n * args.steps, ms, world)
     e2e = None
     if not args.no_e2e:
         E = run_e2e(c, params, head, max(1, min(args.steps, 5)), 1, not args.no_graph)
