@@ -884,7 +884,7 @@ __device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Pa
   if (cnt.record) {
     unsigned long long dc = ndir, dh = dhash;
     for (int o = 1; o < LPG; o <<= 1) { dc += __shfl_xor_sync(kFull, dc, o); dh += __shfl_xor_sync(kFull, dh, o); }
-    if (mine && sl == 0) { cnt.rec_dir_cnt[slot] = dc; cnt.rec_dir_hash[slot] = dh; }
+    if (mine && sl == 0) { atomicAdd(&cnt.rec_dir_cnt[slot], dc); atomicAdd(&cnt.rec_dir_hash[slot], dh); }
   }
   if (!(mine && sl == 0)) return;
   const double rho = p.rho[slot];
@@ -934,16 +934,123 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   load_leaf_geo(t, mc, c, G);
   const bool quad = prm.multipole == 1;
   AccF A = {};
-  unsigned long long nsph = 0, ndir = 0, ncellp = 0, exact = 0, dhash = 0, chash = 0, ccount = 0;
+  unsigned long long nsph = 0, ndir = 0, ndir_b = 0, ncellp = 0, exact = 0, dhash = 0, chash = 0, ccount = 0;
   bool gave_up = false;
   // lists have separate capacities: WarpLists keeps one, so the flush test is done here
   WarpLists L{la, lb, lc, 0, 0, 0, 1 << 30};
+  // Lists B (direct leaves) and C (multipole cells) run one source per lane against every
+  // target particle of the warp: positions relative to the leaf centre (hi + lo pairs,
+  // accurate to a few ulps of the separation), 8 targets per round held in registers, the
+  // per-target sums reduced over the warp afterwards and added to the target's first lane.
+  constexpr int GT = 32 / LPG;
+  const float4 lc_hi = mc.geo_hi[c], lc_lo = mc.geo_lo[c];
+  auto rel = [&](float4 h, float4 l, float& x, float& y, float& z) {
+    x = (h.x - lc_hi.x) + (l.x - lc_lo.x);
+    y = (h.y - lc_hi.y) + (l.y - lc_lo.y);
+    z = (h.z - lc_hi.z) + (l.z - lc_lo.z);
+  };
+  // the warp's targets, broadcast from shared memory: leaf-relative position, w = 1 when active
+  __shared__ float4 s_tgt[8][32];
+  float4* tgt = s_tgt[(threadIdx.x >> 5) & 7];
+  {
+    float x, y, z;
+    rel(T.ph, T.pl, x, y, z);
+    if (sl == 0) tgt[g] = make_float4(x, y, z, mine ? 1.0f : 0.0f);
+    __syncwarp();
+  }
+  auto add_to_targets = [&](float (&acc)[8][4], int u0) {
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      if (u0 + u >= GT) break;
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        for (int o = 16; o > 0; o >>= 1) acc[u][k] = __fadd_rn(acc[u][k], __shfl_xor_sync(kFull, acc[u][k], o));
+      if (lane == (u0 + u) * LPG) {
+        A.ag[0] = __fadd_rn(A.ag[0], acc[u][0]); A.ag[1] = __fadd_rn(A.ag[1], acc[u][1]);
+        A.ag[2] = __fadd_rn(A.ag[2], acc[u][2]); A.gpot = __fadd_rn(A.gpot, acc[u][3]);
+      }
+    }
+  };
   auto consume_c = [&]() {
-    if (!mine) return;
-    for (int e = sl; e < L.nc; e += LPG) {
-      cell_term_f(mc, L.c[e], T, quad, A);
-      ncellp++;
-      if (cnt.record && g == 0) { chash += mix64((unsigned long long) L.c[e]); ccount++; }
+#pragma unroll
+    for (int u0 = 0; u0 < GT; u0 += 8) {
+      float acc[8][4] = {};
+      for (int e = lane; e < L.nc; e += 32) {
+        const int cc = L.c[e];
+        const float4 ch = mc.com_hi[cc], cl = mc.com_lo[cc];
+        float cx, cy, cz;
+        rel(ch, cl, cx, cy, cz);
+        const float4 q = quad ? mc.quad[cc] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float q4 = cl.w;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          if (u0 + u >= GT) continue;
+          const float4 tu = tgt[u0 + u];
+          if (tu.w == 0.0f) continue;
+          // explicit roundings: the same sums in every kernel this leaf code is built into
+          const float dx = __fsub_rn(tu.x, cx), dy = __fsub_rn(tu.y, cy), dz = __fsub_rn(tu.z, cz);
+          const float r2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), 1.0e-20f);
+          const float inv = rsqrtf(r2);
+          const float inv2 = __fmul_rn(inv, inv);
+          const float mon = __fmul_rn(__fmul_rn(ch.w, inv2), inv);
+          float ax = __fmul_rn(-mon, dx), ay = __fmul_rn(-mon, dy), az = __fmul_rn(-mon, dz);
+          float pot = __fmul_rn(ch.w, inv);
+          if (quad) {
+            const float inv5 = __fmul_rn(__fmul_rn(inv2, inv2), inv);
+            const float qzz = -__fadd_rn(q.x, q.z);
+            const float qx = __fmaf_rn(q.w, dz, __fmaf_rn(q.y, dy, __fmul_rn(q.x, dx)));
+            const float qy = __fmaf_rn(q4, dz, __fmaf_rn(q.z, dy, __fmul_rn(q.y, dx)));
+            const float qz = __fmaf_rn(qzz, dz, __fmaf_rn(q4, dy, __fmul_rn(q.w, dx)));
+            const float qscalar = __fmaf_rn(qz, dz, __fmaf_rn(qy, dy, __fmul_rn(qx, dx)));
+            const float qfactor = __fmul_rn(__fmul_rn(__fmul_rn(2.5f, qscalar), inv5), inv2);
+            ax = __fadd_rn(ax, __fmaf_rn(qx, inv5, __fmul_rn(-qfactor, dx)));
+            ay = __fadd_rn(ay, __fmaf_rn(qy, inv5, __fmul_rn(-qfactor, dy)));
+            az = __fadd_rn(az, __fmaf_rn(qz, inv5, __fmul_rn(-qfactor, dz)));
+            pot = __fmaf_rn(__fmul_rn(0.5f, qscalar), inv5, pot);
+          }
+          acc[u][0] = __fadd_rn(acc[u][0], ax); acc[u][1] = __fadd_rn(acc[u][1], ay);
+          acc[u][2] = __fadd_rn(acc[u][2], az); acc[u][3] = __fadd_rn(acc[u][3], pot);
+          ncellp++;
+        }
+        if (u0 == 0 && cnt.record) { chash += mix64((unsigned long long) cc); ccount++; }
+      }
+      add_to_targets(acc, u0);
+    }
+  };
+  auto consume_b = [&]() {
+#pragma unroll
+    for (int u0 = 0; u0 < GT; u0 += 8) {
+      float acc[8][4] = {};
+      for (int e0 = 0; e0 < L.nb; e0 += LPG) {
+        const int e = e0 + lane / GT, q = lane % GT;
+        if (e >= L.nb) continue;
+        const int node = L.b[e];
+        if (q >= t.cell_n[node]) continue;
+        const int j = t.cell_first[node] + q;
+        const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+        float sx, sy, sz;
+        rel(pjh, pjl, sx, sy, sz);
+        const float mj = pjh.w;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          if (u0 + u >= GT) continue;
+          const float4 tu = tgt[u0 + u];
+          if (tu.w == 0.0f) continue;
+          const float dx = __fsub_rn(sx, tu.x), dy = __fsub_rn(sy, tu.y), dz = __fsub_rn(sz, tu.z);
+          const float r2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), 1.0e-20f);
+          const float inv = rsqrtf(r2);
+          const float inv3 = __fmul_rn(__fmul_rn(__fmul_rn(inv, inv), inv), mj);
+          acc[u][0] = __fmaf_rn(dx, inv3, acc[u][0]); acc[u][1] = __fmaf_rn(dy, inv3, acc[u][1]);
+          acc[u][2] = __fmaf_rn(dz, inv3, acc[u][2]); acc[u][3] = __fmaf_rn(mj, inv, acc[u][3]);
+          ndir_b++;
+          if (cnt.record) {
+            const int ts = first + pfirst + u0 + u;
+            atomicAdd(&cnt.rec_dir_cnt[ts], 1ull);
+            atomicAdd(&cnt.rec_dir_hash[ts], mix64((unsigned long long) p.id[j]));
+          }
+        }
+      }
+      add_to_targets(acc, u0);
     }
   };
   auto consume_ab = [&]() {
@@ -971,20 +1078,6 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           ndir++;
           if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
         }
-      }
-    }
-    for (int e = 0; e < L.nb; e++) {
-      const int node = L.b[e];
-      const int f = t.cell_first[node], nn = t.cell_n[node];
-      for (int q = sl; q < nn; q += LPG) {
-        const int j = f + q;
-        const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
-        const float dx = (pjh.x - T.ph.x) + (pjl.x - T.pl.x);
-        const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
-        const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
-        direct_term_f(dx, dy, dz, pjh.w, A);
-        ndir++;
-        if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
       }
     }
   };
@@ -1031,15 +1124,16 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     if (L.nc > capc - 32) { consume_c(); L.nc = 0; __syncwarp(); }
     if (L.na > capa - 32 || L.nb > capb - 32) {
       if (give_up) { gave_up = true; break; }
-      consume_ab(); L.na = 0; L.nb = 0; __syncwarp();
+      consume_ab(); consume_b(); L.na = 0; L.nb = 0; __syncwarp();
     }
   }
   if (gave_up) return false;
   consume_ab();
+  consume_b();
   consume_c();
   lvn_finish(p, slot, mine, lvn_own);
   if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
-  unsigned long long a1 = nsph, a2 = ndir, a3 = ncellp, a4 = exact;
+  unsigned long long a1 = nsph, a2 = ndir + ndir_b, a3 = ncellp, a4 = exact;
   for (int o = 16; o > 0; o >>= 1) {
     a1 += __shfl_xor_sync(kFull, a1, o); a2 += __shfl_xor_sync(kFull, a2, o);
     a3 += __shfl_xor_sync(kFull, a3, o); a4 += __shfl_xor_sync(kFull, a4, o);
@@ -1084,7 +1178,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         tdc += fs->dcnt[w][g];
         tdh += fs->dhash[w][g];
       }
-      if (cnt.record) { cnt.rec_dir_cnt[slot] = tdc; cnt.rec_dir_hash[slot] = tdh; }
+      if (cnt.record) { atomicAdd(&cnt.rec_dir_cnt[slot], tdc); atomicAdd(&cnt.rec_dir_hash[slot], tdh); }
       const double rho = p.rho[slot];
       const double invrho = 1.0 / rho;
       const double divv = tot[8] * invrho;
