@@ -1448,17 +1448,27 @@ constexpr int kKdkPasses = 3;   // the first force pass and up to two CheckTimes
 
 int kdk_step_body(gsph_ctx* c) {
   const KdkState s = make_kdk_state(c);
+  const KdkLeaf l = make_kdk_leaf(c);
   launch_kdk_begin(c->kg, c->stream);
   launch_kdk_advance(s, c->kp, c->kg, c->stream);
   c->launches += 2;
   int rc = do_build(c);
   if (rc) return rc;
   for (int pass = 0; pass < kKdkPasses; pass++) {
-    rc = kdk_pass(c, true);
+    // the tree is the same for all passes of a step: the first gathers every persistent
+    // field into leaf order, the later ones only refresh the active flags and levels
+    if (pass == 0) launch_kdk_gather(s, l, c->kg, c->stream);
+    else launch_kdk_refresh(s, l, c->kg, c->stream);
+    c->launches += 1;
+    rc = do_props(c);
+    if (!rc) rc = do_forces(c, c->cfg.self_gravity != 0);
     if (rc) return rc;
+    launch_kdk_scatter_lvn(s, l, c->stream);
     launch_kdk_check(s, c->kp, c->kg, pass == kKdkPasses - 1, c->stream);
-    c->launches += pass == kKdkPasses - 1 ? 3 : 2;
+    c->launches += pass == kKdkPasses - 1 ? 4 : 3;
   }
+  launch_kdk_scatter_fields(s, l, c->stream);
+  c->launches += 1;
   launch_kdk_timesteps(s, c->kp, c->kg, c->stream);
   launch_kdk_end(s, c->kp, c->kg, c->stream);
   c->launches += 5;

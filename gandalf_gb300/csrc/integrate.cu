@@ -112,6 +112,42 @@ __global__ void k_kdk_scatter(KdkState s, KdkLeaf l) {
   }
 }
 
+// Later passes of a step reuse the leaf-order fields in place: only the active flags, levels
+// and the levelneib accumulators are refreshed.
+__global__ void k_kdk_refresh(KdkState s, KdkLeaf l, KdkGlobal* g) {
+  unsigned long long act = 0;
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
+    const int i = l.id[slot];
+    const unsigned char a = s.flags[i] & kFlagActive;
+    l.active[slot] = a;
+    l.level[slot] = s.level[i];
+    l.lvn[slot] = 0;
+    act += a;
+  }
+  for (int o = 16; o > 0; o >>= 1) act += __shfl_xor_sync(0xffffffffu, act, o);
+  if ((threadIdx.x & 31) == 0 && act) atomicAdd(&g->active_updates, act);
+}
+
+// levelneib only (what CheckTimesteps reads between passes).
+__global__ void k_kdk_scatter_lvn(KdkState s, KdkLeaf l) {
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
+    const int i = l.id[slot];
+    const int base = l.active[slot] ? 0 : s.levelneib[i];
+    s.levelneib[i] = max(base, l.lvn[slot]);
+  }
+}
+
+// Solved fields back to input order, once per step after the last pass.
+__global__ void k_kdk_scatter_fields(KdkState s, KdkLeaf l) {
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
+    const int i = l.id[slot];
+#pragma unroll
+    for (int q = 0; q < kKeep; q++) s.keep[q][i] = l.f[q][slot];
+    s.h[i] = l.h[slot];
+    s.u[i] = l.u[slot];
+  }
+}
+
 __global__ void k_kdk_check_reset(KdkGlobal* g) {
   if (threadIdx.x | blockIdx.x) return;
   g->activecount = 0;
@@ -383,6 +419,18 @@ void launch_kdk_advance(const KdkState& s, const KdkParams& kp, KdkGlobal* g, cu
 
 void launch_kdk_gather(const KdkState& s, const KdkLeaf& l, KdkGlobal* g, cudaStream_t st) {
   k_kdk_gather<<<grid_for(l.n), 256, 0, st>>>(s, l, g);
+}
+
+void launch_kdk_refresh(const KdkState& s, const KdkLeaf& l, KdkGlobal* g, cudaStream_t st) {
+  k_kdk_refresh<<<grid_for(l.n), 256, 0, st>>>(s, l, g);
+}
+
+void launch_kdk_scatter_lvn(const KdkState& s, const KdkLeaf& l, cudaStream_t st) {
+  k_kdk_scatter_lvn<<<grid_for(l.n), 256, 0, st>>>(s, l);
+}
+
+void launch_kdk_scatter_fields(const KdkState& s, const KdkLeaf& l, cudaStream_t st) {
+  k_kdk_scatter_fields<<<grid_for(l.n), 256, 0, st>>>(s, l);
 }
 
 void launch_kdk_scatter(const KdkState& s, const KdkLeaf& l, cudaStream_t st) {

@@ -64,6 +64,9 @@ void launch_kdk_begin(KdkGlobal* g, cudaStream_t st);
 void launch_kdk_advance(const KdkState& s, const KdkParams& kp, KdkGlobal* g, cudaStream_t st);
 void launch_kdk_gather(const KdkState& s, const KdkLeaf& l, KdkGlobal* g, cudaStream_t st);
 void launch_kdk_scatter(const KdkState& s, const KdkLeaf& l, cudaStream_t st);
+void launch_kdk_refresh(const KdkState& s, const KdkLeaf& l, KdkGlobal* g, cudaStream_t st);
+void launch_kdk_scatter_lvn(const KdkState& s, const KdkLeaf& l, cudaStream_t st);
+void launch_kdk_scatter_fields(const KdkState& s, const KdkLeaf& l, cudaStream_t st);
 void launch_kdk_check(const KdkState& s, const KdkParams& kp, KdkGlobal* g, bool last_pass, cudaStream_t st);
 void launch_kdk_timesteps(const KdkState& s, const KdkParams& kp, KdkGlobal* g, cudaStream_t st);
 void launch_kdk_end(const KdkState& s, const KdkParams& kp, KdkGlobal* g, cudaStream_t st);
