@@ -488,7 +488,7 @@ int read_status(gsph_ctx* c) {
   GSPH_CUDA(cudaStreamSynchronize(c->stream));
   c->last.status = (uint32_t) h[0];
   c->last.launches = c->launches;
-  if (mixed(c)) {
+  {
     int hc[2] = {0, 0};
     GSPH_CUDA(cudaMemcpy(hc, c->heavy_count + 2, sizeof(hc), cudaMemcpyDeviceToHost));
     c->last.heavy_density = hc[0];
@@ -545,12 +545,13 @@ int do_props(gsph_ctx* c) {
                                                    make_params(c), make_counters(c), heavy, c->lpg, c->max_leaf,
                                                    c->stream);
   } else {
-    launch_density(t, p, make_params(c), make_counters(c), c->lpg, c->stream);
-    c->launches += 1;
+    GSPH_CUDA(cudaMemsetAsync(c->heavy_count + 2, 0, 2 * sizeof(int), c->stream));
+    launch_density(t, p, make_params(c), make_counters(c), heavy, c->lpg, c->stream);
+    c->launches += 2;
   }
   int rc = check_launch(c, "density");
   if (rc) return rc;
-  if (mixed(c)) GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+  GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
   mark(c, 2);
   launch_update_hmax(t, p, c->stream);
   c->launches += 1;

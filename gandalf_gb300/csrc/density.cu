@@ -17,6 +17,7 @@
 #include "gsph_state.cuh"
 #include "gsph_walk.cuh"
 #include "kernels.cuh"
+#include "mixed_state.cuh"
 #include "stars.cuh"
 
 namespace gsph {
@@ -42,9 +43,31 @@ __device__ __forceinline__ double group_sum(double v) {
   return v;
 }
 
+// Final per-particle results of ComputeH (GradhSph.cpp:262-317).
+__device__ __forceinline__ void write_density(const Particles& p, const SphParams& prm, int slot, double hfin,
+                                              double rho_out, double om_out, double zeta_out, double xi, double yi,
+                                              double zi) {
+  const double invh = 1.0 / hfin;
+  p.h[slot] = hfin;
+  p.rho[slot] = rho_out;
+  p.hfactor[slot] = invh * invh * invh * invh;
+  p.hrangesqd[slot] = __dmul_rn(__dmul_rn(kKernRangeSqd, hfin), hfin);
+  p.div_v[slot] = 0.0;
+  const double drho = -(1.0 / 3.0) * hfin / rho_out;   // h_rho_deriv, src/Headers/Sph.h:264-268
+  const double io = 1.0 / (1.0 - drho * om_out);
+  p.invomega[slot] = io;
+  const double zsum = prm.stars.n ? zeta_out + star_zeta_sum(prm.stars, xi, yi, zi, hfin) : zeta_out;
+  p.zeta[slot] = drho * zsum * io;
+  double u = p.u[slot];
+  const double gm1 = prm.gamma_eos - 1.0;
+  if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
+  p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
+  p.pressure[slot] = gm1 * rho_out * u;
+}
+
 template <int LPG>
 __global__ void __launch_bounds__(kDensWarps * 32)
-k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
+k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList heavy) {
   __shared__ int s_stack[kDensWarps][kDensStack];
   __shared__ int s_list[kDensWarps][kDensList];
   const int wib = threadIdx.x >> 5;
@@ -75,6 +98,7 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
   // the largest h the reference's "h > hmax" test has seen.  (probe == true stops
   // after the fixed-point phase.)
   double mcheck = 0.0;
+  bool gave_up = false;   // gather list too long for one warp: the leaf goes to the heavy kernel
   auto attempt = [&](double hmax_list, bool probe) -> bool {
     const double hr = __dmul_rn(kKernRange, hmax_list);
     double gmin[3], gmax[3];
@@ -111,6 +135,7 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
           }
     };
     walk_all([&]() { overflow = true; });
+    if (overflow && heavy.leaves) { gave_up = true; return false; }
     const int ncached = L.na;
 
     double hi = h_start, h_lower = 0.0, h_upper = hmax_list;
@@ -216,11 +241,19 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
   double hk = __dmul_rn(1.05, hmax);
   for (int a = 0; a < kMaxAttempts && !solved; a++) {
     if (!attempt(hk, false)) {
+      if (gave_up) break;
       solved = true;
     } else {
       int guard = 0;
       do { hk = __dmul_rn(1.05, hk); } while (hk < mcheck && ++guard < 100000);
     }
+  }
+  if (gave_up) {   // nothing written; the heavy kernel solves the leaf from the start
+    if (lane == 0) {
+      const int k = atomicAdd(heavy.count, 1);
+      heavy.leaves[k] = leaf;
+    }
+    return;
   }
   if (!stack_ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
   if (__any_sync(kFull, fail) && lane == 0) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
@@ -230,39 +263,213 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
     for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
     if (lane == 0) atomicAdd(cnt.density_pairs, tot);
   }
-  if (mine && sl == 0) {
-    const double hfin = h_out;
-    const double invh = 1.0 / hfin;
-    p.h[slot] = hfin;
-    p.rho[slot] = rho_out;
-    p.hfactor[slot] = invh * invh * invh * invh;
-    p.hrangesqd[slot] = __dmul_rn(__dmul_rn(kKernRangeSqd, hfin), hfin);
-    p.div_v[slot] = 0.0;
-    const double drho = -(1.0 / 3.0) * hfin / rho_out;   // h_rho_deriv, src/Headers/Sph.h:264-268
-    const double io = 1.0 / (1.0 - drho * om_out);
-    p.invomega[slot] = io;
-    const double zsum = prm.stars.n ? zeta_out + star_zeta_sum(prm.stars, xi, yi, zi, hfin) : zeta_out;
-    p.zeta[slot] = drho * zsum * io;
-    double u = p.u[slot];
-    const double gm1 = prm.gamma_eos - 1.0;
-    if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
-    p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
-    p.pressure[slot] = gm1 * rho_out * u;
+  if (mine && sl == 0) write_density(p, prm, slot, h_out, rho_out, om_out, zeta_out, xi, yi, zi);
+}
+
+
+// ---- heavy leaves ----------------------------------------------------------------------
+// One block per leaf, one warp per particle; each h iteration walks the tree for the
+// particle's own box r +- 2h (a superset: the exact FP64 test below decides every pair),
+// instead of scanning the leaf's whole gather list.  Every pair inside the kernel support
+// of the current h lies inside the leaf's gather box while h stays below hmax_list, so the
+// sums take the same pairs as the warp-per-leaf form; the cell-level attempt protocol is
+// kept across the block.
+constexpr int kPPStack = 1024;
+constexpr int kPPList = 256;
+
+struct PPShared64 {
+  int stack[8][kPPStack];
+  int list[8][kPPList];
+  double h0[32];
+  double mloc[8];
+};
+
+template <int LPG>
+__device__ __forceinline__ void density_pp_leaf_fp64(const Tree& t, const Particles& p, const SphParams& prm,
+                                                     const DeviceCounters& cnt, int leaf, PPShared64& sm) {
+  constexpr int G = 32 / LPG;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* stack = sm.stack[wib];
+  int* list = sm.list[wib];
+  unsigned long long pairs = 0;
+  bool stack_ok = true, fail = false;
+  const int c = t.leaf_cell[leaf];
+  const int first = t.cell_first[c], ncell = t.cell_n[c];
+  __syncthreads();
+  if (threadIdx.x < ncell) sm.h0[threadIdx.x] = p.h[first + threadIdx.x];
+  __syncthreads();
+  double hk = __dmul_rn(1.05, t.geom[c].hmax);
+  bool solved = false;
+  for (int att = 0; att < kMaxAttempts && !solved; att++) {
+    double mloc = 0.0;
+    bool abort_any = false;
+    for (int g = wib; g < ncell; g += 8) {
+      const int slot = first + g;
+      if (!is_active(p, slot)) continue;
+      const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
+      double hi = sm.h0[g], h_lower = 0.0, h_upper = hk;
+      double rho = 0.0, om = 0.0, zeta = 0.0;
+      bool done = false, abort_cell = false;
+      int iteration = 0;
+      while (!done) {
+        iteration++;
+        const double invh = 1.0 / hi;
+        const double invhsqd = invh * invh;
+        double srho = 0.0, som = 0.0, sze = 0.0;
+        const double rr = __dmul_rn(kKernRange * (1.0 + 1.0 / 1024.0), hi);
+        const double gmin[3] = {xi - rr, yi - rr, zi - rr}, gmax[3] = {xi + rr, yi + rr, zi + rr};
+        int nsh[3] = {1, 1, 1}, sh[3][3];
+        for (int q = 0; q < 3; q++) {
+          sh[q][0] = 1;
+          if (prm.periodic) {
+            if (gmax[q] > prm.boxmax[q]) sh[q][nsh[q]++] = 2;
+            if (gmin[q] < prm.boxmin[q]) sh[q][nsh[q]++] = 0;
+          }
+        }
+        WarpLists L{list, list, list, 0, 0, 0, kPPList};
+        auto consume = [&]() {
+          for (int e0 = 0; e0 < L.na; e0 += LPG) {
+            const int e = e0 + lane / G, q = lane % G;
+            if (e >= L.na) continue;
+            const int tagv = list[e];
+            const int node = tagv & ((1 << kNodeBits) - 1);
+            const int code = tagv >> kNodeBits;
+            if (q >= t.cell_n[node]) continue;
+            const int j = t.cell_first[node] + q;
+            double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+            if (code != kNoShift) {
+              const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+              const double lim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+              bool ok = true;
+              if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], lim));
+              if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], lim));
+              if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], lim));
+              if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], lim));
+              if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], lim));
+              if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], lim));
+              if (!ok) continue;
+              xj = __dadd_rn(xj, sx); yj = __dadd_rn(yj, sy); zj = __dadd_rn(zj, sz);
+            }
+            const double dx = xj - xi, dy = yj - yi, dz = zj - zi;
+            const double ssqd = invhsqd * dot3_rn(dx, dy, dz);
+            if (ssqd < kKernRangeSqd) {
+              const double sv = sqrt(ssqd);
+              const double mj = p.m[j];
+              srho = fma(mj, m4_w0(sv), srho);
+              som = fma(mj * invh, m4_womega(sv), som);
+              sze = fma(mj, m4_wzeta(sv), sze);
+              pairs++;
+            }
+          }
+          __syncwarp();
+        };
+        for (int a0 = 0; a0 < nsh[0]; a0++)
+          for (int a1 = 0; a1 < nsh[1]; a1++)
+            for (int a2 = 0; a2 < nsh[2]; a2++) {
+              const int code = sh[0][a0] + 3 * sh[1][a1] + 9 * sh[2][a2];
+              double bmin[3], bmax[3];
+              for (int q = 0; q < 3; q++) {
+                const double sft = shift_of(code, q, prm);
+                bmin[q] = gmin[q] - sft;
+                bmax[q] = gmax[q] - sft;
+              }
+              auto decide = [&](int node, int level) -> int {
+                if (t.cell_n[node] == 0) return kSkip;
+                const CellBox ob = t.bb[node];
+                if (!box_overlap(bmin, bmax, ob.bbmin, ob.bbmax)) return kSkip;
+                return level == t.ltot ? kEmitA : kOpen;
+              };
+              auto tag = [&](int node, int) { return node | (code << kNodeBits); };
+              stack_ok = warp_walk(0, t.ltot, t.cell_level, stack, kPPStack, L, decide, tag, consume) && stack_ok;
+              consume();
+              L.na = 0;
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+          srho += __shfl_xor_sync(kFull, srho, o);
+          som += __shfl_xor_sync(kFull, som, o);
+          sze += __shfl_xor_sync(kFull, sze, o);
+        }
+        // GradhSph::ComputeH iteration (as the warp-per-leaf kernel)
+        const double hfac3 = invh * invh * invh;
+        rho = srho * hfac3;
+        om = som * hfac3;
+        zeta = sze * invhsqd;
+        const double hrho = prm.h_fac * pow(mi / rho, 1.0 / 3.0);
+        if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
+          done = true;
+        } else {
+          if (iteration < 30) hi = hrho;
+          else if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
+          else if (iteration < 150) {
+            if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
+            hi = 0.5 * (h_lower + h_upper);
+          } else {
+            fail = true;
+            done = true;
+          }
+          if (!done) {
+            mloc = fmax(mloc, hi);
+            if (hi > hk) { abort_cell = true; done = true; }
+            else if (!(hi > h_lower && hi < h_upper)) done = true;
+          }
+        }
+        if (!stack_ok) done = true;
+      }
+      abort_any = abort_any || abort_cell;
+      if (!abort_cell && lane == 0) {
+        const double hfin = fmax(prm.h_fac * pow(mi / rho, 1.0 / 3.0), h_lower);
+        write_density(p, prm, slot, hfin, rho, om, zeta, xi, yi, zi);
+      }
+    }
+    if (lane == 0) sm.mloc[wib] = mloc;
+    abort_any = __syncthreads_or(abort_any);
+    if (!abort_any) { solved = true; break; }
+    double mc = 0.0;
+    for (int w = 0; w < 8; w++) mc = fmax(mc, sm.mloc[w]);
+    __syncthreads();
+    int guard = 0;
+    do { hk = __dmul_rn(1.05, hk); } while (hk < mc && ++guard < 100000);
   }
+  unsigned long long tot = pairs;
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
+  if (lane == 0) {
+    if (tot) atomicAdd(cnt.density_pairs, tot);
+    if (!stack_ok) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
+    if (fail) atomicOr(cnt.status, (unsigned) kStatusHNotConverged);
+    if (!solved && wib == 0) atomicOr(cnt.status, (unsigned) kStatusRetryLimit);
+  }
+}
+
+template <int LPG>
+__global__ void __launch_bounds__(256, 2) k_density_fp64_pp(Tree t, Particles p, SphParams prm, DeviceCounters cnt,
+                                                            HeavyList heavy) {
+  __shared__ PPShared64 sm;
+  const int nh = *heavy.count;
+  for (int k = blockIdx.x; k < nh; k += gridDim.x) density_pp_leaf_fp64<LPG>(t, p, prm, cnt, heavy.leaves[k], sm);
 }
 
 }  // namespace
 
 void launch_density(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
-                    int lanes_per_particle, cudaStream_t st) {
+                    const HeavyList& heavy, int lanes_per_particle, cudaStream_t st) {
+  cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
   const int blocks = (t.nleaf + kDensWarps - 1) / kDensWarps;
   switch (lanes_per_particle) {
-    case 32: k_density_fp64<32><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
-    case 16: k_density_fp64<16><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
-    case 8: k_density_fp64<8><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
-    case 4: k_density_fp64<4><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
-    case 2: k_density_fp64<2><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
-    default: k_density_fp64<1><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt); break;
+    case 32: k_density_fp64<32><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 16: k_density_fp64<16><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 8: k_density_fp64<8><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 4: k_density_fp64<4><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 2: k_density_fp64<2><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
+    default: k_density_fp64<1><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
+  }
+  const int gpp = 2 * 152;
+  switch (lanes_per_particle) {
+    case 32: k_density_fp64_pp<32><<<gpp, 256, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 16: k_density_fp64_pp<16><<<gpp, 256, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 8: k_density_fp64_pp<8><<<gpp, 256, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 4: k_density_fp64_pp<4><<<gpp, 256, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 2: k_density_fp64_pp<2><<<gpp, 256, 0, st>>>(t, p, prm, cnt, heavy); break;
+    default: k_density_fp64_pp<1><<<gpp, 256, 0, st>>>(t, p, prm, cnt, heavy); break;
   }
 }
 

@@ -44,8 +44,10 @@ int launch_all_forces_mixed(const Tree& t, const Particles& p, const MixedPartic
 int launch_hydro_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
                        const SphParams& prm, const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st);
 
+// FP64 h solve; leaves whose gather list does not fit one warp go to a heavy-leaf kernel
+// through `heavy` (count zeroed here).  Returns nothing; launches two kernels.
 void launch_density(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
-                    int lanes_per_particle, cudaStream_t st);
+                    const HeavyList& heavy, int lanes_per_particle, cudaStream_t st);
 void launch_hydro_forces(const Tree& t, const Particles& p, const SphParams& prm,
                          const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st);
 void launch_all_forces(const Tree& t, const Particles& p, const SphParams& prm,
