@@ -65,6 +65,8 @@ struct gsph_ctx {
   unsigned long long* key[3] = {};
   int* idx[3] = {};
   int* listb[3] = {};
+  unsigned long long* key2[3] = {};
+  int *radix_hist = nullptr, *radix_tot = nullptr;
   unsigned char *side = nullptr, *seg_axis = nullptr;
   int* blocksum = nullptr;
   unsigned long long* rootkey = nullptr;
@@ -245,6 +247,9 @@ int ensure_capacity(gsph_ctx* c, int n) {
     for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->key[q], capP);
     for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->idx[q], capP);
     for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->listb[q], capn);
+    for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->key2[q], capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->radix_hist, (size_t) 3 * 256 * radix_tiles(capn));
+    if (rc == GSPH_OK) rc = alloc(c, c->radix_tot, 3 * 256);
     if (rc == GSPH_OK) rc = alloc(c, c->side, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->seg_axis, (capc + 1) / 2);
     if (rc == GSPH_OK) rc = alloc(c, c->blocksum, 3 * (size_t) partition_blocks(capn) + 3);
@@ -517,7 +522,11 @@ int do_build(gsph_ctx* c) {
   BuildArgs a{};
   a.n = c->n; a.ltot = c->ltot; a.P = c->P;
   a.in = InputArrays{c->in[0], c->in[1], c->in[2], c->in[3], c->in[4], c->in[5], c->in[6], c->in[7], c->in[8]};
-  for (int q = 0; q < 3; q++) { a.sort.key[q] = c->key[q]; a.sort.idx[q] = c->idx[q]; a.lists_b[q] = c->listb[q]; }
+  for (int q = 0; q < 3; q++) {
+    a.sort.key[q] = c->key[q]; a.sort.idx[q] = c->idx[q]; a.lists_b[q] = c->listb[q]; a.key2[q] = c->key2[q];
+  }
+  a.radix_hist = c->radix_hist;
+  a.radix_tot = c->radix_tot;
   a.side = c->side; a.seg_axis = c->seg_axis; a.blocksum = c->blocksum; a.rootkey = c->rootkey; a.ibox = c->ibox;
   a.heap_first = c->heap_first; a.heap_n = c->heap_n; a.heap_ones_before = c->heap_ones;
   a.p = make_particles(c);

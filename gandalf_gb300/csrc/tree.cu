@@ -117,6 +117,116 @@ __global__ void k_bitonic_global(SortArrays s, int P, int k, int j) {
   }
 }
 
+
+// ---- LSD radix sort of the (key, index) lists ------------------------------------------
+// Eight passes of 8-bit digits; each pass is stable, so equal keys keep ascending index
+// order and the result is the order of (key, index), as the bitonic network gives.  The
+// three axes are sorted together (blockIdx.y).  Per pass: per-tile digit histograms,
+// per-digit prefix over tiles, and a stable scatter in which each tile ranks its elements
+// round by round (256 consecutive elements per round: warp match for the rank inside a
+// warp, per-warp digit counts in shared memory for the rank across warps).
+constexpr int kRadixTile = 4096;           // elements per tile (256 threads x 16 rounds)
+constexpr int kRadixRounds = kRadixTile / 256;
+
+// Axis selection with constant indices, so the argument arrays stay in parameter space.
+template <class T>
+__device__ __forceinline__ T pick3(const T (&v)[3], int a) { return a == 0 ? v[0] : (a == 1 ? v[1] : v[2]); }
+
+__global__ void __launch_bounds__(256) k_radix_hist(RadixArgs r, int shift) {
+  __shared__ unsigned cnt[256];
+  const int a = blockIdx.y, b = blockIdx.x;
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const unsigned long long* key = pick3(r.src_key, a);
+  const int base = b * kRadixTile;
+  for (int q = 0; q < kRadixRounds; q++) {
+    const int i = base + q * 256 + threadIdx.x;
+    if (i < r.n) atomicAdd(&cnt[(unsigned) (key[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  r.hist[((size_t) a * 256 + threadIdx.x) * r.ntiles + b] = (int) cnt[threadIdx.x];
+}
+
+// Exclusive prefix over the tiles of one digit; the digit's total goes to tot.
+__global__ void __launch_bounds__(1024) k_radix_scan(RadixArgs r) {
+  __shared__ int part[1024];
+  const int a = blockIdx.y, d = blockIdx.x;
+  int* h = r.hist + ((size_t) a * 256 + d) * r.ntiles;
+  int carry = 0;
+  for (int c0 = 0; c0 < r.ntiles; c0 += 1024) {
+    const int i = c0 + threadIdx.x;
+    const int v = i < r.ntiles ? h[i] : 0;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const int add = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+      __syncthreads();
+      part[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (i < r.ntiles) h[i] = carry + part[threadIdx.x] - v;
+    carry += part[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) r.tot[a * 256 + d] = carry;
+}
+
+__global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
+  __shared__ int dbase[256];           // digit start in the output for this tile
+  __shared__ int wcnt[8][256];         // per-warp digit counts of the current round
+  __shared__ int run[256];             // elements of each digit already placed by this tile
+  const int a = blockIdx.y, b = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  {
+    // exclusive scan of the digit totals (256 values) + this tile's offset within the digit
+    __shared__ int tsum[256];
+    tsum[tid] = r.tot[a * 256 + tid];
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+      const int add = tid >= o ? tsum[tid - o] : 0;
+      __syncthreads();
+      tsum[tid] += add;
+      __syncthreads();
+    }
+    dbase[tid] = tsum[tid] - r.tot[a * 256 + tid] + r.hist[((size_t) a * 256 + tid) * r.ntiles + b];
+    run[tid] = 0;
+  }
+  const unsigned long long* key = pick3(r.src_key, a);
+  const int* idx = pick3(r.src_idx, a);
+  unsigned long long* okey = pick3(r.dst_key, a);
+  int* oidx = pick3(r.dst_idx, a);
+  const unsigned lt = (1u << lane) - 1u;
+  const int base = b * kRadixTile;
+  for (int q = 0; q < kRadixRounds; q++) {
+    for (int d = tid; d < 8 * 256; d += 256) (&wcnt[0][0])[d] = 0;
+    __syncthreads();
+    const int i = base + q * 256 + tid;
+    const bool valid = i < r.n;
+    unsigned long long k = 0;
+    int id = 0;
+    unsigned dig = 256u + (unsigned) lane;   // distinct dummy digits for invalid lanes
+    if (valid) { k = key[i]; id = idx[i]; dig = (unsigned) (k >> shift) & 255u; }
+    const unsigned peers = __match_any_sync(kFull, dig);
+    const int rank = __popc(peers & lt);
+    if (valid && rank == 0) wcnt[w][dig] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      int before = run[dig];
+      for (int v = 0; v < w; v++) before += wcnt[v][dig];
+      const int pos = dbase[dig] + before + rank;
+      okey[pos] = k;
+      oidx[pos] = id;
+    }
+    __syncthreads();
+    {
+      int add = 0;
+      for (int v = 0; v < 8; v++) add += wcnt[v][tid];
+      run[tid] += add;
+    }
+    __syncthreads();
+  }
+}
+
 // Segment containing position j on level l (recursive halving of [0, n)).
 __device__ __forceinline__ int seg_of(int j, int n, int l, int& first, int& cnt) {
   int s = 0, f = 0, c = n;
@@ -490,6 +600,8 @@ int sort_padded_size(int n) {
 
 int partition_blocks(int n) { return (n + kScanBlock - 1) / kScanBlock; }
 
+int radix_tiles(int n) { return (n + kRadixTile - 1) / kRadixTile; }
+
 int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
   int launches = 0;
   const int n = a.n;
@@ -497,17 +609,30 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
   k_root_box<<<grid_for(n, 256, 152 * 4), 256, 0, st>>>(a.in.x, a.in.y, a.in.z, a.in.h, n, a.rootkey);
   k_root_box_store<<<1, 32, 0, st>>>(a.rootkey, a.ibox);
   launches += 3;
-  const int P = a.P;
-  k_sort_init<<<dim3(grid_for(P, 256), 3), 256, 0, st>>>(a.in.x, a.in.y, a.in.z, n, P, a.sort);
-  k_bitonic_smem<<<dim3(P / kSortBlock, 3), kSortBlock / 2, 0, st>>>(a.sort, 2, kSortBlock, kSortBlock / 2);
-  launches += 2;
-  for (int k = 2 * kSortBlock; k <= P; k <<= 1) {
-    for (int j = k >> 1; j >= kSortBlock; j >>= 1) {
-      k_bitonic_global<<<dim3(grid_for(P / 2, 256, 1 << 20), 3), 256, 0, st>>>(a.sort, P, k, j);
-      launches++;
+  k_sort_init<<<dim3(grid_for(n, 256), 3), 256, 0, st>>>(a.in.x, a.in.y, a.in.z, n, n, a.sort);
+  launches += 1;
+  {
+    // radix passes ping-pong between the sort arrays and (key2, lists_b); eight passes
+    // end in the sort arrays
+    RadixArgs r{};
+    r.n = n;
+    r.ntiles = radix_tiles(n);
+    r.hist = a.radix_hist;
+    r.tot = a.radix_tot;
+    const dim3 grid(r.ntiles, 3);
+    for (int pass = 0; pass < 8; pass++) {
+      for (int q = 0; q < 3; q++) {
+        const bool even = (pass & 1) == 0;
+        r.src_key[q] = even ? a.sort.key[q] : a.key2[q];
+        r.src_idx[q] = even ? a.sort.idx[q] : a.lists_b[q];
+        r.dst_key[q] = even ? a.key2[q] : a.sort.key[q];
+        r.dst_idx[q] = even ? a.lists_b[q] : a.sort.idx[q];
+      }
+      k_radix_hist<<<grid, 256, 0, st>>>(r, 8 * pass);
+      k_radix_scan<<<dim3(256, 3), 1024, 0, st>>>(r);
+      k_radix_scatter<<<grid, 256, 0, st>>>(r, 8 * pass);
+      launches += 3;
     }
-    k_bitonic_smem<<<dim3(P / kSortBlock, 3), kSortBlock / 2, 0, st>>>(a.sort, k, k, kSortBlock / 2);
-    launches++;
   }
   BuildLists cur, nxt;
   for (int q = 0; q < 3; q++) { cur.l[q] = a.sort.idx[q]; nxt.l[q] = a.lists_b[q]; }

@@ -9,6 +9,17 @@ struct SortArrays {
   int* idx[3];                  // particle indices, padded length P
 };
 
+// One radix-sort pass over the three axes' (key, index) lists.
+struct RadixArgs {
+  int n, ntiles;
+  const unsigned long long* src_key[3];
+  const int* src_idx[3];
+  unsigned long long* dst_key[3];
+  int* dst_idx[3];
+  int* hist;                    // 3 x 256 x ntiles, digit-major
+  int* tot;                     // 3 x 256
+};
+
 struct BuildLists {
   int* l[3];                    // per-axis position lists of particle indices
 };
@@ -22,6 +33,9 @@ struct BuildArgs {
   InputArrays in;
   SortArrays sort;
   int* lists_b[3];              // second buffer of the ping-pong position lists (length n)
+  unsigned long long* key2[3];  // second key buffer of the radix sort (length n)
+  int* radix_hist;              // 3 x 256 x radix_tiles(n)
+  int* radix_tot;               // 3 x 256
   unsigned char* side;          // per particle: 0 first child, 1 second child
   unsigned char* seg_axis;      // per segment of the current level
   int* blocksum;                // 3 * partition_blocks(n)
@@ -38,6 +52,7 @@ struct BuildArgs {
 
 int sort_padded_size(int n);
 int partition_blocks(int n);
+int radix_tiles(int n);
 int launch_build_tree(const BuildArgs& a, cudaStream_t st);   // returns kernels launched
 void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st);
 
