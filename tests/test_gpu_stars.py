@@ -4,7 +4,7 @@ Gas <- stars: the stars' softened gravity in a, atree and gpot, gpot_hydro witho
 and the SPH-star zeta term of the h solve.  Star <- gas: a, adot and gpot of every star
 from the gas tree.  FP64 form: FP64_TOL and STAR_TOL of tests/parity.py.  Mixed form:
 its gas fields within MIXED_TOL; the star pass is FP64 arithmetic on the mixed form's
-smoothing lengths, within 1e-6.
+smoothing lengths (float h iteration, h within MIXED_TOL), within 1e-5.
 """
 import numpy as np
 import pytest
@@ -48,7 +48,7 @@ def test_stars_match_oracle(n, nstar):
     mo, ms = run(c, params, precision="mixed")
     check_mixed(mo, r["particles"])
     for k in ("ax", "ay", "az", "gpot"):
-        assert_close("mixed star " + k, ms[k], r["stars"][k], 1e-6)
+        assert_close("mixed star " + k, ms[k], r["stars"][k], 1e-5)
 
 
 def test_hydro_only_gas_feels_stars():
