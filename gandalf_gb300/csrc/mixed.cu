@@ -941,8 +941,9 @@ __device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Pa
   p.gpot[slot] = grav ? gpot0 + gp : 0.0;
 }
 
+constexpr int kForceWarps = 4;    // warps per block of the warp-per-leaf force kernels
 constexpr int kFStack = 1024;
-constexpr int kFListA = 256, kFListB = 128, kFListC = 1024;         // warp-per-leaf
+constexpr int kFListA = 256, kFListB = 128, kFListC = 512;         // warp-per-leaf
 constexpr int kWListA = 256, kWListB = 512, kWListC = 1024;         // wide kernel, per warp
 
 // One leaf (or one particle of a leaf) through the gravity walk and all its terms.
@@ -993,8 +994,9 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     z = (h.z - lc_hi.z) + (l.z - lc_lo.z);
   };
   // the warp's targets, broadcast from shared memory: leaf-relative position, w = 1 when active
-  __shared__ float4 s_tgt[8][32];
-  float4* tgt = s_tgt[(threadIdx.x >> 5) & 7];
+  constexpr int kTW = SLICES == 1 ? kForceWarps : 8;   // warps per block
+  __shared__ float4 s_tgt[kTW][GT];
+  float4* tgt = s_tgt[(threadIdx.x >> 5) % kTW];
   {
     float x, y, z;
     rel(T.ph, T.pl, x, y, z);
@@ -1242,8 +1244,6 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   __syncthreads();
   return true;
 }
-
-constexpr int kForceWarps = 4;
 
 template <int LPG>
 __global__ void __launch_bounds__(kForceWarps * 32)
