@@ -24,7 +24,7 @@ namespace gsph {
 
 namespace {
 
-constexpr int kDensWarps = 4;          // warps per block
+constexpr int kDensWarps = 1;          // warps per block (a block's slot frees when its leaf is done)
 constexpr int kDensStack = 1024;       // walk stack entries per warp
 constexpr int kDensList = 1024;        // gather-list entries per warp
 constexpr int kMaxAttempts = 256;      // attempts of the (skipping) hmax sequence
@@ -66,7 +66,7 @@ __device__ __forceinline__ void write_density(const Particles& p, const SphParam
 }
 
 template <int LPG>
-__global__ void __launch_bounds__(kDensWarps * 32)
+__global__ void __launch_bounds__(kDensWarps * 32, 16 / kDensWarps)
 k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList heavy) {
   __shared__ int s_stack[kDensWarps][kDensStack];
   __shared__ int s_list[kDensWarps][kDensList];

@@ -706,27 +706,27 @@ __host__ __device__ constexpr int compact_stride() {
                    : ((kCompactPerWarp / (32 / LPG) - LPG) / 16) * 16 + LPG;
 }
 
-size_t dens_smem_normal() {
-  return sizeof(float2) * kDensWarps * kCompactPerWarp + sizeof(int) * kDensWarps * (kDensStack + kDensListNormal);
+size_t dens_smem(int warps) {
+  return (sizeof(float2) * kCompactPerWarp + sizeof(int) * (kDensStack + kDensListNormal)) * warps;
 }
 
-// Shared memory limits the warp-per-leaf density kernel to 3 blocks per SM, so the
-// register budget is set for 3 (168 registers a thread).
+// One warp per block, one leaf per warp: a block's slot frees as soon as its leaf is
+// done (leaf costs vary by an order of magnitude, and warps of a larger block would wait
+// for the slowest).  Shared memory (17 KB a warp) and registers (168 a thread) allow 12
+// resident warps per SM.
 template <int LPG>
-__global__ void __launch_bounds__(kDensWarps * 32, 3)
+__global__ void __launch_bounds__(32, 12)
 k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
                 HeavyList heavy, bool handover) {
   extern __shared__ float2 s_dyn2[];
   float2* s_compact = s_dyn2;
-  int* s_stack = reinterpret_cast<int*>(s_dyn2 + kDensWarps * kCompactPerWarp);
-  int* s_list = s_stack + kDensWarps * kDensStack;
-  const int wib = threadIdx.x >> 5;
-  const int leaf = blockIdx.x * kDensWarps + wib;
+  int* s_stack = reinterpret_cast<int*>(s_dyn2 + kCompactPerWarp);
+  int* s_list = s_stack + kDensStack;
+  const int leaf = blockIdx.x;
   if (leaf >= t.nleaf) return;
   const int kcap = compact_stride<LPG>();
-  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack + wib * kDensStack,
-                                       s_list + wib * kDensListNormal, kDensListNormal,
-                                       s_compact + wib * kCompactPerWarp, kcap, handover, nullptr);
+  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack, s_list, kDensListNormal, s_compact,
+                                       kcap, handover, nullptr);
   if (!ok && (threadIdx.x & 31) == 0) {
     const int k = atomicAdd(heavy.count, 1);
     heavy.leaves[k] = leaf;
@@ -1550,14 +1550,9 @@ int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles
                          const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
                          int lanes_per_particle, int max_leaf, cudaStream_t st) {
   cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
-  const int blocks = (t.nleaf + kDensWarps - 1) / kDensWarps;
-  const size_t smem_n = dens_smem_normal();
-  for (auto f : {k_density_mixed<1>, k_density_mixed<2>, k_density_mixed<4>, k_density_mixed<8>,
-                 k_density_mixed<16>, k_density_mixed<32>})
-    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_n);
+  const size_t smem_n = dens_smem(1);
   (void) max_leaf;
-  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, blocks, kDensWarps * 32, smem_n, t, p, mp, mc, prm, cnt, heavy,
-                 true)
+  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, t.nleaf, 32, smem_n, t, p, mp, mc, prm, cnt, heavy, true)
   GSPH_MIXED_LPG(k_density_mixed_pp, lanes_per_particle, 2 * 152, 256, 0, t, p, mp, mc, prm, cnt, heavy)
   return 2;
 }
@@ -1586,7 +1581,7 @@ int launch_hydro_mixed(const Tree& t, const Particles& p, const MixedParticles& 
 
 int launch_batch_density(const BatchQueue& q, int lpg, cudaStream_t st) {
   cudaMemsetAsync(q.next, 0, 4 * sizeof(int), st);
-  const size_t smem_n = dens_smem_normal();
+  const size_t smem_n = dens_smem(kDensWarps);
   for (auto f : {k_batch_density<1>, k_batch_density<2>, k_batch_density<4>, k_batch_density<8>,
                  k_batch_density<16>, k_batch_density<32>})
     cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_n);
