@@ -374,14 +374,19 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     const float lim2 = (float) (kKernRangeSqd * hmax_list * hmax_list) * (1.0f + kMargin);
     if (!overflow) {
       const int ntgt = ncell < G ? ncell : G;
+      // positions relative to the leaf centre (hi + lo pairs): a few float ulps of the
+      // separation, three registers a target
+      const float4 lch = mc.geo_hi[c], lcl = mc.geo_lo[c];
       for (int gc = 0; gc < ntgt; gc += 8) {
-        float4 th[8], tl[8];
+        float tx[8], ty[8], tz[8];
         int tc[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
           const int tg = gc + u < ntgt ? gc + u : ntgt - 1;
-          th[u] = mp.pos_hi[first + tg];
-          tl[u] = mp.pos_lo[first + tg];
+          const float4 h = mp.pos_hi[first + tg], l = mp.pos_lo[first + tg];
+          tx[u] = (h.x - lch.x) + (l.x - lcl.x);
+          ty[u] = (h.y - lch.y) + (l.y - lcl.y);
+          tz[u] = (h.z - lch.z) + (l.z - lcl.z);
           tc[u] = 0;
         }
         for (int e0 = 0; e0 < ncached; e0 += LPG) {
@@ -394,12 +399,15 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
             const int code = tagv >> kNodeBits;
             if (q < t.cell_n[node]) valid = cand_pos(t.cell_first[node] + q, code, ch, cl);
           }
+          const float cx = (ch.x - lch.x) + (cl.x - lcl.x);
+          const float cy = (ch.y - lch.y) + (cl.y - lcl.y);
+          const float cz = (ch.z - lch.z) + (cl.z - lcl.z);
 #pragma unroll
           for (int u = 0; u < 8; u++) {
             if (gc + u >= ntgt) break;
-            const float dx = (ch.x - th[u].x) + (cl.x - tl[u].x);
-            const float dy = (ch.y - th[u].y) + (cl.y - tl[u].y);
-            const float dz = (ch.z - th[u].z) + (cl.z - tl[u].z);
+            const float dx = cx - tx[u];
+            const float dy = cy - ty[u];
+            const float dz = cz - tz[u];
             const float d2 = dx * dx + dy * dy + dz * dz;
             const bool keep = valid && d2 <= lim2;
             const unsigned b = __ballot_sync(kFull, keep);
