@@ -8,9 +8,10 @@
 //   * cells are stocked bottom-up; cdistsqd = max(rmax^2, hmax^2) / theta^2 (:807-1083)
 //
 // GB300 design: the recursion becomes ltot level-synchronous passes over position lists.
-// Each particle's index is presorted once per axis (bitonic sort on (coordinate, index)),
-// so every segment's median along its split axis sits at position first + n/2 of that
-// axis list.  A pass then marks each particle's side and stable-partitions all three lists
+// Each particle's index is presorted once per axis on (coordinate key, index) — an LSD
+// radix sort in the allocating build, a bitonic network in the allocation-free one (its
+// scratch has no room for the radix sort's second buffers) — so every segment's median
+// along its split axis sits at position first + n/2 of that axis list.  A pass then marks each particle's side and stable-partitions all three lists
 // with one global scan, which keeps each child's lists sorted.  Particles are never moved
 // until the final gather into leaf order.  Stocking is one launch: each leaf thread stocks
 // its leaf and climbs while it is the second child to arrive at a parent.
