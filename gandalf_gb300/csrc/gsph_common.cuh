@@ -146,6 +146,24 @@ __device__ __forceinline__ float m4f_wpot(float s) {
            (1.0f / 30.0f) * s2 * s2 * s;
   return 1.0f / s;
 }
+// The same two functions with 1/s supplied by the caller (h / |r| from the pair's rsqrt),
+// so the pair loops carry no division.
+__device__ __forceinline__ float m4f_wgrav_r(float s, float inv_s) {
+  const float s2 = s * s;
+  if (s < 1.0f) return 1.3333333333f * s - 1.2f * s2 * s + 0.5f * s2 * s2;
+  const float inv_s2 = inv_s * inv_s;
+  if (s < 2.0f)
+    return 2.6666666667f * s - 3.0f * s2 + 1.2f * s2 * s - 0.1666666667f * s2 * s2 - 0.0666666667f * inv_s2;
+  return inv_s2;
+}
+__device__ __forceinline__ float m4f_wpot_r(float s, float inv_s) {
+  const float s2 = s * s;
+  if (s < 1.0f) return 1.4f - 0.6666666667f * s2 + 0.3f * s2 * s2 - 0.1f * s2 * s2 * s;
+  if (s < 2.0f)
+    return -(1.0f / 15.0f) * inv_s + 1.6f - 1.3333333333f * s2 + s2 * s - 0.3f * s2 * s2 +
+           (1.0f / 30.0f) * s2 * s2 * s;
+  return inv_s;
+}
 
 // ---- status words written by kernels (never trap) --------------------------------------
 enum StatusBits : unsigned {

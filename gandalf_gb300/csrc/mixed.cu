@@ -800,9 +800,9 @@ __device__ __forceinline__ float pair_pressure_f(const SphParams& prm, const Tar
 __device__ __forceinline__ void hydro_pair_f(const SphParams& prm, const MixedParticles& mp, const TargetF& T, int j,
                                              float dx, float dy, float dz, float d2, float mj, AccF& A) {
   const float4 vj = mp.vel[j], hj = mp.hyd[j], xj = mp.aux[j];
-  const float drmag = fsqrt_pos(d2);
-  float ux = dx, uy = dy, uz = dz;
-  if (drmag > 0.0f) { const float inv = 1.0f / drmag; ux *= inv; uy *= inv; uz *= inv; }
+  const float inv = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
+  const float drmag = d2 * inv;
+  const float ux = dx * inv, uy = dy * inv, uz = dz * inv;
   const float wi = T.aux.x * m4f_w1(drmag * T.hyd.x);
   const float wj = xj.x * m4f_w1(drmag * hj.x);
   const float dvdr = (vj.x - T.vel.x) * ux + (vj.y - T.vel.y) * uy + (vj.z - T.vel.z) * uz;
@@ -824,9 +824,12 @@ __device__ __forceinline__ void hydro_grav_pair_f(const SphParams& prm, const Mi
   const float wj = xj.x * m4f_w1(sj);
   const float paux = pair_pressure_f(prm, T, wi, wj, hj.y, hj.z, hj.w, mj, dvdr, A.dudt);
   A.ah[0] += mj * ux * paux; A.ah[1] += mj * uy * paux; A.ah[2] += mj * uz * paux;
-  const float pg = 0.5f * (T.hyd.x * T.hyd.x * m4f_wgrav(si) + T.aux.y * wi + hj.x * hj.x * m4f_wgrav(sj) + xj.y * wj);
+  // 1/s = h / |r|: the float h of each particle (vel.w) times the pair's rsqrt
+  const float isi = T.vel.w * invdrmag, isj = vj.w * invdrmag;
+  const float pg = 0.5f * (T.hyd.x * T.hyd.x * m4f_wgrav_r(si, isi) + T.aux.y * wi +
+                           hj.x * hj.x * m4f_wgrav_r(sj, isj) + xj.y * wj);
   A.ag[0] += mj * ux * pg; A.ag[1] += mj * uy * pg; A.ag[2] += mj * uz * pg;
-  A.gpot += 0.5f * mj * (T.hyd.x * m4f_wpot(si) + hj.x * m4f_wpot(sj));
+  A.gpot += 0.5f * mj * (T.hyd.x * m4f_wpot_r(si, isi) + hj.x * m4f_wpot_r(sj, isj));
   A.divv -= mj * dvdr * wi;
 }
 
