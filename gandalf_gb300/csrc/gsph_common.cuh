@@ -165,6 +165,42 @@ __device__ __forceinline__ float m4f_wpot_r(float s, float inv_s) {
   return inv_s;
 }
 
+// w0, womega and wzeta of one s together (the three sums of the h iteration), one branch.
+__device__ __forceinline__ void m4f_w0_omega_zeta(float s, float& w0, float& wom, float& wze) {
+  const float s2 = s * s;
+  if (s < 1.0f) {
+    w0 = (float) kInvPi * (1.0f - 1.5f * s2 + 0.75f * s2 * s);
+    wom = (float) kInvPi * (-3.0f + 7.5f * s2 - 4.5f * s2 * s);
+    wze = 1.4f - 2.0f * s2 + 1.5f * s2 * s2 - 0.6f * s2 * s2 * s;
+  } else {
+    const float t = 2.0f - s;
+    w0 = 0.25f * (float) kInvPi * (t * t * t);
+    wom = (float) kInvPi * (-6.0f + 12.0f * s - 7.5f * s2 + 1.5f * s2 * s);
+    wze = 1.6f - 4.0f * s2 + 4.0f * s2 * s - 1.5f * s2 * s2 + 0.2f * s2 * s2 * s;
+  }
+}
+
+// w1, wgrav and wpot of one s together (one branch on the kernel's piecewise range for
+// the three functions), with 1/s supplied by the caller.
+__device__ __forceinline__ void m4f_w1_grav_pot(float s, float inv_s, float& w1, float& wg, float& wp) {
+  const float s2 = s * s;
+  if (s < 1.0f) {
+    w1 = (float) kInvPi * (-3.0f * s + 2.25f * s2);
+    wg = 1.3333333333f * s - 1.2f * s2 * s + 0.5f * s2 * s2;
+    wp = 1.4f - 0.6666666667f * s2 + 0.3f * s2 * s2 - 0.1f * s2 * s2 * s;
+  } else if (s < 2.0f) {
+    const float inv_s2 = inv_s * inv_s;
+    w1 = -0.75f * (float) kInvPi * (2.0f - s) * (2.0f - s);
+    wg = 2.6666666667f * s - 3.0f * s2 + 1.2f * s2 * s - 0.1666666667f * s2 * s2 - 0.0666666667f * inv_s2;
+    wp = -(1.0f / 15.0f) * inv_s + 1.6f - 1.3333333333f * s2 + s2 * s - 0.3f * s2 * s2 +
+         (1.0f / 30.0f) * s2 * s2 * s;
+  } else {
+    w1 = 0.0f;
+    wg = inv_s * inv_s;
+    wp = inv_s;
+  }
+}
+
 // ---- status words written by kernels (never trap) --------------------------------------
 enum StatusBits : unsigned {
   kStatusStackOverflow = 1u << 0,   // walk stack exceeded its capacity

@@ -445,9 +445,11 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         const float ssqd = d2 * invhsqd_f;
         if (ssqd < 4.0f) {
           const float s = fsqrt_pos(ssqd);
-          srho = fmaf(mj, m4f_w0(s), srho);
-          som = fmaf(mj * invh_f, m4f_womega(s), som);
-          sze = fmaf(mj, m4f_wzeta(s), sze);
+          float w0, wom, wze;   // s < 2 here
+          m4f_w0_omega_zeta(s, w0, wom, wze);
+          srho = fmaf(mj, w0, srho);
+          som = fmaf(mj * invh_f, wom, som);
+          sze = fmaf(mj, wze, sze);
           pairs++;
         }
       };
@@ -632,9 +634,11 @@ __device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& 
             const float ssqd = (dx * dx + dy * dy + dz * dz) * invhsqd_f;
             if (ssqd < 4.0f) {
               const float sv = fsqrt_pos(ssqd);
-              srho = fmaf(mj, m4f_w0(sv), srho);
-              som = fmaf(mj * invh_f, m4f_womega(sv), som);
-              sze = fmaf(mj, m4f_wzeta(sv), sze);
+              float w0, wom, wze;   // sv < 2 here
+              m4f_w0_omega_zeta(sv, w0, wom, wze);
+              srho = fmaf(mj, w0, srho);
+              som = fmaf(mj * invh_f, wom, som);
+              sze = fmaf(mj, wze, sze);
               pairs++;
             }
           }
@@ -820,16 +824,17 @@ __device__ __forceinline__ void hydro_grav_pair_f(const SphParams& prm, const Mi
   const float ux = dx * invdrmag, uy = dy * invdrmag, uz = dz * invdrmag;
   const float dvdr = (vj.x - T.vel.x) * ux + (vj.y - T.vel.y) * uy + (vj.z - T.vel.z) * uz;
   const float si = drmag * T.hyd.x, sj = drmag * hj.x;
-  const float wi = T.aux.x * m4f_w1(si);
-  const float wj = xj.x * m4f_w1(sj);
+  // 1/s = h / |r|: the float h of each particle (vel.w) times the pair's rsqrt
+  float w1i, wgi, wpi, w1j, wgj, wpj;
+  m4f_w1_grav_pot(si, T.vel.w * invdrmag, w1i, wgi, wpi);
+  m4f_w1_grav_pot(sj, vj.w * invdrmag, w1j, wgj, wpj);
+  const float wi = T.aux.x * w1i;
+  const float wj = xj.x * w1j;
   const float paux = pair_pressure_f(prm, T, wi, wj, hj.y, hj.z, hj.w, mj, dvdr, A.dudt);
   A.ah[0] += mj * ux * paux; A.ah[1] += mj * uy * paux; A.ah[2] += mj * uz * paux;
-  // 1/s = h / |r|: the float h of each particle (vel.w) times the pair's rsqrt
-  const float isi = T.vel.w * invdrmag, isj = vj.w * invdrmag;
-  const float pg = 0.5f * (T.hyd.x * T.hyd.x * m4f_wgrav_r(si, isi) + T.aux.y * wi +
-                           hj.x * hj.x * m4f_wgrav_r(sj, isj) + xj.y * wj);
+  const float pg = 0.5f * (T.hyd.x * T.hyd.x * wgi + T.aux.y * wi + hj.x * hj.x * wgj + xj.y * wj);
   A.ag[0] += mj * ux * pg; A.ag[1] += mj * uy * pg; A.ag[2] += mj * uz * pg;
-  A.gpot += 0.5f * mj * (T.hyd.x * m4f_wpot_r(si, isi) + hj.x * m4f_wpot_r(sj, isj));
+  A.gpot += 0.5f * mj * (T.hyd.x * wpi + hj.x * wpj);
   A.divv -= mj * dvdr * wi;
 }
 
