@@ -88,7 +88,7 @@ struct gsph_ctx {
   float4 *mp_pos_hi = nullptr, *mp_pos_lo = nullptr, *mp_vel = nullptr, *mp_hyd = nullptr, *mp_aux = nullptr;
   float4 *mc_geo_hi = nullptr, *mc_geo_lo = nullptr, *mc_com_hi = nullptr, *mc_com_lo = nullptr, *mc_quad = nullptr,
          *mc_bbmin = nullptr, *mc_bbmax = nullptr, *mc_hbmin = nullptr, *mc_hbmax = nullptr;
-  float* mc_cdist = nullptr;
+  float4* mc_meta = nullptr;
   int* heavy_leaves = nullptr;
   int* heavy_count = nullptr;
   int max_leaf = 8;
@@ -263,7 +263,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
       float4** cf[9] = {&c->mc_geo_hi, &c->mc_geo_lo, &c->mc_com_hi, &c->mc_com_lo, &c->mc_quad,
                         &c->mc_bbmin, &c->mc_bbmax, &c->mc_hbmin, &c->mc_hbmax};
       for (int q = 0; q < 9 && rc == GSPH_OK; q++) rc = alloc(c, *cf[q], capc);
-      if (rc == GSPH_OK) rc = alloc(c, c->mc_cdist, capc);
+      if (rc == GSPH_OK) rc = alloc(c, c->mc_meta, capc);
     }
     if (rc == GSPH_OK) rc = alloc(c, c->heavy_leaves, (capc + 1) / 2);
     if (rc == GSPH_OK) rc = alloc(c, c->heavy_count, 4);
@@ -363,7 +363,7 @@ MixedParticles make_mixed_particles(gsph_ctx* c) {
 }
 
 MixedCells make_mixed_cells(gsph_ctx* c) {
-  return MixedCells{c->mc_geo_hi, c->mc_geo_lo, c->mc_cdist, c->mc_com_hi, c->mc_com_lo, c->mc_quad,
+  return MixedCells{c->mc_geo_hi, c->mc_geo_lo, c->mc_meta, c->mc_com_hi, c->mc_com_lo, c->mc_quad,
                     c->mc_bbmin, c->mc_bbmax, c->mc_hbmin, c->mc_hbmax};
 }
 

@@ -27,11 +27,11 @@ struct WarpLists {
 };
 
 // Returns false when the stack would overflow (status is then the caller's to set).
-// decide(node, level) -> WalkAction, called by active lanes only.
+// decide(node, int& level) -> WalkAction, called by active lanes only; it reports the
+// cell's level (callers whose cell records carry it save a load).
 // emit_tag(node, action) -> value stored in the list (lets callers pack extra bits).
 template <class Decide, class Tag, class Flush>
-__device__ __forceinline__ bool warp_walk(int root, int ltot, const unsigned char* __restrict__ cell_level,
-                                          int* stack, int stack_cap, WarpLists& L, Decide decide,
+__device__ __forceinline__ bool warp_walk_lv(int root, int ltot, int* stack, int stack_cap, WarpLists& L, Decide decide,
                                           Tag emit_tag, Flush flush) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -45,10 +45,7 @@ __device__ __forceinline__ bool warp_walk(int root, int ltot, const unsigned cha
     top -= take;
     __syncwarp();
     int act = kSkip, level = 0;
-    if (node >= 0) {
-      level = cell_level[node];
-      act = decide(node, level);
-    }
+    if (node >= 0) act = decide(node, level);
     const unsigned mo = __ballot_sync(kFull, act == kOpen);
     const int nopen = __popc(mo);
     if (top + 2 * nopen > stack_cap) return false;
@@ -79,6 +76,18 @@ __device__ __forceinline__ bool warp_walk(int root, int ltot, const unsigned cha
     }
   }
   return true;
+}
+
+// The same walk with the level read from cell_level; decide(node, level) -> WalkAction.
+template <class Decide, class Tag, class Flush>
+__device__ __forceinline__ bool warp_walk(int root, int ltot, const unsigned char* __restrict__ cell_level,
+                                          int* stack, int stack_cap, WarpLists& L, Decide decide,
+                                          Tag emit_tag, Flush flush) {
+  auto decide_lv = [&](int node, int& level) -> int {
+    level = cell_level[node];
+    return decide(node, level);
+  };
+  return warp_walk_lv(root, ltot, stack, stack_cap, L, decide_lv, emit_tag, flush);
 }
 
 __device__ __forceinline__ bool box_overlap(const double* amin, const double* amax, const double* bmin,

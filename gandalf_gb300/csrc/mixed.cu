@@ -55,16 +55,17 @@ __global__ void k_prep_build_cells(Tree t, MixedCells mc) {
     for (int k = 0; k < 3; k++) split2(g.rcell[k], h[k], l[k]);
     mc.geo_hi[c] = make_float4(h[0], h[1], h[2], __double2float_rn(g.rmax));
     mc.geo_lo[c] = make_float4(l[0], l[1], l[2], __double2float_rn(g.hmax));
-    mc.cdist[c] = __double2float_rn(g.cdistsqd);
+    mc.meta[c] = make_float4(__double2float_rn(g.cdistsqd), __int_as_float(t.cell_n[c]),
+                             __int_as_float((int) t.cell_level[c]), 0.0f);
     for (int k = 0; k < 3; k++) split2(m.r[k], h[k], l[k]);
     mc.com_hi[c] = make_float4(h[0], h[1], h[2], __double2float_rn(m.m));
     mc.com_lo[c] = make_float4(l[0], l[1], l[2], __double2float_rn(m.q[4]));
     mc.quad[c] = make_float4(__double2float_rn(m.q[0]), __double2float_rn(m.q[1]), __double2float_rn(m.q[2]),
                              __double2float_rn(m.q[3]));
     mc.bbmin[c] = make_float4(__double2float_rd(b.bbmin[0]), __double2float_rd(b.bbmin[1]),
-                              __double2float_rd(b.bbmin[2]), 0.0f);
+                              __double2float_rd(b.bbmin[2]), __int_as_float(t.cell_n[c]));
     mc.bbmax[c] = make_float4(__double2float_ru(b.bbmax[0]), __double2float_ru(b.bbmax[1]),
-                              __double2float_ru(b.bbmax[2]), 0.0f);
+                              __double2float_ru(b.bbmax[2]), __int_as_float((int) t.cell_level[c]));
   }
 }
 
@@ -297,13 +298,16 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
               bmin[k] = __double2float_rd(gmin[k] - s);
               bmax[k] = __double2float_ru(gmax[k] - s);
             }
-            auto decide = [&](int node, int level) -> int {
-              if (t.cell_n[node] == 0) return kSkip;
-              if (!fbox_overlap(bmin, bmax, mc.bbmin[node], mc.bbmax[node])) return kSkip;
+            // cell count and level ride in the float box's w lanes: two loads a decision
+            auto decide = [&](int node, int& level) -> int {
+              const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];
+              level = __float_as_int(b1.w);
+              if (__float_as_int(b0.w) == 0) return kSkip;
+              if (!fbox_overlap(bmin, bmax, b0, b1)) return kSkip;
               return level == t.ltot ? kEmitA : kOpen;
             };
             auto tag = [&](int node, int) { return node | (code << kNodeBits); };
-            stack_ok = stack_ok && warp_walk(0, t.ltot, t.cell_level, stack, kDensStack, L, decide, tag, flush);
+            stack_ok = stack_ok && warp_walk_lv(0, t.ltot, stack, kDensStack, L, decide, tag, flush);
           }
     };
     walk_all([&]() { overflow = true; });
@@ -654,13 +658,15 @@ __device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& 
                 bmin[q] = __double2float_rd(gmin[q] - sft);
                 bmax[q] = __double2float_ru(gmax[q] - sft);
               }
-              auto decide = [&](int node, int level) -> int {
-                if (t.cell_n[node] == 0) return kSkip;
-                if (!fbox_overlap(bmin, bmax, mc.bbmin[node], mc.bbmax[node])) return kSkip;
+              auto decide = [&](int node, int& level) -> int {
+                const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];   // w: cell_n, level
+                level = __float_as_int(b1.w);
+                if (__float_as_int(b0.w) == 0) return kSkip;
+                if (!fbox_overlap(bmin, bmax, b0, b1)) return kSkip;
                 return level == t.ltot ? kEmitA : kOpen;
               };
               auto tag = [&](int node, int) { return node | (code << kNodeBits); };
-              stack_ok = warp_walk(0, t.ltot, t.cell_level, stack, kPPStack, L, decide, tag, consume) && stack_ok;
+              stack_ok = warp_walk_lv(0, t.ltot, stack, kPPStack, L, decide, tag, consume) && stack_ok;
               consume();
               L.na = 0;
             }
@@ -882,8 +888,8 @@ struct LeafGeo {
 };
 
 __device__ __forceinline__ int grav_decide(const Tree& t, const MixedCells& mc, const LeafGeo& G, int node, int level,
-                                           unsigned long long& exact) {
-  const int on = t.cell_n[node];
+                                           float4 mt, unsigned long long& exact) {
+  const int on = __float_as_int(mt.y);
   const float4 gh = mc.geo_hi[node], gl = mc.geo_lo[node];
   const float dx = (gh.x - G.hi.x) + (gl.x - G.lo.x);
   const float dy = (gh.y - G.hi.y) + (gl.y - G.lo.y);
@@ -896,7 +902,7 @@ __device__ __forceinline__ int grav_decide(const Tree& t, const MixedCells& mc, 
   if (d2 < thr * (1.0f - kMargin)) near = 1;
   else if (d2 > thr * (1.0f + kMargin)) near = 0;
   else near = -1;
-  const float cd = mc.cdist[node];
+  const float cd = mt.x;
   int open_mac;   // 1: too close (open), 0: accept
   if (d2 < cd * (1.0f - kMargin)) open_mac = 1;
   else if (d2 > cd * (1.0f + kMargin)) open_mac = 0;
@@ -1156,7 +1162,11 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     top -= take;
     __syncwarp();
     int act = kSkip, level = 0;
-    if (node >= 0) { level = t.cell_level[node]; act = grav_decide(t, mc, G, node, level, exact); }
+    if (node >= 0) {
+      const float4 mt = mc.meta[node];
+      level = __float_as_int(mt.z);
+      act = grav_decide(t, mc, G, node, level, mt, exact);
+    }
     const unsigned mo = __ballot_sync(kFull, act == kOpen);
     const int nopen = __popc(mo);
     if (top + 2 * nopen > kFStack) { stack_ok = false; break; }
@@ -1340,9 +1350,11 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
     }
     return true;
   };
-  auto decide = [&](int node, int level) -> int {
-    if (t.cell_n[node] == 0) return kSkip;
-    if (!(pbox(bmin_f, bmax_f, mc.hbmin[node], mc.hbmax[node]) || pbox(hmin_f, hmax_f, mc.bbmin[node], mc.bbmax[node])))
+  auto decide = [&](int node, int& level) -> int {
+    const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];   // w: cell_n, level
+    level = __float_as_int(b1.w);
+    if (__float_as_int(b0.w) == 0) return kSkip;
+    if (!(pbox(bmin_f, bmax_f, mc.hbmin[node], mc.hbmax[node]) || pbox(hmin_f, hmax_f, b0, b1)))
       return kSkip;
     return level == t.ltot ? kEmitA : kOpen;
   };
@@ -1382,7 +1394,7 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
       }
     }
   };
-  const bool ok = warp_walk(0, t.ltot, t.cell_level, stack, kFStack, L, decide, tag, consume);
+  const bool ok = warp_walk_lv(0, t.ltot, stack, kFStack, L, decide, tag, consume);
   consume();
   if (!ok && lane == 0) atomicOr(cnt.status, (unsigned) kStatusStackOverflow);
   unsigned long long a1 = npairs, a4 = exact;

@@ -23,7 +23,7 @@ struct MixedParticles {
 struct MixedCells {
   float4* geo_hi;   // rcell_hi xyz, rmax
   float4* geo_lo;   // rcell_lo xyz, hmax (after the h solve)
-  float* cdist;     // cdistsqd
+  float4* meta;     // cdistsqd, cell_n and level (int bits), 0: one load per walk decision
   float4* com_hi;   // com_hi xyz, m
   float4* com_lo;   // com_lo xyz, q4
   float4* quad;     // q0 q1 q2 q3
