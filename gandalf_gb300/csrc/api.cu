@@ -66,6 +66,7 @@ struct gsph_ctx {
   int* idx[3] = {};
   int* listb[3] = {};
   unsigned long long* key2[3] = {};
+  int* deep_inv = nullptr;
   int *radix_hist = nullptr, *radix_tot = nullptr;
   unsigned char *side = nullptr, *seg_axis = nullptr;
   int* blocksum = nullptr;
@@ -250,6 +251,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
     for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->key2[q], capn);
     if (rc == GSPH_OK) rc = alloc(c, c->radix_hist, (size_t) 3 * 256 * radix_tiles(capn));
     if (rc == GSPH_OK) rc = alloc(c, c->radix_tot, 3 * 256);
+    if (rc == GSPH_OK) rc = alloc(c, c->deep_inv, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->side, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->seg_axis, (capc + 1) / 2);
     if (rc == GSPH_OK) rc = alloc(c, c->blocksum, 3 * (size_t) partition_blocks(capn) + 3);
@@ -527,6 +529,7 @@ int do_build(gsph_ctx* c) {
   }
   a.radix_hist = c->radix_hist;
   a.radix_tot = c->radix_tot;
+  a.deep_inv = c->deep_inv;
   a.side = c->side; a.seg_axis = c->seg_axis; a.blocksum = c->blocksum; a.rootkey = c->rootkey; a.ibox = c->ibox;
   a.heap_first = c->heap_first; a.heap_n = c->heap_n; a.heap_ones_before = c->heap_ones;
   a.p = make_particles(c);

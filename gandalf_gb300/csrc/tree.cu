@@ -11,8 +11,10 @@
 // Each particle's index is presorted once per axis on (coordinate key, index) — an LSD
 // radix sort in the allocating build, a bitonic network in the allocation-free one (its
 // scratch has no room for the radix sort's second buffers) — so every segment's median
-// along its split axis sits at position first + n/2 of that axis list.  A pass then marks each particle's side and stable-partitions all three lists
-// with one global scan, which keeps each child's lists sorted.  Particles are never moved
+// along its split axis sits at position first + n/2 of that axis list.  A pass then
+// marks each particle's side and stable-partitions all three lists with one global scan,
+// which keeps each child's lists sorted; once the segments are small, one block per
+// segment finishes the remaining levels in shared memory.  Particles are never moved
 // until the final gather into leaf order.  Stocking is one launch: each leaf thread stocks
 // its leaf and climbs while it is the second child to arrive at a parent.
 #include "gsph_state.cuh"
@@ -372,6 +374,105 @@ __global__ void __launch_bounds__(1024) k_part_scatter(int l, int n, BuildLists 
   }
 }
 
+// ---- the deep levels of a segment in shared memory ---------------------------------------
+// Once every segment of a level holds at most kDeepMax particles, one block finishes its
+// segment's remaining levels in shared memory: the same split axis, median coordinate,
+// child boxes, side marks and stable partitions as the level passes, on 16-bit local ids
+// (a particle's position in the segment's x list), with one launch instead of five per
+// level.  The block writes the segment's final first list (leaf order) back in place.
+constexpr int kDeepMax = 1024;
+constexpr int kDeepThreads = 512;
+
+__global__ void __launch_bounds__(kDeepThreads) k_build_deep(int L0, int ltot, BuildLists cur, int* inv,
+                                                            const double* __restrict__ x,
+                                                            const double* __restrict__ y,
+                                                            const double* __restrict__ z,
+                                                            const int* __restrict__ heap_first,
+                                                            const int* __restrict__ heap_n, double* ibox) {
+  __shared__ unsigned short s_l[2][3][kDeepMax];
+  __shared__ int s_glob[kDeepMax];
+  __shared__ int s_scan[kDeepMax];
+  __shared__ unsigned char s_side[kDeepMax];
+  __shared__ unsigned char s_kd[kDeepMax / 2];
+  __shared__ int ws[33];
+  const int tid = threadIdx.x;
+  const int s0 = blockIdx.x;
+  const int h0 = (1 << L0) - 1 + s0;
+  const int first = heap_first[h0], cnt = heap_n[h0];
+  for (int q = tid; q < cnt; q += kDeepThreads) {
+    const int gid = cur.l[0][first + q];
+    s_glob[q] = gid;
+    s_l[0][0][q] = (unsigned short) q;
+    inv[gid] = q;
+  }
+  __syncthreads();
+  for (int a = 1; a < 3; a++)
+    for (int q = tid; q < cnt; q += kDeepThreads) s_l[0][a][q] = (unsigned short) inv[cur.l[a][first + q]];
+  __syncthreads();
+  int cb = 0;
+  for (int l = L0; l < ltot; l++) {
+    const int d = l - L0, nsub = 1 << d;
+    // split axis, median and child boxes of each sub-segment (k_split_prepare)
+    for (int q = tid; q < nsub; q += kDeepThreads) {
+      const int hidx = (1 << l) - 1 + (s0 << d) + q;
+      const int f = heap_first[hidx] - first, c = heap_n[hidx];
+      double bmin[3], bmax[3];
+      for (int k = 0; k < 3; k++) { bmin[k] = ibox[6 * hidx + k]; bmax[k] = ibox[6 * hidx + 3 + k]; }
+      int kd = 0;
+      double rkmax = 0.0;
+      for (int k = 0; k < 3; k++) {
+        const double ext = __dsub_rn(bmax[k], bmin[k]);
+        if (ext > rkmax) { rkmax = ext; kd = k; }
+      }
+      s_kd[q] = (unsigned char) kd;
+      double rdiv = 0.0;
+      if (c > 0) {
+        const int id = s_glob[s_l[cb][kd][f + c / 2]];
+        rdiv = kd == 0 ? x[id] : (kd == 1 ? y[id] : z[id]);
+      }
+      const int c1 = 2 * hidx + 1, c2 = 2 * hidx + 2;
+      for (int k = 0; k < 3; k++) {
+        ibox[6 * c1 + k] = bmin[k]; ibox[6 * c1 + 3 + k] = bmax[k];
+        ibox[6 * c2 + k] = bmin[k]; ibox[6 * c2 + 3 + k] = bmax[k];
+      }
+      ibox[6 * c1 + 3 + kd] = rdiv;
+      ibox[6 * c2 + kd] = rdiv;
+    }
+    __syncthreads();
+    // side marks (k_mark_side)
+    for (int q = tid; q < cnt; q += kDeepThreads) {
+      int f, c;
+      const int sub = seg_of(q, cnt, d, f, c);
+      s_side[s_l[cb][s_kd[sub]][q]] = (unsigned char) (q - f >= (c >> 1));
+    }
+    __syncthreads();
+    // stable partition of the three lists inside each sub-segment (k_part_scatter)
+    for (int a = 0; a < 3; a++) {
+      const int q0 = 2 * tid, q1 = q0 + 1;
+      const int f0 = q0 < cnt ? s_side[s_l[cb][a][q0]] : 0;
+      const int f1 = q1 < cnt ? s_side[s_l[cb][a][q1]] : 0;
+      int total;
+      const int ex = block_exscan(f0 + f1, ws, total);
+      if (q0 < cnt) s_scan[q0] = ex;
+      if (q1 < cnt) s_scan[q1] = ex + f0;
+      __syncthreads();
+      const int qq[2] = {q0, q1}, ff[2] = {f0, f1};
+      for (int r = 0; r < 2; r++) {
+        const int q = qq[r];
+        if (q >= cnt) continue;
+        int f, c;
+        seg_of(q, cnt, d, f, c);
+        const int ones = s_scan[q] - s_scan[f];   // ones before q inside its sub-segment
+        const int pos = ff[r] ? f + (c >> 1) + ones : f + (q - f) - ones;
+        s_l[cb ^ 1][a][pos] = s_l[cb][a][q];
+      }
+      __syncthreads();
+    }
+    cb ^= 1;
+  }
+  for (int q = tid; q < cnt; q += kDeepThreads) cur.l[0][first + q] = s_glob[s_l[cb][0][q]];
+}
+
 __global__ void k_gather_leaf_order(int n, const int* __restrict__ perm, InputArrays in, Particles p,
                                     int* id_out) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
@@ -638,7 +739,11 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
   BuildLists cur, nxt;
   for (int q = 0; q < 3; q++) { cur.l[q] = a.sort.idx[q]; nxt.l[q] = a.lists_b[q]; }
   const int nb = partition_blocks(n);
-  for (int l = 0; l < a.ltot; l++) {
+  // levels from L0 on run in shared memory, one block per segment of level L0
+  int L0 = 0;
+  while (L0 < a.ltot && ((n + (1 << L0) - 1) >> L0) > kDeepMax) L0++;
+  if (!a.deep_inv) L0 = a.ltot;
+  for (int l = 0; l < L0; l++) {
     const int nseg = 1 << l;
     k_split_prepare<<<(nseg + 127) / 128, 128, 0, st>>>(l, cur, a.in.x, a.in.y, a.in.z, a.heap_first,
                                                          a.heap_n, a.ibox, a.seg_axis);
@@ -648,6 +753,11 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
     k_part_scatter<<<dim3(nb, 3), 1024, 0, st>>>(l, n, cur, nxt, a.side, a.blocksum, nb, a.heap_ones_before);
     BuildLists tmp = cur; cur = nxt; nxt = tmp;
     launches += 5;
+  }
+  if (L0 < a.ltot) {
+    k_build_deep<<<1 << L0, kDeepThreads, 0, st>>>(L0, a.ltot, cur, a.deep_inv, a.in.x, a.in.y, a.in.z,
+                                                   a.heap_first, a.heap_n, a.ibox);
+    launches++;
   }
   k_gather_leaf_order<<<grid_for(n, 256), 256, 0, st>>>(n, cur.l[0], a.in, a.p, a.id_out);
   cudaMemsetAsync(a.tree.climb, 0, sizeof(unsigned) * (size_t) a.tree.ncell, st);

@@ -36,6 +36,7 @@ struct BuildArgs {
   unsigned long long* key2[3];  // second key buffer of the radix sort (length n)
   int* radix_hist;              // 3 x 256 x radix_tiles(n)
   int* radix_tot;               // 3 x 256
+  int* deep_inv;                // n: global -> local id of the shared-memory deep levels
   unsigned char* side;          // per particle: 0 first child, 1 second child
   unsigned char* seg_axis;      // per segment of the current level
   int* blocksum;                // 3 * partition_blocks(n)
