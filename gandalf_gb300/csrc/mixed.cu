@@ -269,8 +269,8 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   double mcheck = 0.0;
   double h_out = h_start, rho_out = 0.0, om_out = 0.0, zeta_out = 0.0;
 
-  // returns 1 if the cell aborts (some h > hmax_list), 2 if the warp gives up (list too
-  // long for a warp on its own; only when give_up), 0 when solved
+  // returns 1 if the cell aborts (some h > hmax_list), 2 if the warp gives up (gather or
+  // compact list too long for a warp on its own; only when give_up), 0 when solved
   auto attempt = [&](double hmax_list) -> int {
     const double hr = __dmul_rn(kKernRange, hmax_list);
     double gmin[3], gmax[3];
@@ -427,6 +427,10 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
           if (gc + u == g) ccount = tc[u];
       }
     }
+    // A particle whose compact list does not fit would rescan every candidate in every
+    // iteration, and its warp with it (such leaves took 5-10x the mean): hand the leaf to
+    // the heavy-leaf kernel instead.
+    if (give_up && __any_sync(kFull, mine && !overflow && ccount > kcap)) return 2;
     const bool use_compact = !overflow && ccount <= kcap;
 
     float hi = (float) h_start, h_lower = 0.0f, h_upper = (float) hmax_list;
