@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--impl", default="gsph", choices=["gsph", "reference"])
     ap.add_argument("--workload", default="plummer_sphere")
     ap.add_argument("--n", type=int, default=0)
+    ap.add_argument("--nleafmax", type=int, default=0,
+                    help="evrard_sphere: leaf size to use instead of the autotuner's choice")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -198,7 +200,8 @@ def evrard_main(args, rank, world, local):
     steps = args.steps if args.steps != 10 else 3
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     with ClockSampler(local) as clk:
-        tune = tune_leaf_size(c, params, precision=form, steps=1, device=local)
+        tune = ({"nleafmax": args.nleafmax, "ms_per_step": None} if args.nleafmax > 0 else
+                tune_leaf_size(c, params, precision=form, steps=1, device=local))
         t = GradhSphTree(params, precision=form, nleafmax=tune["nleafmax"], device=local)
         stream = torch.cuda.current_stream()
         t.set_stream(stream.cuda_stream)
@@ -230,10 +233,11 @@ def evrard_main(args, rank, world, local):
             "data": "synthetic",
             "config": {"workload": "evrard_sphere", "n": n, "nstar": 64, "star_mass": 1e-3, "star_h": 0.01,
                        "thetamaxsqd": 0.25, "multipole": "quadrupole", "precision": form,
-                       "nleafmax_autotuned": tune, "cuda_graph": True, "parallelism": f"replicas{world}",
+                       ("nleafmax" if args.nleafmax > 0 else "nleafmax_autotuned"): tune, "cuda_graph": True, "parallelism": f"replicas{world}",
                        "l2": "flushed between timed steps (256 MiB write)"},
             "gpu_launches": st["launches"],
             "counts": {k: st[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs", "cell_pairs")},
+            "heavy_leaves": {"density": st["heavy_density"], "forces": st["heavy_forces"]},
             "phases_ms_last_step": {k: st[k] for k in ("ms_build", "ms_density", "ms_hmax", "ms_forces")},
             "star_gpot_mean": float(np.mean(sf["gpot"])),
             "roofline": {"bound": "fp32" if form == "mixed" else "fp64", "kernel": "whole step",
@@ -660,7 +664,9 @@ def main():
                         "phases_ms": {k: round(v, 4) for k, v in Rf["per"].items()},
                         "counts": {k: Rf["stats"][k] for k in ("density_pairs", "hydro_pairs",
                                                                "direct_pairs", "cell_pairs",
-                                                               "exact_checks", "launches")}}
+                                                               "exact_checks", "launches")},
+                        "heavy_leaves": {"density": Rf["stats"]["heavy_density"],
+                                         "forces": Rf["stats"]["heavy_forces"]}}
     if "fp64" in ok and "mixed" in ok:
         a, b = results["mixed"]["results"], results["fp64"]["results"]
         errs = {}

@@ -96,6 +96,8 @@ struct gsph_ctx {
   // star particles: 8 input arrays (x y z vx vy vz m h) then 7 results (a, adot, gpot)
   int nstar = 0, star_cap = 0;
   double* star_buf = nullptr;
+  float4* star_f = nullptr;               // mixed form: 2 x star_cap (hi xyz m, lo xyz h)
+  std::vector<float4> star_f_host;        // staging of the last upload
   bool have_star_forces = false;
   // KDK integration with block timesteps (gsph_kdk_*)
   bool kdk = false;
@@ -317,6 +319,8 @@ StarSet make_stars(const gsph_ctx* c) {
   double* o = c->star_buf + 8 * k;
   s.ax = o; s.ay = o + k; s.az = o + 2 * k; s.adotx = o + 3 * k; s.adoty = o + 4 * k; s.adotz = o + 5 * k;
   s.gpot = o + 6 * k;
+  s.fhi = c->star_f;
+  s.flo = c->star_f + k;
   return s;
 }
 
@@ -607,7 +611,8 @@ int do_forces(gsph_ctx* c, bool gravity) {
     c->launches += 1;
   }
   // star gravity on the gas, after gpot_hydro is taken (GradhSphTree.cpp:596-606)
-  c->launches += (unsigned) launch_gas_from_stars(p, make_stars(c), c->stream);
+  c->launches += (unsigned) (mixed(c) ? launch_gas_from_stars_mixed(p, make_mixed_particles(c), make_stars(c), c->stream)
+                                      : launch_gas_from_stars(p, make_stars(c), c->stream));
   c->have_forces = true;
   c->have_star_forces = false;
   return check_launch(c, "forces");
@@ -708,6 +713,7 @@ void gsph_destroy(gsph_ctx* c) {
   free_all(c);
   if (c->aos) cudaFree(c->aos);
   if (c->star_buf) cudaFree(c->star_buf);
+  if (c->star_f) cudaFree(c->star_f);
   for (int q = 0; q < 5; q++) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -937,14 +943,31 @@ int32_t gsph_set_stars(gsph_ctx* c, int64_t nstar, const double* x, const double
   if (nstar > c->star_cap) {
     drop_graph(c);
     if (c->star_buf) cudaFree(c->star_buf);
+    if (c->star_f) cudaFree(c->star_f);
     c->star_buf = nullptr;
+    c->star_f = nullptr;
     c->star_cap = 0;
     GSPH_CUDA(cudaMalloc(&c->star_buf, sizeof(double) * 15 * (size_t) nstar));
+    GSPH_CUDA(cudaMalloc(&c->star_f, sizeof(float4) * 2 * (size_t) nstar));
     c->star_cap = (int) nstar;
   }
   for (int q = 0; q < 8 && nstar > 0; q++)
     GSPH_CUDA(cudaMemcpyAsync(c->star_buf + (size_t) q * c->star_cap, a[q], sizeof(double) * (size_t) nstar,
                               cudaMemcpyHostToDevice, c->stream));
+  if (nstar > 0) {
+    // positions as unevaluated float sums hi + lo (as the gas mirrors), mass and h
+    c->star_f_host.assign(2 * (size_t) c->star_cap, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int64_t i = 0; i < nstar; i++) {
+      float hi[3], lo[3];
+      const double r[3] = {x[i], y[i], z[i]};
+      for (int k = 0; k < 3; k++) { hi[k] = (float) r[k]; lo[k] = (float) (r[k] - (double) hi[k]); }
+      c->star_f_host[i] = make_float4(hi[0], hi[1], hi[2], (float) m[i]);
+      c->star_f_host[c->star_cap + i] = make_float4(lo[0], lo[1], lo[2], (float) h[i]);
+    }
+    GSPH_CUDA(cudaMemcpyAsync(c->star_f, c->star_f_host.data(), sizeof(float4) * 2 * (size_t) c->star_cap,
+                              cudaMemcpyHostToDevice, c->stream));
+    GSPH_CUDA(cudaStreamSynchronize(c->stream));   // the staging vector may change before a later copy
+  }
   if ((int) nstar != c->nstar || nstar > c->star_cap) drop_graph(c);
   c->nstar = (int) nstar;
   // the h solve (zeta term) and both force passes depend on the stars

@@ -9,6 +9,7 @@ namespace gsph {
 struct StarSet {
   int n;
   const double *x, *y, *z, *vx, *vy, *vz, *m, *h;
+  const float4 *fhi, *flo;   // mixed form: (x_hi y_hi z_hi m), (x_lo y_lo z_lo h)
   double *ax, *ay, *az, *adotx, *adoty, *adotz, *gpot;
 };
 

@@ -224,8 +224,7 @@ __device__ __forceinline__ void h_update_f(float drho, float dom, float dze, flo
 // Final per-particle results of the h solve (GradhSph.cpp:262-317): h, rho, hfactor,
 // hrangesqd, invomega, zeta (with the SPH-star term), the EOS quantities.
 __device__ __forceinline__ void finish_density(const Particles& p, const SphParams& prm, int slot, double hfin,
-                                               double rho_out, double om_out, double zeta_out, double xi, double yi,
-                                               double zi) {
+                                               double rho_out, double om_out, double zeta_out, double star_zeta) {
   const double invh = 1.0 / hfin;
   p.h[slot] = hfin;
   p.rho[slot] = rho_out;
@@ -235,7 +234,7 @@ __device__ __forceinline__ void finish_density(const Particles& p, const SphPara
   const double drho = -(1.0 / 3.0) * hfin / rho_out;
   const double io = 1.0 / (1.0 - drho * om_out);
   p.invomega[slot] = io;
-  const double zsum = prm.stars.n ? zeta_out + star_zeta_sum(prm.stars, xi, yi, zi, hfin) : zeta_out;
+  const double zsum = zeta_out + star_zeta;
   p.zeta[slot] = drho * zsum * io;
   double u = p.u[slot];
   const double gm1 = prm.gamma_eos - 1.0;
@@ -534,7 +533,14 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   unsigned long long tot = pairs;
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(kFull, tot, o);
   if (lane == 0) atomicAdd(cnt.density_pairs, tot);
-  if (mine && sl == 0 && wib == 0) finish_density(p, prm, slot, h_out, rho_out, om_out, zeta_out, xi, yi, zi);
+  // the SPH-star zeta term, the particle's LPG lanes sharing the stars
+  float zs = 0.0f;
+  if (prm.stars.n) {
+    if (mine) zs = star_zeta_part_f(prm.stars, pih, pil, (float) h_out, sl, LPG);
+#pragma unroll
+    for (int o = 1; o < LPG; o <<= 1) zs += __shfl_xor_sync(kFull, zs, o);
+  }
+  if (mine && sl == 0 && wib == 0) finish_density(p, prm, slot, h_out, rho_out, om_out, zeta_out, (double) zs);
   return true;
 }
 
@@ -684,8 +690,14 @@ __device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& 
         if (!stack_ok) done = true;
       }
       abort_any = abort_any || abort_cell;
+      // the SPH-star zeta term, the warp's lanes sharing the stars (h is warp-uniform here)
+      float zs = 0.0f;
+      if (prm.stars.n && !abort_cell) {
+        zs = star_zeta_part_f(prm.stars, pih, pil, (float) fmax(hrho_last, h_lower), lane, 32);
+        for (int o = 16; o > 0; o >>= 1) zs += __shfl_xor_sync(kFull, zs, o);
+      }
       if (!abort_cell && lane == 0)
-        finish_density(p, prm, slot, fmax(hrho_last, h_lower), rho, om, zeta, xi, yi, zi);
+        finish_density(p, prm, slot, fmax(hrho_last, h_lower), rho, om, zeta, (double) zs);
     }
     if (lane == 0) sm.mloc[wib] = mloc;
     abort_any = __syncthreads_or(abort_any);

@@ -1,4 +1,5 @@
-// Star-gas gravitational coupling (FP64 in both precision forms).
+// Star-gas gravitational coupling.  FP64, except gas <- stars in the mixed form (FP32
+// pair arithmetic on hi + lo float positions, like the form's other pair terms).
 //
 //  gas <- stars   GradhSph::ComputeStarGravForces (src/GradhSph/GradhSph.cpp:698-743), run
 //                 inside the gas force passes after gpot_hydro is taken
@@ -15,6 +16,7 @@
 // stars staged in shared memory, and the star <- gas pass is one warp per star.
 #include "gsph_walk.cuh"
 #include "kernels.cuh"
+#include "mixed_state.cuh"
 #include "stars.cuh"
 
 namespace gsph {
@@ -50,6 +52,52 @@ __global__ void __launch_bounds__(256) k_gas_from_stars(Particles p, StarSet s) 
           const double paux = ms * invhmean * invhmean * m4_wgrav(drmag * invhmean) * invdrmag;
           ax += paux * dx; ay += paux * dy; az += paux * dz;
           pot += ms * invhmean * m4_wpot(drmag * invhmean);
+        }
+      }
+    }
+    if (mine) {
+      p.gpot_hydro[slot] = p.gpot[slot];
+      p.agx[slot] += ax; p.agy[slot] += ay; p.agz[slot] += az;
+      p.ax[slot] += ax; p.ay[slot] += ay; p.az[slot] += az;
+      p.gpot[slot] += pot;
+    }
+  }
+}
+
+// Mixed form: the same sums in single precision (positions as hi + lo float pairs, one
+// reciprocal per pair and no other division), added to the fp64 accumulators.
+__global__ void __launch_bounds__(256) k_gas_from_stars_f(Particles p, MixedParticles mp, StarSet s) {
+  __shared__ float4 shi[kStarChunk], slo[kStarChunk];
+  const int n = p.n;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const int slot = base + threadIdx.x;
+    const bool mine = slot < n && is_active(p, slot);
+    float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pl = ph;
+    float hi = 1.0f;
+    if (mine) { ph = mp.pos_hi[slot]; pl = mp.pos_lo[slot]; hi = (float) p.h[slot]; }
+    float ax = 0.0f, ay = 0.0f, az = 0.0f, pot = 0.0f;
+    for (int c0 = 0; c0 < s.n; c0 += kStarChunk) {
+      const int cn = min(kStarChunk, s.n - c0);
+      __syncthreads();
+      for (int q = threadIdx.x; q < cn; q += blockDim.x) { shi[q] = s.fhi[c0 + q]; slo[q] = s.flo[c0 + q]; }
+      __syncthreads();
+      if (mine) {
+        for (int j = 0; j < cn; j++) {
+          const float4 sh = shi[j], sl = slo[j];
+          const float dx = (sh.x - ph.x) + (sl.x - pl.x);
+          const float dy = (sh.y - ph.y) + (sl.y - pl.y);
+          const float dz = (sh.z - ph.z) + (sl.z - pl.z);
+          const float r2 = dx * dx + dy * dy + dz * dz + 1.0e-20f;
+          const float invdrmag = rsqrtf(r2);
+          const float drmag = r2 * invdrmag;
+          const float hsum = hi + sl.w;
+          const float invhmean = __fdividef(2.0f, hsum);
+          // 1/s = hmean / |r|
+          float w1, wg, wp;
+          m4f_w1_grav_pot(drmag * invhmean, 0.5f * hsum * invdrmag, w1, wg, wp);
+          const float paux = sh.w * invhmean * invhmean * wg * invdrmag;
+          ax += paux * dx; ay += paux * dy; az += paux * dz;
+          pot += sh.w * invhmean * wp;
         }
       }
     }
@@ -206,6 +254,13 @@ int launch_gas_from_stars(const Particles& p, const StarSet& s, cudaStream_t st)
   if (s.n <= 0) return 0;
   const int blocks = std::max(1, std::min((p.n + 255) / 256, 152 * 8));
   k_gas_from_stars<<<blocks, 256, 0, st>>>(p, s);
+  return 1;
+}
+
+int launch_gas_from_stars_mixed(const Particles& p, const MixedParticles& mp, const StarSet& s, cudaStream_t st) {
+  if (s.n <= 0) return 0;
+  const int blocks = std::max(1, std::min((p.n + 255) / 256, 152 * 8));
+  k_gas_from_stars_f<<<blocks, 256, 0, st>>>(p, mp, s);
   return 1;
 }
 

@@ -20,7 +20,28 @@ __device__ __forceinline__ double star_zeta_sum(const StarSet& s, double xi, dou
   return z;
 }
 
+// The same sum in single precision for the mixed form, positions as hi + lo float pairs;
+// stars j0, j0 + stride, ... (the lanes of a particle share the stars and add up).
+__device__ __forceinline__ float star_zeta_part_f(const StarSet& s, float4 ph, float4 pl, float h, int j0,
+                                                  int stride) {
+  float z = 0.0f;
+  for (int j = j0; j < s.n; j += stride) {
+    const float4 sh = s.fhi[j], sl = s.flo[j];
+    const float ih = __fdividef(2.0f, h + sl.w);
+    const float ihsqd = ih * ih;
+    const float dx = (sh.x - ph.x) + (sl.x - pl.x);
+    const float dy = (sh.y - ph.y) + (sl.y - pl.y);
+    const float dz = (sh.z - ph.z) + (sl.z - pl.z);
+    const float ssqd = (dx * dx + dy * dy + dz * dz) * ihsqd;
+    const float sv = ssqd > 0.0f ? ssqd * rsqrtf(ssqd) : 0.0f;
+    z += sh.w * ihsqd * m4f_wzeta(sv);
+  }
+  return z;
+}
+
 int launch_gas_from_stars(const Particles& p, const StarSet& s, cudaStream_t st);
+struct MixedParticles;
+int launch_gas_from_stars_mixed(const Particles& p, const MixedParticles& mp, const StarSet& s, cudaStream_t st);
 int launch_stars_from_gas(const Tree& t, const Particles& p, const StarSet& s, const SphParams& prm,
                           const DeviceCounters& cnt, int max_leaf, cudaStream_t st);
 
