@@ -331,6 +331,7 @@ SphParams make_params(const gsph_ctx* c) {
   p.h_fac = cfg.h_fac; p.h_converge = cfg.h_converge; p.alpha_visc = cfg.alpha_visc;
   p.beta_visc = cfg.beta_visc; p.gamma_eos = cfg.gamma_eos; p.temp0 = cfg.temp0; p.mu_bar = cfg.mu_bar;
   p.thetamaxsqd = cfg.thetamaxsqd;
+  p.u_iso = cfg.temp0 / (cfg.gamma_eos - 1.0) / cfg.mu_bar;
   for (int k = 0; k < 3; k++) {
     p.boxmin[k] = cfg.boxmin[k]; p.boxmax[k] = cfg.boxmax[k];
     p.boxsize[k] = cfg.boxmax[k] - cfg.boxmin[k];

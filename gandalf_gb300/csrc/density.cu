@@ -60,7 +60,7 @@ __device__ __forceinline__ void write_density(const Particles& p, const SphParam
   p.zeta[slot] = drho * zsum * io;
   double u = p.u[slot];
   const double gm1 = prm.gamma_eos - 1.0;
-  if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
+  if (prm.eos == 1) { u = prm.u_iso; p.u[slot] = u; }
   p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
   p.pressure[slot] = gm1 * rho_out * u;
 }

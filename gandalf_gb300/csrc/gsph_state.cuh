@@ -15,6 +15,7 @@ struct StarSet {
 
 struct SphParams {
   double h_fac, h_converge, alpha_visc, beta_visc, gamma_eos, temp0, mu_bar, thetamaxsqd;
+  double u_iso;     // isothermal specific energy temp0 / (gamma - 1) / mu_bar, evaluated on the host
   double boxmin[3], boxmax[3], boxsize[3], boxhalf[3];
   int eos;          // 0 adiabatic energy equation, 1 isothermal
   int periodic;     // 0 open, 1 periodic in x, y and z

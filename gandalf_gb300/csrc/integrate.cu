@@ -401,7 +401,7 @@ __global__ void k_kdk_thermal(Particles p, SphParams prm) {
   const double gm1 = prm.gamma_eos - 1.0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < p.n; s += gridDim.x * blockDim.x) {
     double u = p.u[s];
-    if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[s] = u; }
+    if (prm.eos == 1) { u = prm.u_iso; p.u[s] = u; }
     p.sound[s] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
     p.pressure[s] = gm1 * p.rho[s] * u;
   }

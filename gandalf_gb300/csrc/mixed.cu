@@ -103,6 +103,12 @@ __device__ __forceinline__ double gsum_d(double v) {
   for (int o = 1; o < LPG; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
   return v;
 }
+template <int LPG>
+__device__ __forceinline__ float gsum_f(float v) {
+#pragma unroll
+  for (int o = 1; o < LPG; o <<= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
 
 __device__ __forceinline__ float fsqrt_pos(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
 
@@ -223,24 +229,27 @@ __device__ __forceinline__ void h_update_f(float drho, float dom, float dze, flo
 
 // Final per-particle results of the h solve (GradhSph.cpp:262-317): h, rho, hfactor,
 // hrangesqd, invomega, zeta (with the SPH-star term), the EOS quantities.
+// The derived quantities in single precision (the form's h and rho carry float accuracy),
+// stored as fp64; hrangesqd keeps the fp64 product, which the exact membership checks use.
 __device__ __forceinline__ void finish_density(const Particles& p, const SphParams& prm, int slot, double hfin,
                                                double rho_out, double om_out, double zeta_out, double star_zeta) {
-  const double invh = 1.0 / hfin;
+  const float hf = (float) hfin, rf = (float) rho_out;
+  const float invh = __frcp_rn(hf);
+  const float ih2 = invh * invh;
   p.h[slot] = hfin;
   p.rho[slot] = rho_out;
-  p.hfactor[slot] = invh * invh * invh * invh;
+  p.hfactor[slot] = (double) (ih2 * ih2);
   p.hrangesqd[slot] = __dmul_rn(__dmul_rn(kKernRangeSqd, hfin), hfin);
   p.div_v[slot] = 0.0;
-  const double drho = -(1.0 / 3.0) * hfin / rho_out;
-  const double io = 1.0 / (1.0 - drho * om_out);
-  p.invomega[slot] = io;
-  const double zsum = zeta_out + star_zeta;
-  p.zeta[slot] = drho * zsum * io;
+  const float drho = -(1.0f / 3.0f) * hf * __frcp_rn(rf);
+  const float io = __frcp_rn(1.0f - drho * (float) om_out);
+  p.invomega[slot] = (double) io;
+  p.zeta[slot] = (double) (drho * (float) (zeta_out + star_zeta) * io);
   double u = p.u[slot];
-  const double gm1 = prm.gamma_eos - 1.0;
-  if (prm.eos == 1) { u = prm.temp0 / gm1 / prm.mu_bar; p.u[slot] = u; }
-  p.sound[slot] = prm.eos == 1 ? sqrt(gm1 * u) : sqrt(prm.gamma_eos * gm1 * u);
-  p.pressure[slot] = gm1 * rho_out * u;
+  if (prm.eos == 1) { u = prm.u_iso; p.u[slot] = u; }
+  const float gm1 = (float) (prm.gamma_eos - 1.0), uf = (float) u;
+  p.sound[slot] = (double) (prm.eos == 1 ? sqrtf(gm1 * uf) : sqrtf((float) prm.gamma_eos * gm1 * uf));
+  p.pressure[slot] = (double) (gm1 * rf * uf);
 }
 
 template <int LPG, int WARPS>
@@ -957,26 +966,30 @@ template <int LPG>
 __device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Particles& p, const DeviceCounters& cnt,
                                                   bool mine, int sl, int slot, const AccF& A, double gpot0,
                                                   unsigned long long ndir, unsigned long long dhash, bool grav) {
-  double ah[3], ag[3], gp, du, dv;
-  for (int k = 0; k < 3; k++) { ah[k] = gsum_d<LPG>((double) A.ah[k]); ag[k] = gsum_d<LPG>((double) A.ag[k]); }
-  gp = gsum_d<LPG>((double) A.gpot);
-  du = gsum_d<LPG>((double) A.dudt);
-  dv = gsum_d<LPG>((double) A.divv);
+  // the lanes' partial sums added in float (each holds a few hundred float terms already),
+  // the per-particle arithmetic after them in float too; results stored as fp64
+  float ah[3], ag[3], gp, du, dv;
+  for (int k = 0; k < 3; k++) { ah[k] = gsum_f<LPG>(A.ah[k]); ag[k] = gsum_f<LPG>(A.ag[k]); }
+  gp = gsum_f<LPG>(A.gpot);
+  du = gsum_f<LPG>(A.dudt);
+  dv = gsum_f<LPG>(A.divv);
   if (cnt.record) {
     unsigned long long dc = ndir, dh = dhash;
     for (int o = 1; o < LPG; o <<= 1) { dc += __shfl_xor_sync(kFull, dc, o); dh += __shfl_xor_sync(kFull, dh, o); }
     if (mine && sl == 0) { atomicAdd(&cnt.rec_dir_cnt[slot], dc); atomicAdd(&cnt.rec_dir_hash[slot], dh); }
   }
   if (!(mine && sl == 0)) return;
-  const double rho = p.rho[slot];
-  const double invrho = 1.0 / rho;
-  const double divv = dv * invrho;
-  const double P = (prm.gamma_eos - 1.0) * rho * p.u[slot];
-  p.div_v[slot] = divv;
-  p.dudt[slot] = du - P * divv * invrho * p.invomega[slot];
-  p.ax[slot] = ah[0] + ag[0]; p.ay[slot] = ah[1] + ag[1]; p.az[slot] = ah[2] + ag[2];
+  const float rho = (float) p.rho[slot];
+  const float invrho = __frcp_rn(rho);
+  const float divv = dv * invrho;
+  const float P = (float) (prm.gamma_eos - 1.0) * rho * (float) p.u[slot];
+  p.div_v[slot] = (double) divv;
+  p.dudt[slot] = (double) (du - P * divv * invrho * (float) p.invomega[slot]);
+  p.ax[slot] = (double) ah[0] + (double) ag[0];
+  p.ay[slot] = (double) ah[1] + (double) ag[1];
+  p.az[slot] = (double) ah[2] + (double) ag[2];
   p.agx[slot] = ag[0]; p.agy[slot] = ag[1]; p.agz[slot] = ag[2];
-  p.gpot[slot] = grav ? gpot0 + gp : 0.0;
+  p.gpot[slot] = grav ? gpot0 + (double) gp : 0.0;
 }
 
 constexpr int kForceWarps = 4;    // warps per block of the warp-per-leaf force kernels
@@ -1233,7 +1246,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   if (cnt.record) {
     for (int o = 16; o > 0; o >>= 1) { cc += __shfl_xor_sync(kFull, cc, o); ch += __shfl_xor_sync(kFull, ch, o); }
   }
-  const double gpot0 = (p.m[slot] / p.h[slot]) * m4_wpot(0.0);
+  const double gpot0 = (double) (T.ph.w * T.hyd.x * (float) m4_wpot(0.0));   // (m / h) wpot(0)
   if (SLICES == 1) {
     if (cnt.record && pfirst == 0 && lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
     finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, gpot0, ndir, dhash, true);
