@@ -67,6 +67,7 @@ struct gsph_ctx {
   int* listb[3] = {};
   unsigned long long* key2[3] = {};
   int* deep_inv = nullptr;
+  int* slot_of = nullptr;                 // slot of each input particle (inverse of id)
   int *radix_hist = nullptr, *radix_tot = nullptr;
   unsigned char *side = nullptr, *seg_axis = nullptr;
   int* blocksum = nullptr;
@@ -254,6 +255,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
     if (rc == GSPH_OK) rc = alloc(c, c->radix_hist, (size_t) 3 * 256 * radix_tiles(capn));
     if (rc == GSPH_OK) rc = alloc(c, c->radix_tot, 3 * 256);
     if (rc == GSPH_OK) rc = alloc(c, c->deep_inv, capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->slot_of, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->side, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->seg_axis, (capc + 1) / 2);
     if (rc == GSPH_OK) rc = alloc(c, c->blocksum, 3 * (size_t) partition_blocks(capn) + 3);
@@ -457,8 +459,9 @@ __global__ void k_pack_aos(unsigned char* base, int n, int64_t stride, gsph_fiel
   }
 }
 
-__global__ void k_scatter_field(const double* __restrict__ src, const int* __restrict__ id, int n, double* dst) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) dst[id[s]] = src[s];
+// Leaf order -> input order, written in input order (coalesced stores, random loads).
+__global__ void k_scatter_field(const double* __restrict__ src, const int* __restrict__ slot_of, int n, double* dst) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[slot_of[i]];
 }
 
 int field_index(const gsph_ctx* c, int field) {
@@ -539,6 +542,7 @@ int do_build(gsph_ctx* c) {
   a.heap_first = c->heap_first; a.heap_n = c->heap_n; a.heap_ones_before = c->heap_ones;
   a.p = make_particles(c);
   a.id_out = c->id;
+  a.slot_of = c->slot_of;
   a.tree = make_tree(c);
   a.thetamaxsqd = c->cfg.thetamaxsqd;
   c->launches += (unsigned) launch_build_tree(a, c->stream);
@@ -1009,7 +1013,7 @@ int32_t gsph_get_field_device(gsph_ctx* c, int32_t field, double* out) {
   if (fi < 0) return fail(c, GSPH_ERR_INVALID, "unknown field");
   if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "no results yet");
   cudaSetDevice(c->device);
-  k_scatter_field<<<grid1(c->n), 256, 0, c->stream>>>(c->f[fi], c->id, c->n, out);
+  k_scatter_field<<<grid1(c->n), 256, 0, c->stream>>>(c->f[fi], c->slot_of, c->n, out);
   return check_launch(c, "scatter field");
 }
 
@@ -1455,6 +1459,7 @@ KdkLeaf make_kdk_leaf(gsph_ctx* c) {
   KdkLeaf l{};
   l.n = c->n;
   l.id = c->id;
+  l.slot_of = c->slot_of;
   for (int q = 0; q < kKeep; q++) l.f[q] = c->f[kKeepField[q]];
   l.h = c->f[kFH];
   l.u = c->f[kFU];

@@ -101,8 +101,8 @@ __global__ void k_kdk_gather(KdkState s, KdkLeaf l, KdkGlobal* g) {
 
 // Solved fields back to input order; levelneib = max(old (0 if active), neighbours).
 __global__ void k_kdk_scatter(KdkState s, KdkLeaf l) {
-  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
-    const int i = l.id[slot];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l.n; i += gridDim.x * blockDim.x) {
+    const int slot = l.slot_of[i];
 #pragma unroll
     for (int q = 0; q < kKeep; q++) s.keep[q][i] = l.f[q][slot];
     s.h[i] = l.h[slot];
@@ -130,8 +130,8 @@ __global__ void k_kdk_refresh(KdkState s, KdkLeaf l, KdkGlobal* g) {
 
 // levelneib only (what CheckTimesteps reads between passes).
 __global__ void k_kdk_scatter_lvn(KdkState s, KdkLeaf l) {
-  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
-    const int i = l.id[slot];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l.n; i += gridDim.x * blockDim.x) {
+    const int slot = l.slot_of[i];
     const int base = l.active[slot] ? 0 : s.levelneib[i];
     s.levelneib[i] = max(base, l.lvn[slot]);
   }
@@ -139,8 +139,8 @@ __global__ void k_kdk_scatter_lvn(KdkState s, KdkLeaf l) {
 
 // Solved fields back to input order, once per step after the last pass.
 __global__ void k_kdk_scatter_fields(KdkState s, KdkLeaf l) {
-  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
-    const int i = l.id[slot];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l.n; i += gridDim.x * blockDim.x) {
+    const int slot = l.slot_of[i];
 #pragma unroll
     for (int q = 0; q < kKeep; q++) s.keep[q][i] = l.f[q][slot];
     s.h[i] = l.h[slot];

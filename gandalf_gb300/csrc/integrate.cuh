@@ -54,6 +54,8 @@ constexpr unsigned char kFlagActive = 1, kFlagEndStep = 2;
 struct KdkLeaf {
   int n;
   const int* id;
+  const int* slot_of;      // slot of each input index: scatters run in input order (coalesced
+                           // stores, random loads instead of random stores)
   double* f[kKeep];        // leaf-order fields matching keep[]
   double *h, *u;           // leaf-order h and u
   unsigned char* active;

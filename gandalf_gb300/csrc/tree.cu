@@ -474,10 +474,11 @@ __global__ void __launch_bounds__(kDeepThreads) k_build_deep(int L0, int ltot, B
 }
 
 __global__ void k_gather_leaf_order(int n, const int* __restrict__ perm, InputArrays in, Particles p,
-                                    int* id_out) {
+                                    int* id_out, int* slot_of) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const int i = perm[s];
     id_out[s] = i;
+    slot_of[i] = s;
     p.x[s] = in.x[i]; p.y[s] = in.y[i]; p.z[s] = in.z[i];
     p.vx[s] = in.vx[i]; p.vy[s] = in.vy[i]; p.vz[s] = in.vz[i];
     p.m[s] = in.m[i]; p.u[s] = in.u[i]; p.h[s] = in.h[i]; p.h0[s] = in.h[i];
@@ -759,7 +760,7 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
                                                    a.heap_first, a.heap_n, a.ibox);
     launches++;
   }
-  k_gather_leaf_order<<<grid_for(n, 256), 256, 0, st>>>(n, cur.l[0], a.in, a.p, a.id_out);
+  k_gather_leaf_order<<<grid_for(n, 256), 256, 0, st>>>(n, cur.l[0], a.in, a.p, a.id_out, a.slot_of);
   cudaMemsetAsync(a.tree.climb, 0, sizeof(unsigned) * (size_t) a.tree.ncell, st);
   k_stock<<<(a.tree.nleaf + 127) / 128, 128, 0, st>>>(a.tree, a.p, a.thetamaxsqd);
   return launches + 2;

@@ -47,6 +47,7 @@ struct BuildArgs {
   const int* heap_ones_before;
   Particles p;                  // leaf-ordered destination
   int* id_out;                  // input index of each slot
+  int* slot_of;                 // slot of each input index (the inverse permutation)
   Tree tree;
   double thetamaxsqd;
 };
