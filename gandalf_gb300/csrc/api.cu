@@ -68,6 +68,8 @@ struct gsph_ctx {
   unsigned long long* key2[3] = {};
   int* deep_inv = nullptr;
   int* slot_of = nullptr;                 // slot of each input particle (inverse of id)
+  int* dens_next = nullptr;               // FP64 h solve: leaf counter of its persistent warps
+  double2* dens_comp = nullptr;           // FP64 h solve: per-warp compact lists
   int *radix_hist = nullptr, *radix_tot = nullptr;
   unsigned char *side = nullptr, *seg_axis = nullptr;
   int* blocksum = nullptr;
@@ -256,6 +258,8 @@ int ensure_capacity(gsph_ctx* c, int n) {
     if (rc == GSPH_OK) rc = alloc(c, c->radix_tot, 3 * 256);
     if (rc == GSPH_OK) rc = alloc(c, c->deep_inv, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->slot_of, capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->dens_next, 1);
+    if (rc == GSPH_OK && c->cfg.precision != GSPH_PRECISION_MIXED) rc = alloc(c, c->dens_comp, density_fp64_scratch_entries());
     if (rc == GSPH_OK) rc = alloc(c, c->side, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->seg_axis, (capc + 1) / 2);
     if (rc == GSPH_OK) rc = alloc(c, c->blocksum, 3 * (size_t) partition_blocks(capn) + 3);
@@ -567,7 +571,7 @@ int do_props(gsph_ctx* c) {
                                                    c->stream);
   } else {
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count + 2, 0, 2 * sizeof(int), c->stream));
-    launch_density(t, p, make_params(c), make_counters(c), heavy, c->lpg, c->stream);
+    launch_density(t, p, make_params(c), make_counters(c), heavy, c->lpg, c->dens_next, c->dens_comp, c->stream);
     c->launches += 2;
   }
   int rc = check_launch(c, "density");

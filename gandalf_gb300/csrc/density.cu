@@ -24,7 +24,6 @@ namespace gsph {
 
 namespace {
 
-constexpr int kDensWarps = 1;          // warps per block (a block's slot frees when its leaf is done)
 constexpr int kDensStack = 1024;       // walk stack entries per warp
 constexpr int kDensList = 1024;        // gather-list entries per warp
 constexpr int kMaxAttempts = 256;      // attempts of the (skipping) hmax sequence
@@ -65,14 +64,19 @@ __device__ __forceinline__ void write_density(const Particles& p, const SphParam
   p.pressure[slot] = gm1 * rho_out * u;
 }
 
+// Per-lane compact lists of (|dr|^2, m) for the candidates inside 2 hmax_list, built once
+// per attempt in global scratch (one region per resident warp): every iteration then reads
+// the lane's own list instead of recomputing |dr|^2 of every candidate.  Each lane keeps
+// its candidates in the order it visits them, so the sums are the same, bit for bit, as
+// the rescanning form; a lane whose list overflows rescans.
+constexpr int kCompLane = 64;                              // entries per lane
+constexpr int kCompWarp = 32 * kCompLane;                  // double2 entries per warp
+constexpr int kDensResident = 152 * 16;                    // persistent warps (blocks)
+
 template <int LPG>
-__global__ void __launch_bounds__(kDensWarps * 32, 16 / kDensWarps)
-k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList heavy) {
-  __shared__ int s_stack[kDensWarps][kDensStack];
-  __shared__ int s_list[kDensWarps][kDensList];
-  const int wib = threadIdx.x >> 5;
-  const int leaf = blockIdx.x * kDensWarps + wib;
-  if (leaf >= t.nleaf) return;
+__device__ __forceinline__ void density_leaf_fp64(const Tree& t, const Particles& p, const SphParams& prm,
+                                                  const DeviceCounters& cnt, const HeavyList& heavy, int leaf,
+                                                  int* stack, int* list, double2* comp) {
   const int lane = threadIdx.x & 31;
   const int g = lane / LPG, sl = lane % LPG;
   const int c = t.leaf_cell[leaf];
@@ -84,8 +88,6 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList
   const double h_start = p.h[slot];
   const CellBox bb = t.bb[c];
   double hmax = t.geom[c].hmax;
-  int* stack = s_stack[wib];
-  int* list = s_list[wib];
   unsigned long long pairs = 0;
 
   // final per-particle results
@@ -138,6 +140,43 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList
     if (overflow && heavy.leaves) { gave_up = true; return false; }
     const int ncached = L.na;
 
+    // |dr|^2 exactly as the iteration computes it; every pair inside the kernel support
+    // of an h <= hmax_list has |dr|^2 < 4 hmax_list^2 (the margin covers the roundings)
+    int ncomp = 0;
+    if (!overflow && mine) {
+      const double lim = 4.0 * hmax_list * hmax_list * (1.0 + 1.0e-12);
+      for (int e = 0; e < ncached; e++) {
+        const int tagv = list[e];
+        const int node = tagv & ((1 << kNodeBits) - 1);
+        const int code = tagv >> kNodeBits;
+        const int f = t.cell_first[node], nn = t.cell_n[node];
+        const double sx = shift_of(code, 0, prm), sy = shift_of(code, 1, prm), sz = shift_of(code, 2, prm);
+        for (int q = sl; q < nn; q += LPG) {
+          const int j = f + q;
+          double xj = p.x[j], yj = p.y[j], zj = p.z[j];
+          if (code != kNoShift) {
+            const double glim = __dmul_rn(kGhostRange * kKernRange, p.h0[j]);
+            bool ok = true;
+            if (sx > 0.0) ok = ok && (xj < __dadd_rn(prm.boxmin[0], glim));
+            if (sx < 0.0) ok = ok && (xj > __dsub_rn(prm.boxmax[0], glim));
+            if (sy > 0.0) ok = ok && (yj < __dadd_rn(prm.boxmin[1], glim));
+            if (sy < 0.0) ok = ok && (yj > __dsub_rn(prm.boxmax[1], glim));
+            if (sz > 0.0) ok = ok && (zj < __dadd_rn(prm.boxmin[2], glim));
+            if (sz < 0.0) ok = ok && (zj > __dsub_rn(prm.boxmax[2], glim));
+            if (!ok) continue;
+            xj = __dadd_rn(xj, sx); yj = __dadd_rn(yj, sy); zj = __dadd_rn(zj, sz);
+          }
+          const double dx = xj - xi, dy = yj - yi, dz = zj - zi;
+          const double drsqd = dot3_rn(dx, dy, dz);
+          if (drsqd <= lim) {
+            if (ncomp < kCompLane) comp[(g * kCompLane + ncomp) * LPG + sl] = make_double2(drsqd, p.m[j]);
+            ncomp++;
+          }
+        }
+      }
+    }
+    const bool use_comp = !overflow && ncomp <= kCompLane;
+
     double hi = h_start, h_lower = 0.0, h_upper = hmax_list;
     double rho = 0.0, om = 0.0, zeta = 0.0;
     int iteration = 0;
@@ -184,7 +223,21 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList
           }
         }
       };
-      if (!overflow) {
+      if (use_comp) {
+        if (!done) {
+          for (int k = 0; k < ncomp; k++) {
+            const double2 v = comp[(g * kCompLane + k) * LPG + sl];
+            const double ssqd = invhsqd * v.x;
+            if (ssqd < kKernRangeSqd) {
+              const double s = sqrt(ssqd);
+              srho = fma(v.y, m4_w0(s), srho);
+              som = fma(v.y * invh, m4_womega(s), som);
+              sze = fma(v.y, m4_wzeta(s), sze);
+              pairs++;
+            }
+          }
+        }
+      } else if (!overflow) {
         consume(ncached);
       } else {
         L = WarpLists{list, list, list, 0, 0, 0, kDensList};
@@ -264,6 +317,25 @@ k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList
     if (lane == 0) atomicAdd(cnt.density_pairs, tot);
   }
   if (mine && sl == 0) write_density(p, prm, slot, h_out, rho_out, om_out, zeta_out, xi, yi, zi);
+}
+
+// Persistent warps (one per block) take leaves in depth-first order from a counter.
+template <int LPG>
+__global__ void __launch_bounds__(32, 16)
+k_density_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt, HeavyList heavy, int* next,
+               double2* scratch) {
+  __shared__ int s_stack[kDensStack];
+  __shared__ int s_list[kDensList];
+  double2* comp = scratch + (size_t) blockIdx.x * kCompWarp;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int leaf = 0;
+    if (lane == 0) leaf = atomicAdd(next, 1);
+    leaf = __shfl_sync(kFull, leaf, 0);
+    if (leaf >= t.nleaf) break;
+    density_leaf_fp64<LPG>(t, p, prm, cnt, heavy, leaf, s_stack, s_list, comp);
+    __syncwarp();
+  }
 }
 
 
@@ -450,17 +522,20 @@ __global__ void __launch_bounds__(256, 2) k_density_fp64_pp(Tree t, Particles p,
 
 }  // namespace
 
+size_t density_fp64_scratch_entries() { return (size_t) kDensResident * kCompWarp; }
+
 void launch_density(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
-                    const HeavyList& heavy, int lanes_per_particle, cudaStream_t st) {
+                    const HeavyList& heavy, int lanes_per_particle, int* next, double2* scratch, cudaStream_t st) {
   cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
-  const int blocks = (t.nleaf + kDensWarps - 1) / kDensWarps;
+  cudaMemsetAsync(next, 0, sizeof(int), st);
+  const int blocks = kDensResident < t.nleaf ? kDensResident : t.nleaf;
   switch (lanes_per_particle) {
-    case 32: k_density_fp64<32><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
-    case 16: k_density_fp64<16><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
-    case 8: k_density_fp64<8><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
-    case 4: k_density_fp64<4><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
-    case 2: k_density_fp64<2><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
-    default: k_density_fp64<1><<<blocks, kDensWarps * 32, 0, st>>>(t, p, prm, cnt, heavy); break;
+    case 32: k_density_fp64<32><<<blocks, 32, 0, st>>>(t, p, prm, cnt, heavy, next, scratch); break;
+    case 16: k_density_fp64<16><<<blocks, 32, 0, st>>>(t, p, prm, cnt, heavy, next, scratch); break;
+    case 8: k_density_fp64<8><<<blocks, 32, 0, st>>>(t, p, prm, cnt, heavy, next, scratch); break;
+    case 4: k_density_fp64<4><<<blocks, 32, 0, st>>>(t, p, prm, cnt, heavy, next, scratch); break;
+    case 2: k_density_fp64<2><<<blocks, 32, 0, st>>>(t, p, prm, cnt, heavy, next, scratch); break;
+    default: k_density_fp64<1><<<blocks, 32, 0, st>>>(t, p, prm, cnt, heavy, next, scratch); break;
   }
   const int gpp = 2 * 152;
   switch (lanes_per_particle) {

@@ -45,9 +45,11 @@ int launch_hydro_mixed(const Tree& t, const Particles& p, const MixedParticles& 
                        const SphParams& prm, const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st);
 
 // FP64 h solve; leaves whose gather list does not fit one warp go to a heavy-leaf kernel
-// through `heavy` (count zeroed here).  Returns nothing; launches two kernels.
+// through `heavy` (count zeroed here).  `next` is a leaf counter (zeroed here) and
+// `scratch` holds density_fp64_scratch_entries() double2.  Launches two kernels.
+size_t density_fp64_scratch_entries();
 void launch_density(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
-                    const HeavyList& heavy, int lanes_per_particle, cudaStream_t st);
+                    const HeavyList& heavy, int lanes_per_particle, int* next, double2* scratch, cudaStream_t st);
 void launch_hydro_forces(const Tree& t, const Particles& p, const SphParams& prm,
                          const DeviceCounters& cnt, int lanes_per_particle, cudaStream_t st);
 void launch_all_forces(const Tree& t, const Particles& p, const SphParams& prm,
