@@ -79,6 +79,7 @@ __global__ void k_prep_hydro_particles(Particles p, MixedParticles mp) {
                             __double2float_rn(p.sound[s]));
     mp.aux[s] = make_float4(__double2float_rn(p.hfactor[s]), __double2float_rn(p.zeta[s]),
                             __double2float_rn(p.hrangesqd[s]), 0.0f);
+    mp.pos_lo[s].w = __double2float_rn(p.hrangesqd[s]);   // the neighbour test's candidate load
   }
 }
 
@@ -1161,7 +1162,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
         const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
         const float d2 = dx * dx + dy * dy + dz * dz;
-        if (sph_member(p, T, j, d2, mp.aux[j].z, prm, exact)) {
+        if (sph_member(p, T, j, d2, pjl.w, prm, exact)) {
           hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
           lvn_pair(p, slot, j, lvn_own);
           nsph++;
@@ -1412,7 +1413,7 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
           if ((sh[0] | sh[1] | sh[2]) && !ghost_exists(prm, p, j, sh)) continue;
         }
         const float d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        if (!sph_member(p, T, j, d2, mp.aux[j].z, prm, exact)) continue;
+        if (!sph_member(p, T, j, d2, pjl.w, prm, exact)) continue;
         hydro_pair_f(prm, mp, T, j, d[0], d[1], d[2], d2, pjh.w, A);
         lvn_pair(p, slot, j, lvn_own);
         npairs++;

@@ -14,7 +14,7 @@ namespace gsph {
 
 struct MixedParticles {
   float4* pos_hi;   // x_hi y_hi z_hi m
-  float4* pos_lo;   // x_lo y_lo z_lo 0
+  float4* pos_lo;   // x_lo y_lo z_lo, hrangesqd (0 until the h solve)
   float4* vel;      // vx vy vz h
   float4* hyd;      // 1/h  P*invomega/rho^2  1/rho  sound
   float4* aux;      // hfactor zeta hrangesqd 0
