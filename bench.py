@@ -47,7 +47,7 @@ FLOPS = dict(density=42, hydro=80, hydro_grav=145, direct=24, quad=82, mono=24)
 
 # DRAM bytes (read + write) per force pass, from one-pass ncu captures of the force kernels
 # (profiles/forces_density_mixed_plummer262k_dram.md): (workload, n, form) -> bytes.
-FORCE_TRAFFIC = {("plummer_sphere", 262144, "mixed"): 49.09e6 + 0.697e6 + 5.79e6}
+FORCE_TRAFFIC = {("plummer_sphere", 262144, "mixed"): 45.65e6 + 0.55e6 + 5.15e6}
 
 
 def max_over_ranks(ms, world, device="cuda"):
