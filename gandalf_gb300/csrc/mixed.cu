@@ -1611,7 +1611,9 @@ int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles
   const size_t smem_n = dens_smem(1);
   (void) max_leaf;
   GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, t.nleaf, 32, smem_n, t, p, mp, mc, prm, cnt, heavy, true)
-  GSPH_MIXED_LPG(k_density_mixed_pp, lanes_per_particle, 2 * 152, 256, 0, t, p, mp, mc, prm, cnt, heavy)
+  // 41 KB of shared memory a block: up to 5 blocks an SM; 4 per SM keep the heavy leaves
+  // (a few percent of all) spread over every SM
+  GSPH_MIXED_LPG(k_density_mixed_pp, lanes_per_particle, 4 * 152, 256, 0, t, p, mp, mc, prm, cnt, heavy)
   return 2;
 }
 

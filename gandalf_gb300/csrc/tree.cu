@@ -525,7 +525,10 @@ __device__ void stock_leaf(const Tree& t, const Particles& p, int c, double thet
       hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
     }
   }
-  if (m > 0.0) for (int k = 0; k < 3; k++) r[k] /= m;
+  if (m > 0.0) {
+    const double im = 1.0 / m;   // one division for the three components
+    for (int k = 0; k < 3; k++) r[k] *= im;
+  }
   CellGeom g;
   finish_geometry(n, bmin, bmax, hmax, theta2, g);
   double q[5] = {0, 0, 0, 0, 0};
@@ -586,7 +589,10 @@ __device__ void stock_parent(const Tree& t, int c, int level, double theta2) {
   const int n = n1 + n2;
   const double m = cm[0] + cm[1];
   double r[3] = {0.0, 0.0, 0.0};
-  if (m > 0.0) for (int k = 0; k < 3; k++) r[k] = (cm[0] * cr[0][k] + cm[1] * cr[1][k]) / m;
+  if (m > 0.0) {
+    const double im = 1.0 / m;
+    for (int k = 0; k < 3; k++) r[k] = (cm[0] * cr[0][k] + cm[1] * cr[1][k]) * im;
+  }
   CellGeom g;
   finish_geometry(n, bmin, bmax, hmax, theta2, g);
   double q[5] = {0, 0, 0, 0, 0};
