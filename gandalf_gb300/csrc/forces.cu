@@ -120,10 +120,12 @@ __device__ __forceinline__ void hydro_grav_pair(const SphParams& prm, const Part
   const double mj = p.m[j];
   const double paux = pair_pressure(prm, T, wi, wj, facj, invrhoj, p.sound[j], mj, dvdr, A.dudt);
   A.ah[0] += mj * ux * paux; A.ah[1] += mj * uy * paux; A.ah[2] += mj * uz * paux;
-  const double pg = 0.5 * (T.invh * T.invh * m4_wgrav(si) + T.zeta * wi + invhj * invhj * m4_wgrav(sj) +
-                           p.zeta[j] * wj);
+  // 1/s = h / |r|
+  const double isi = T.h * invdrmag, isj = hj * invdrmag;
+  const double pg = 0.5 * (T.invh * T.invh * m4_wgrav_r(si, isi) + T.zeta * wi +
+                           invhj * invhj * m4_wgrav_r(sj, isj) + p.zeta[j] * wj);
   A.ag[0] += mj * ux * pg; A.ag[1] += mj * uy * pg; A.ag[2] += mj * uz * pg;
-  A.gpot += 0.5 * mj * (T.invh * m4_wpot(si) + invhj * m4_wpot(sj));
+  A.gpot += 0.5 * mj * (T.invh * m4_wpot_r(si, isi) + invhj * m4_wpot_r(sj, isj));
   A.divv -= mj * dvdr * wi;
 }
 
