@@ -53,7 +53,7 @@ struct gsph_ctx {
   int ltot = 0, ncell = 0, nleaf = 0, P = 0, lpg = 4;
   // device arrays
   double* in[9] = {};        // x y z vx vy vz m u h (input order)
-  double* f[27] = {};        // leaf-order fields (see kF* below)
+  double* f[30] = {};        // leaf-order fields (see kF* below)
   int* id = nullptr;
   int *cell_first = nullptr, *cell_n = nullptr, *cell_parent = nullptr, *leaf_cell = nullptr;
   unsigned char* cell_level = nullptr;
@@ -132,8 +132,9 @@ namespace {
 enum {
   kFX = 0, kFY, kFZ, kFVX, kFVY, kFVZ, kFM, kFU, kFH, kFH0, kFRho, kFInvOmega, kFZeta, kFHfactor,
   kFHrangesqd, kFPressure, kFSound, kFAX, kFAY, kFAZ, kFAGX, kFAGY, kFAGZ, kFGpot, kFDudt, kFDivV,
-  kFGpotHydro, kNumFields
+  kFGpotHydro, kFInvH, kFInvRho, kFFac, kNumFields
 };
+static_assert(kNumFields == 30, "gsph_ctx::f holds kNumFields pointers");
 
 int fail(gsph_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -358,6 +359,7 @@ Particles make_particles(gsph_ctx* c) {
   p.hrangesqd = f[kFHrangesqd]; p.pressure = f[kFPressure]; p.sound = f[kFSound];
   p.ax = f[kFAX]; p.ay = f[kFAY]; p.az = f[kFAZ]; p.agx = f[kFAGX]; p.agy = f[kFAGY]; p.agz = f[kFAGZ];
   p.gpot = f[kFGpot]; p.dudt = f[kFDudt]; p.div_v = f[kFDivV]; p.gpot_hydro = f[kFGpotHydro];
+  p.invh_p = f[kFInvH]; p.invrho_p = f[kFInvRho]; p.fac_p = f[kFFac];
   if (c->kdk) { p.active = c->leaf_active; p.level = c->leaf_level; p.lvn = c->leaf_lvn; }
   return p;
 }
@@ -617,7 +619,7 @@ int do_forces(gsph_ctx* c, bool gravity) {
   } else {
     if (gravity) launch_all_forces(t, p, make_params(c), make_counters(c), c->lpg, c->stream);
     else launch_hydro_forces(t, p, make_params(c), make_counters(c), c->lpg, c->stream);
-    c->launches += 1;
+    c->launches += 2;
   }
   // star gravity on the gas, after gpot_hydro is taken (GradhSphTree.cpp:596-606)
   c->launches += (unsigned) (mixed(c) ? launch_gas_from_stars_mixed(p, make_mixed_particles(c), make_stars(c), c->stream)

@@ -88,9 +88,10 @@ __device__ __forceinline__ double pair_pressure(const SphParams& prm, const Targ
 // GradhSph::ComputeSphHydroForces, one pair (src/GradhSph/GradhSph.cpp:384-447).
 __device__ __forceinline__ void hydro_pair(const SphParams& prm, const Particles& p, const Target& T, int j,
                                            double dx, double dy, double dz, double drsqd, Acc& A) {
-  const double hj = p.h[j], rhoj = p.rho[j];
-  const double invhj = 1.0 / hj, invrhoj = 1.0 / rhoj;
-  const double facj = (p.pressure[j] * p.invomega[j]) / (rhoj * rhoj);
+  // the neighbour's quotients, computed once per particle (the same IEEE results as here)
+  const double hj = p.h[j];
+  const double invhj = p.invh_p[j], invrhoj = p.invrho_p[j];
+  const double facj = p.fac_p[j];
   const double drmag = sqrt(drsqd);
   double ux = dx, uy = dy, uz = dz;
   if (drmag > 0.0) { const double inv = 1.0 / drmag; ux *= inv; uy *= inv; uz *= inv; }
@@ -107,9 +108,10 @@ __device__ __forceinline__ void hydro_pair(const SphParams& prm, const Particles
 // GradhSph::ComputeSphHydroGravForces, one pair (src/GradhSph/GradhSph.cpp:498-571).
 __device__ __forceinline__ void hydro_grav_pair(const SphParams& prm, const Particles& p, const Target& T,
                                                 int j, double dx, double dy, double dz, double drsqd, Acc& A) {
-  const double hj = p.h[j], rhoj = p.rho[j];
-  const double invhj = 1.0 / hj, invrhoj = 1.0 / rhoj;
-  const double facj = (p.pressure[j] * p.invomega[j]) / (rhoj * rhoj);
+  // the neighbour's quotients, computed once per particle (the same IEEE results as here)
+  const double hj = p.h[j];
+  const double invhj = p.invh_p[j], invrhoj = p.invrho_p[j];
+  const double facj = p.fac_p[j];
   const double drmag = sqrt(drsqd + kSmall);
   const double invdrmag = 1.0 / drmag;
   const double ux = dx * invdrmag, uy = dy * invdrmag, uz = dz * invdrmag;
@@ -398,14 +400,36 @@ k_all_forces_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
     default: KERNEL<1><<<blocks, kForceWarps * 32, 0, st>>>(__VA_ARGS__); break;     \
   }
 
+namespace {
+
+// Per-particle quotients every pair of the FP64 force pass needs from its neighbour
+// (GradhSph.cpp:398-402, :509-515 evaluate them per pair).
+__global__ void k_pair_quotients_fp64(Particles p) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < p.n; s += gridDim.x * blockDim.x) {
+    const double rho = p.rho[s];
+    p.invh_p[s] = 1.0 / p.h[s];
+    p.invrho_p[s] = 1.0 / rho;
+    p.fac_p[s] = (p.pressure[s] * p.invomega[s]) / (rho * rho);
+  }
+}
+
+void launch_pair_quotients(const Particles& p, cudaStream_t st) {
+  const int blocks = (p.n + 255) / 256 < 152 * 8 ? (p.n + 255) / 256 : 152 * 8;
+  k_pair_quotients_fp64<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p);
+}
+
+}  // namespace
+
 void launch_hydro_forces(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
                          int lanes_per_particle, cudaStream_t st) {
+  launch_pair_quotients(p, st);
   const int blocks = (t.nleaf + kForceWarps - 1) / kForceWarps;
   GSPH_DISPATCH_LPG(k_hydro_fp64, lanes_per_particle, t, p, prm, cnt)
 }
 
 void launch_all_forces(const Tree& t, const Particles& p, const SphParams& prm, const DeviceCounters& cnt,
                        int lanes_per_particle, cudaStream_t st) {
+  launch_pair_quotients(p, st);
   const int blocks = (t.nleaf + kForceWarps - 1) / kForceWarps;
   GSPH_DISPATCH_LPG(k_all_forces_fp64, lanes_per_particle, t, p, prm, cnt)
 }

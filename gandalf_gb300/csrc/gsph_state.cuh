@@ -33,6 +33,7 @@ struct Particles {
   double *rho, *invomega, *zeta, *hfactor, *hrangesqd, *pressure, *sound;
   double *ax, *ay, *az, *agx, *agy, *agz, *gpot, *dudt, *div_v;
   double* gpot_hydro;         // gpot before the star terms (written only with stars)
+  double *invh_p, *invrho_p, *fac_p;   // FP64 force pass: 1/h, 1/rho, P Omega^-1 / rho^2 per slot
   // block timesteps (nullptr when every particle is active and levels are not tracked)
   const unsigned char* active;   // per slot: 1 = the h solve and forces are computed
   const int* level;              // per slot: timestep level
