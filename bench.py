@@ -253,8 +253,8 @@ def kdk_main(args, rank, world, local):
     """Rotating isothermal cloud (uniform sphere, m = 2 perturbation, solid-body rotation),
     N = 1,048,576, self-gravity theta = 0.5 quadrupole, 4 block-timestep levels: K KDK main
     loop steps (default 20) replayed from one CUDA graph, FP64 and mixed forms.  The unit
-    of work is one active particle through one force pass (SURVEY metric for block-timestep
-    configurations)."""
+    of work is one active particle through one force pass (the metric's unit for
+    block-timestep configurations: active particles per KDK substep)."""
     import torch
     from gandalf_gb300 import ics as ics_mod
     from gandalf_gb300 import _native
