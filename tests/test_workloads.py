@@ -99,3 +99,17 @@ def test_kh_ensemble_sizes():
     assert len(boxes) == 64
     assert sizes.min() >= 4096 and sizes.max() <= 131072
     assert 1.5e6 < sizes.sum() < 2.7e6
+
+
+def test_leaf_size_tuner_reuses_its_cache(tmp_path):
+    """A cached result for the same (N, precision, gravity, periodic) is returned without
+    timing anything (no GPU needed)."""
+    import json
+    from gandalf_gb300.autotune import tune_leaf_size
+    c = ics_mod.periodic_cube(1000, seed=1)
+    params = c.pop("params")
+    key = f"1000:mixed:{params['self_gravity']}:{params['periodic']}"
+    cached = {"nleafmax": 12, "ms_per_step": {"8": 2.0, "12": 1.5}}
+    path = tmp_path / "tune.json"
+    path.write_text(json.dumps({key: cached}))
+    assert tune_leaf_size(c, params, precision="mixed", cache=str(path)) == cached
