@@ -70,3 +70,46 @@ def test_float_membership_with_margin_never_contradicts_fp64():
     assert not np.any(no & member64)
     # the margin band (fp64 re-check) takes a small fraction even of these near-boundary pairs
     assert np.mean(~(yes | no)) < 0.5
+
+
+def test_float_walk_decisions_with_margin_never_contradict_fp64():
+    """The gravity walk's near test and MAC of the mixed form: float values with a 2^-14
+    margin (fp64 re-test inside it) agree with the fp64 decisions of the reference's walk
+    wherever the float test decides."""
+    margin = 2.0 ** -14
+    rng = np.random.default_rng(41)
+    n = 300000
+    rc_leaf = rng.uniform(-3.0, 3.0, (n, 3))
+    rmax_leaf = 10.0 ** rng.uniform(-3, -1, n)
+    rmax_c = rmax_leaf * 10.0 ** rng.uniform(0, 1.5, n)
+    hmax_leaf = rmax_leaf * rng.uniform(0.5, 2.0, n)
+    hmax_c = rmax_c * rng.uniform(0.1, 1.0, n)
+    cdist = np.maximum(rmax_c ** 2, hmax_c ** 2) / 0.25
+    # cell centres near either boundary
+    target = np.where(rng.random(n) < 0.5,
+                      np.maximum(rmax_c + rmax_leaf + 2.0 * hmax_leaf, rmax_leaf + rmax_c + 2.0 * hmax_c),
+                      np.sqrt(cdist))
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    rc_c = rc_leaf + u * (target * (1.0 + rng.normal(0.0, 3e-4, n)))[:, None]
+    d64 = rc_c - rc_leaf
+    drsqd = np.einsum("ij,ij->i", d64, d64)
+    t1 = (rmax_c + rmax_leaf + 2.0 * hmax_leaf) ** 2
+    t2 = (rmax_leaf + rmax_c + 2.0 * hmax_c) ** 2
+    near64 = (drsqd <= t1) | (drsqd <= t2)
+    open64 = drsqd < cdist
+    hi_a, lo_a = split(rc_leaf)
+    hi_b, lo_b = split(rc_c)
+    d32 = (hi_b - hi_a) + (lo_b - lo_a)
+    d2 = np.einsum("ij,ij->i", d32, d32).astype(np.float32)
+    f = lambda a: a.astype(np.float32)
+    a1 = f(rmax_c) + f(rmax_leaf) + np.float32(2.0) * f(hmax_leaf)
+    a2 = f(rmax_leaf) + f(rmax_c) + np.float32(2.0) * f(hmax_c)
+    thr = np.maximum(a1 * a1, a2 * a2)
+    near_yes = d2 < thr * np.float32(1.0 - margin)
+    near_no = d2 > thr * np.float32(1.0 + margin)
+    assert not np.any(near_yes & ~near64) and not np.any(near_no & near64)
+    cd = f(cdist)
+    open_yes = d2 < cd * np.float32(1.0 - margin)
+    open_no = d2 > cd * np.float32(1.0 + margin)
+    assert not np.any(open_yes & ~open64) and not np.any(open_no & open64)
