@@ -128,9 +128,11 @@ __device__ __forceinline__ double shift_of(int code, int k, const SphParams& prm
 // ==========================================================================================
 // Density / h solve, mixed form.
 //
-// One cell's solve, shared by the warp kernel (WARPS = 1) and the wide kernel (WARPS = 8,
-// the cell's candidate leaves dealt round-robin to the warps; per-iteration sums are
-// combined across warps in shared memory, in warp order).
+// One cell's solve by one warp (WARPS = 1), shared by the single-simulation and the batch
+// kernels.  The template also carries a block-wide form (WARPS warps share one cell, its
+// candidate leaves dealt round-robin, per-iteration sums combined in warp order in shared
+// memory) that no kernel instantiates at present: leaves too large for one warp go to the
+// per-particle heavy-leaf kernel instead.
 // ==========================================================================================
 constexpr int kDensStack = 1024;
 constexpr int kDensListNormal = 256;    // leaves a warp handles alone
