@@ -1,6 +1,6 @@
-// Mixed-precision form of the per-leaf kernels: fp32 pair arithmetic, fp64 positions,
-// fp64 h-rho iteration logic, fp64 cell moments (kept as float hi/lo pairs for the
-// pair loops), and interaction lists identical to the fp64 form.
+// Mixed-precision form of the per-leaf kernels: fp32 pair arithmetic and h-rho iteration
+// (the heavy-leaf kernel iterates in fp64), fp64 positions and cell moments (kept as float
+// hi/lo pairs for the pair loops), and interaction lists identical to the fp64 form.
 //
 // Pair formulas are those of the fp64 kernels (density.cu, forces.cu; reference
 // src/GradhSph/GradhSph.cpp:141-690, src/Headers/NeighbourSearch.h:423-449) evaluated in
@@ -10,10 +10,11 @@
 // arithmetic when the float value lands inside the margin, so the lists are the fp64
 // lists exactly.
 //
-// Load balance: the warp-per-leaf kernels hand a leaf over to a wide kernel when its
-// lists outgrow the warp's shared memory (density: the gather list; forces: the near or
-// direct-sum list).  The wide kernels give such a leaf a whole block — density: 8 warps
-// share the candidates of the cell; forces: one warp per particle.
+// Load balance: the warp-per-leaf kernels hand a leaf over to a heavy-leaf kernel when its
+// lists outgrow the warp's shared memory (density: the gather list or a particle's
+// compact list; forces: the near or direct-sum list).  The heavy-leaf kernels give such a
+// leaf a whole block — density: one warp per particle, each iteration walking the tree
+// for the particle's own 2h box; forces: 8 warps sharing the leaf's lists round-robin.
 #include "gsph_state.cuh"
 #include "gsph_walk.cuh"
 #include "kernels.cuh"
@@ -531,7 +532,7 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   double hk = __dmul_rn(1.05, hmax0);
   for (int a = 0; a < kMaxAttempts && !solved; a++) {
     const int r = attempt(hk);
-    if (r == 2) return false;   // handed over to the wide kernel
+    if (r == 2) return false;   // handed over to the heavy-leaf kernel
     if (r == 0) {
       solved = true;
     } else {

@@ -33,7 +33,7 @@ struct MixedCells {
   float4* hbmax;
 };
 
-// Leaves the warp-per-leaf kernels hand over to the wide kernels.
+// Leaves the warp-per-leaf kernels hand over to the heavy-leaf kernels.
 struct HeavyList {
   int* leaves;      // leaf indices
   int* count;       // device counter
