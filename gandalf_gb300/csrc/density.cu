@@ -1,4 +1,4 @@
-// Grad-h density and smoothing-length solve, one warp per leaf cell.
+// Grad-h density and smoothing-length solve, one warp per leaf cell (fp64 form).
 //
 // Reference: GradhSphTree::UpdateAllSphProperties (src/GradhSph/GradhSphTree.cpp:82-271)
 // drives, per active leaf cell, the gather walk Tree::ComputeGatherNeighbourList
@@ -8,8 +8,11 @@
 // lanes of a group split the candidate particles and reduce their sums with xor
 // shuffles, so every lane of a group holds the same totals and runs the reference's
 // scalar iteration logic in lock step.  The gather list (leaf cells overlapping the
-// gather box, tagged with a periodic-image code) is staged in shared memory; if it does
-// not fit, every iteration re-walks the tree and consumes the list in chunks instead.
+// gather box, tagged with a periodic-image code) is staged in shared memory; a leaf
+// whose list does not fit goes to the per-particle heavy-leaf kernel.  Each lane keeps
+// (|r_ij|^2, m_j) of its candidates inside 2 hmax in its own compact list in global
+// scratch, built once per attempt, and the iterations read it.  The warps are
+// persistent and take leaves in depth-first order from a counter.
 //
 // The reference's retry protocol is kept: when any particle's h exceeds the cell's
 // hmax (times 1.05 per attempt) the whole cell restarts from the input h with a 5 %
