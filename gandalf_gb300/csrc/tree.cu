@@ -812,10 +812,13 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-// Device address of g_noalloc_scratch, looked up once per device (host code cannot use
-// the symbol itself as a device pointer).
+// Device address of g_noalloc_scratch and the SM count, looked up once per device (host
+// code cannot use the symbol itself as a device pointer).  The cached address belongs to
+// the context that was current at the lookup (the device's primary context); after a
+// cudaDeviceReset, or with another context made current, it no longer names the array.
 constexpr int kNaMaxDevices = 64;
 NoAllocScratch* g_noalloc_ptr[kNaMaxDevices] = {};
+int g_noalloc_sms[kNaMaxDevices] = {};
 
 // Heap-indexed segment tables of level l (block l): first, count and the number of
 // second-child positions before each segment.
@@ -859,18 +862,26 @@ extern "C" int32_t gsph_kdtree_order_noalloc(const double* x, const double* y, c
   int ltot = 0;
   while ((double) nleafmax * (double) (1 << ltot) < (double) n && ltot <= kNaMaxLtot) ltot++;
   if (n > kNaMaxN || ltot > kNaMaxLtot) return -6;                          // GSPH_ERR_CAPACITY
+  // an error left pending by the caller's earlier work is reported, not taken as ours
+  // (and not cleared: it stays for the caller to read)
+  if (cudaPeekAtLastError() != cudaSuccess) return -2;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return -2;
   if (!g_noalloc_ptr[dev]) {
     NoAllocScratch* p = nullptr;
     if (cudaGetSymbolAddress((void**) &p, g_noalloc_scratch) != cudaSuccess || !p) return -2;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return -2;
+    g_noalloc_sms[dev] = sms;
     g_noalloc_ptr[dev] = p;
   }
   NoAllocScratch* s = g_noalloc_ptr[dev];
+  const int sms = g_noalloc_sms[dev];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   k_noalloc_heap_tables<<<ltot + 1, 1024, 0, st>>>(n, s);
+  if (cudaGetLastError() != cudaSuccess) return -2;   // a bad stream fails here, before more work
   k_root_box_init<<<1, 32, 0, st>>>(s->rootkey);
-  k_root_box<<<grid_for(n, 256, 152 * 4), 256, 0, st>>>(x, y, z, h, n, s->rootkey);
+  k_root_box<<<grid_for(n, 256, sms * 4), 256, 0, st>>>(x, y, z, h, n, s->rootkey);
   k_root_box_store<<<1, 32, 0, st>>>(s->rootkey, s->ibox);
   SortArrays sa;
   for (int q = 0; q < 3; q++) { sa.key[q] = s->key[q]; sa.idx[q] = s->idx[q]; }

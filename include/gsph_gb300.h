@@ -263,7 +263,13 @@ int32_t gsph_get_tree(gsph_ctx* ctx, int32_t* cell_n, int32_t* cell_first, int32
  *   overlaps on the GPU race; serialise them (one stream, or events).  Each call fully
  *   rewrites the scratch it reads, so nothing left by a previous call leaks into a result.
  *   Set-up: the first call on each device (with that device current) looks up the
- *   array's device address; make that first call before any stream capture.
+ *   array's device address and the SM count; make that first call before any stream
+ *   capture.  The address is cached per device for the process: it belongs to the context
+ *   current at that first call (the primary context), so do not use this entry point after
+ *   cudaDeviceReset or with another context current on that device.
+ *   Errors: a CUDA error left pending by the caller's earlier work makes the call return
+ *   GSPH_ERR_CUDA before it launches anything (the error is left for the caller to read);
+ *   a launch failure of this call's own work returns GSPH_ERR_CUDA.
  *   Limits: 1 <= n <= GSPH_NOALLOC_MAX_N and a tree of at most 13 levels
  *   (Nleafmax * 2^13 >= n).  Larger requests return GSPH_ERR_CAPACITY; bad pointers or
  *   sizes GSPH_ERR_INVALID; CUDA failures GSPH_ERR_CUDA. */

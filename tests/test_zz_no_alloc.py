@@ -21,8 +21,8 @@ pytestmark = pytest.mark.gpu
 MAX_N = 32768
 
 
-def regular_order(c):
-    t = GradhSphTree(c["params"])
+def regular_order(c, nleafmax=8):
+    t = GradhSphTree(c["params"], nleafmax=nleafmax)
     t.set_particles(c)
     t.BuildTree()
     order = t.tree()["order"]
@@ -56,6 +56,20 @@ def test_noalloc_order_matches_regular_build_twice():
             assert np.array_equal(got, want)
 
 
+def test_noalloc_order_at_the_depth_limit():
+    """Nleafmax 1 and 8,192 particles: a 13-level tree, the deepest the fixed scratch
+    holds (heap indices up to 16,382, 4,096 segments on the last level)."""
+    import torch
+    torch.cuda.init()
+    lib = _native.load()
+    c = ics_mod.plummer_sphere(8192, seed=35)
+    want = regular_order(c, nleafmax=1)
+    for _ in range(2):
+        rc, got = noalloc_order(lib, c, nleafmax=1)
+        assert rc == 0
+        assert np.array_equal(got, want)
+
+
 def test_noalloc_rejects_sizes_beyond_its_limit():
     import torch
     torch.cuda.init()
@@ -64,6 +78,10 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
     rc, got = noalloc_order(lib, c)
     assert rc == -6                             # GSPH_ERR_CAPACITY
     assert np.all(got == -1)                    # nothing was written
+    c = ics_mod.plummer_sphere(8193, seed=36)     # within the particle limit, but 14 levels
+    rc, got = noalloc_order(lib, c, nleafmax=1)
+    assert rc == -6
+    assert np.all(got == -1)
     c = ics_mod.plummer_sphere(1000, seed=34)
     rc, _ = noalloc_order(lib, c, nleafmax=0)
     assert rc == -1                             # GSPH_ERR_INVALID
