@@ -1,6 +1,6 @@
-// Mixed-precision form of the per-leaf kernels: fp32 pair arithmetic and h-rho iteration
-// (the heavy-leaf kernel iterates in fp64), fp64 positions and cell moments (kept as float
-// hi/lo pairs for the pair loops), and interaction lists identical to the fp64 form.
+// Mixed-precision form of the per-leaf kernels: fp32 pair arithmetic and kernel sums, an
+// fp64 h-rho iteration state and convergence test, fp64 positions and cell moments (kept
+// as float hi/lo pairs for the pair loops), and interaction lists identical to the fp64 form.
 //
 // Pair formulas are those of the fp64 kernels (density.cu, forces.cu; reference
 // src/GradhSph/GradhSph.cpp:141-690, src/Headers/NeighbourSearch.h:423-449) evaluated in
@@ -186,47 +186,6 @@ __device__ __forceinline__ void h_update(double drho, double dom, double dze, do
     invh = 1.0 / hi;
   }
   mloc = fmax(mloc, hi);
-  if (hi > hmax_list) { abort_cell = true; done = true; }
-  else if (!(hi > h_lower && hi < h_upper)) done = true;
-}
-
-// h_update in single precision, for the warp kernel of the mixed form: the same steps,
-// with the float reciprocal cube root used as it is (relative error ~1e-7, far inside
-// the form's 1e-4 tolerance).  Double-precision arithmetic runs at 1/64 of the float
-// rate on this GPU, so the fp64 form of this step costs as much as the pair sums.
-__device__ __forceinline__ void h_update_f(float drho, float dom, float dze, float inv_m, float inv_hfac,
-                                           float invhsqd, float hmax_list, float h_fac, float h_converge,
-                                           int iteration, float& hi, float& invh, float& h_lower, float& h_upper,
-                                           float& hrho_last, float& rho, float& om, float& zeta, float& mloc,
-                                           bool& done, bool& abort_cell, bool& fail) {
-  const float hfac3 = invh * invhsqd;
-  rho = drho * hfac3;
-  om = dom * hfac3;
-  zeta = dze * invhsqd;
-  const float w = drho * inv_m;
-  const float r = rcbrtf(w);
-  const float hrho = h_fac * hi * r;
-  hrho_last = hrho;
-  if (rho > 0.0f && hi > h_lower && fabsf(hi - hrho) * invh < h_converge) {
-    done = true;
-    return;
-  }
-  if (iteration < 30) {
-    invh = invh * (w * r * r) * inv_hfac;   // 1 / hrho
-    hi = hrho;
-  } else {
-    if (iteration == 30) hi = 0.5f * (h_lower + h_upper);
-    else if (iteration < 150) {
-      if (rho < (float) kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
-      hi = 0.5f * (h_lower + h_upper);
-    } else {
-      fail = true;
-      done = true;
-      return;
-    }
-    invh = 1.0f / hi;
-  }
-  mloc = fmaxf(mloc, hi);
   if (hi > hmax_list) { abort_cell = true; done = true; }
   else if (!(hi > h_lower && hi < h_upper)) done = true;
 }
@@ -445,21 +404,22 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     if (give_up && __any_sync(kFull, mine && !overflow && ccount > kcap)) return 2;
     const bool use_compact = !overflow && ccount <= kcap;
 
-    float hi = (float) h_start, h_lower = 0.0f, h_upper = (float) hmax_list;
-    float invh = 1.0f / hi, hrho_last = hi;
-    const float inv_m = (float) (1.0 / mi), inv_hfac = (float) (1.0 / prm.h_fac);
-    const float h_fac_f = (float) prm.h_fac, h_conv_f = (float) prm.h_converge, hmax_list_f = (float) hmax_list;
-    float rho = 0.0f, om = 0.0f, zeta = 0.0f;
+    // The iteration state (h, its bracket, the h(rho) target) and the convergence test are
+    // fp64, as in the reference (GradhSph.cpp:206-254); the kernel sums are float.
+    double hi = h_start, h_lower = 0.0, h_upper = hmax_list;
+    double invh = 1.0 / hi, hrho_last = hi;
+    const double inv_m = 1.0 / mi, inv_hfac = 1.0 / prm.h_fac;
+    double rho = 0.0, om = 0.0, zeta = 0.0;
     int iteration = 0;
     bool done = !mine, abort_cell = false;
-    float mloc = 0.0f;
+    double mloc = 0.0;
     for (;;) {
       bool any_active = __any_sync(kFull, !done);
       if (WARPS > 1) any_active = __syncthreads_or(any_active);
       if (!any_active) break;
       iteration++;
-      const float invhsqd = invh * invh;
-      const float invh_f = invh, invhsqd_f = invhsqd;
+      const double invhsqd = invh * invh;
+      const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
       float srho = 0.0f, som = 0.0f, sze = 0.0f;
       auto add = [&](float d2, float mj) {
         const float ssqd = d2 * invhsqd_f;
@@ -511,17 +471,16 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         __syncthreads();
       }
       if (!done)
-        h_update_f(drho, dom, dze, inv_m, inv_hfac, invhsqd, hmax_list_f, h_fac_f, h_conv_f, iteration, hi, invh,
-                   h_lower, h_upper, hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
+        h_update((double) drho, (double) dom, (double) dze, inv_m, inv_hfac, invhsqd, hmax_list, prm, iteration, hi,
+                 invh, h_lower, h_upper, hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
     }
-    float mwf = mloc;
-    for (int o = 16; o > 0; o >>= 1) mwf = fmaxf(mwf, __shfl_xor_sync(kFull, mwf, o));
-    const double mw = mwf;
+    double mw = mloc;
+    for (int o = 16; o > 0; o >>= 1) mw = fmax(mw, __shfl_xor_sync(kFull, mw, o));
     bool any_abort = __any_sync(kFull, abort_cell);
     if (WARPS > 1) any_abort = __syncthreads_or(any_abort);
     mcheck = fmax(mcheck, mw);
     if (!any_abort && mine) {
-      h_out = fmaxf(hrho_last, h_lower);
+      h_out = fmax(hrho_last, h_lower);
       rho_out = rho; om_out = om; zeta_out = zeta;
     }
     return any_abort ? 1 : 0;

@@ -30,6 +30,7 @@
 //
 // Build with -ffp-contract=off so that x86-64 and aarch64 give the same bits.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -137,6 +138,20 @@ struct Oracle {
   std::vector<int64_t> dir_count, cell_count;
   std::vector<uint64_t> dir_hash, cell_hash;
   int64_t n_density_pairs = 0, n_hydro_pairs = 0, n_direct_pairs = 0, n_cell_pairs = 0;
+  // Active particles (the reference's `active` flag, src/Headers/Flags.h:33): empty means
+  // every particle is active.  The h solve and the force passes work on active particles
+  // only (Tree::ComputeActiveCellList / ComputeActiveParticleList, src/Tree/Tree.cpp:59-115).
+  std::vector<unsigned char> active;
+  // Timestep levels, and the neighbour-level bookkeeping of a force pass
+  // (GradhSph.cpp:445-446, :569-570; GradhSphTree.cpp:375-417, :610-640).  Empty: not kept.
+  std::vector<int> level, levelneib;
+  bool is_active(int64_t i) const { return active.empty() || active[i]; }
+  bool leaf_has_active(const Cell& cell) const {
+    if (active.empty()) return cell.n > 0;
+    for (int j = 0; j < cell.n; j++)
+      if (active[order[cell.first + j]]) return true;
+    return false;
+  }
 
   int c2_of(int c, int level) const { return c + (1 << (ltot - level)); }
   int cnext_of(int c, int level) const {
@@ -449,7 +464,7 @@ struct Oracle {
       for (int li = 0; li < (int) leaves.size(); li++) {
         const int c = leaves[li];
         const Cell& cell = cells[c];
-        if (cell.n == 0) continue;
+        if (!leaf_has_active(cell)) continue;
         double hmax = cell.hmax;
         std::vector<double> hsave(cell.n);
         for (int j = 0; j < cell.n; j++) hsave[j] = h[order[cell.first + j]];
@@ -461,6 +476,7 @@ struct Oracle {
           gather_for_leaf(c, hmax, cand);
           for (int j = 0; j < cell.n; j++) {
             const int i = order[cell.first + j];
+            if (!is_active(i)) continue;
             const double rp[3] = {x[0][i], x[1][i], x[2][i]};
             const double hrs = kKernRangeSqd * hmax * hmax;
             ngb2.clear();
@@ -487,15 +503,17 @@ struct Oracle {
   // ---------------------------------------------------------------------------------
   // Hydro-only forces (periodic or open) for all particles.
   void hydro_forces() {
+    begin_levels();
 #pragma omp parallel
     {
       std::vector<int> cand_id;
       std::vector<double> cand_r;
       int64_t local_pairs = 0;
+      int* lv = thread_levels();
 #pragma omp for schedule(guided)
       for (int li = 0; li < (int) leaves.size(); li++) {
         const Cell& cell = cells[leaves[li]];
-        if (cell.n == 0) continue;
+        if (!leaf_has_active(cell)) continue;
         cand_id.clear(); cand_r.clear();
         const double hrangemaxsqd = std::pow(cell.rmax + kKernRange * cell.hmax, 2);
         walk([&](int cc, const Cell& o) -> int {
@@ -519,12 +537,46 @@ struct Oracle {
         });
         for (int j = 0; j < cell.n; j++) {
           const int i = order[cell.first + j];
-          pair_loop(i, cand_id, cand_r, false, nullptr, local_pairs);
+          if (!is_active(i)) continue;
+          pair_loop(i, cand_id, cand_r, false, nullptr, local_pairs, lv);
         }
       }
 #pragma omp atomic
       n_hydro_pairs += local_pairs;
     }
+    end_levels();
+  }
+
+  // Per-thread neighbour-level buffers (the reference's levelneibbuf, HydroTree.cpp:230-240)
+  // and their reduction into levelneib: an active particle's levelneib restarts from 0
+  // (Sph::ZeroAccelerations, src/Hydrodynamics/Sph.cpp:126-140) and every particle takes
+  // the max with what the pass found (GradhSphTree.cpp:412-417, :635-640).
+  std::vector<std::vector<int>> lvbuf;
+  void begin_levels() {
+    if (level.empty()) return;
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    lvbuf.assign(nt, std::vector<int>(n, 0));
+  }
+  int* thread_levels() {
+    if (level.empty()) return nullptr;
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    return lvbuf[t].data();
+  }
+  void end_levels() {
+    if (level.empty()) return;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      int v = is_active(i) ? 0 : levelneib[i];
+      for (const auto& b : lvbuf) v = std::max(v, b[i]);
+      levelneib[i] = v;
+    }
+    lvbuf.clear();
   }
 
   bool periodic_box_overlap(const double* amin, const double* amax, const double* bmin, const double* bmax) const {
@@ -561,7 +613,7 @@ struct Oracle {
   // Pair loop over candidate SPH neighbours of particle i (hydro or hydro+gravity).
   // With gravity, candidates that fail the SPH test are Newtonian direct terms.
   void pair_loop(int i, const std::vector<int>& cid, const std::vector<double>& cr, bool grav,
-                 std::vector<int>* direct_out, int64_t& pairs) {
+                 std::vector<int>* direct_out, int64_t& pairs, int* lv = nullptr) {
     const double hi = h[i], rhoi = rho[i];
     const double invh_i = 1.0 / hi, invrho_i = 1.0 / rhoi, invhsqdi = invh_i * invh_i;
     const double rp[3] = {x[0][i], x[1][i], x[2][i]};
@@ -588,6 +640,10 @@ struct Oracle {
       }
       if (want_lists || want_summary) hydro_neib[i].push_back(j);
       pairs++;
+      if (lv) {   // GradhSph.cpp:445-446 / :569-570
+        lv[i] = std::max(lv[i], level[j]);
+        lv[j] = std::max(lv[j], level[i]);
+      }
       const double invh_j = 1.0 / h[j], invrho_j = 1.0 / rho[j];
       const double fac_j = (pressure[j] * invomega[j]) / (rho[j] * rho[j]);
       if (!grav) {
@@ -668,16 +724,18 @@ struct Oracle {
   // Hydro + self-gravity forces (open boundaries).
   void all_forces() {
     const bool quad = p.multipole == 1;
+    begin_levels();
 #pragma omp parallel
     {
       std::vector<int> near_id, direct_id, gcells;
       std::vector<double> near_r;
       int64_t local_pairs = 0, local_direct = 0, local_cells = 0;
+      int* lv = thread_levels();
 #pragma omp for schedule(guided)
       for (int li = 0; li < (int) leaves.size(); li++) {
         const int lc = leaves[li];
         const Cell& cell = cells[lc];
-        if (cell.n == 0) continue;
+        if (!leaf_has_active(cell)) continue;
         near_id.clear(); near_r.clear(); direct_id.clear(); gcells.clear();
         const double hrangemax = kKernRange * cell.hmax, rmax = cell.rmax;
         const double hrangemaxsqd = std::pow(cell.rmax + kKernRange * cell.hmax, 2);
@@ -724,13 +782,16 @@ struct Oracle {
           cell_count[li] = (int64_t) gcells.size();
           cell_hash[li] = hsh;
         }
+        int nact = 0;
         for (int j = 0; j < cell.n; j++) {
           const int i = order[cell.first + j];
+          if (!is_active(i)) continue;
+          nact++;
           gpot[i] = (m[i] / h[i]) * wpot(0.0);
           for (int k = 0; k < 3; k++) ag[k][i] = 0.0;
           std::vector<int> dl;
           const int64_t before = local_pairs;
-          pair_loop(i, near_id, near_r, true, (want_lists || want_summary) ? &dl : nullptr, local_pairs);
+          pair_loop(i, near_id, near_r, true, (want_lists || want_summary) ? &dl : nullptr, local_pairs, lv);
           local_direct += (int64_t) near_id.size() - (local_pairs - before);
           for (int id : direct_id) direct_term(i, x[0][id], x[1][id], x[2][id], m[id]);
           for (int cc : gcells) cell_term(i, cells[cc], quad);
@@ -747,8 +808,8 @@ struct Oracle {
           }
           for (int k = 0; k < 3; k++) a[k][i] += ag[k][i];
         }
-        local_direct += (int64_t) cell.n * (int64_t) direct_id.size();
-        local_cells += (int64_t) cell.n * (int64_t) gcells.size();
+        local_direct += (int64_t) nact * (int64_t) direct_id.size();
+        local_cells += (int64_t) nact * (int64_t) gcells.size();
       }
 #pragma omp atomic
       n_hydro_pairs += local_pairs;
@@ -757,6 +818,7 @@ struct Oracle {
 #pragma omp atomic
       n_cell_pairs += local_cells;
     }
+    end_levels();
   }
 
   // ComputeQuadropole<3> (NeighbourSearch.h:423-449) or the monopole sum (:349-377).
@@ -912,10 +974,293 @@ struct Oracle {
   bool given = false;
   std::vector<double> g_h, g_rho, g_invomega, g_zeta, g_pressure, g_sound;
 
+  // ---------------------------------------------------------------------------------
+  // KDK leapfrog with block timesteps: the gas part of SphSimulation::PostInitialConditionsSetup
+  // and MainLoop (src/Hydrodynamics/SphSimulation.cpp:203-565, :573-880) with SphLeapfrogKDK
+  // (src/Hydrodynamics/SphLeapfrogKDK.cpp:76-331), SphIntegration::Timestep
+  // (src/Hydrodynamics/SphIntegration.cpp:81-130) and Simulation::ComputeBlockTimesteps
+  // (src/Common/Simulation.cpp:1764-2190; ComputeGlobalTimestep :1664-1752 for one level).
+  struct KdkParams { int32_t nlevels, level_diff_max, pad0, pad1; double courant_mult, accel_mult, energy_mult, pad2; };
+  KdkParams kp{};
+  bool energy_eq = false;
+  int kn = 0, nresync = 0, level_max = 0, level_step = 1, Nsteps = 0;
+  double t = 0.0, timestep = 0.0, dt_max = 0.0, timestep_old = 0.0;
+  int64_t active_updates = 0;
+  unsigned kdk_status = 0;       // 1 invalid timestep, 2 CheckTimesteps did not settle
+  std::vector<double> r0[3], v0[3], a0[3], u0, dudt0, dt, dt_next, tlast;
+  std::vector<int> nlast, nstep;
+  std::vector<unsigned char> endstep;
+  static int pow2i(int k) { return k >= 0 ? (1 << k) : 0; }   // (int) pow(2, k)
+
+  // ComputeTimestepLevel, src/Headers/InlineFuncs.h:550-557
+  static int timestep_level(double dt_, double dtmax) {
+    const double kInvLogTwo = 1.44269504088896;   // invlogetwo, src/Headers/Constants.h:64
+    const int l = (int) (kInvLogTwo * std::log(dtmax / dt_)) + 1;
+    return l > 0 ? l : 0;
+  }
+
+  // SphIntegration::Timestep: Courant, acceleration and energy conditions
+  double particle_timestep(int64_t i) {
+    const double kSmallDp = 1.0e-50;   // small_number_dp, src/Headers/Constants.h:90
+    const double hi = h[i];
+    double ts = (kp.courant_mult * hi) / ((sound[i] + hi * std::fabs(div_v[i])) + kSmallDp);
+    const double amag = std::sqrt((a[0][i] * a[0][i] + a[1][i] * a[1][i]) + a[2][i] * a[2][i]);
+    ts = std::fmin(ts, kp.accel_mult * std::sqrt(hi / (amag + kSmallDp)));
+    if (energy_eq) ts = std::fmin(ts, kp.energy_mult * (u[i] / (std::fabs(dudt[i]) + 1.0e-20)));
+    if (!(ts <= 1.0e20) || !(ts > 0.0)) kdk_status |= 1u;
+    return ts;
+  }
+
+  // GradhSph::ComputeThermalProperties for every particle before a force pass (the
+  // radiation-step update of MainLoop, SphSimulation.cpp:672-679)
+  void thermal_all() {
+    const double gm1 = p.gamma_eos - 1.0;
+    const double u_iso = p.temp0 / (p.gamma_eos - 1.0) / p.mu_bar;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      if (p.eos == 1) u[i] = u_iso;
+      sound[i] = p.eos == 1 ? std::sqrt(gm1 * u[i]) : std::sqrt(p.gamma_eos * gm1 * u[i]);
+      pressure[i] = gm1 * rho[i] * u[i];
+    }
+  }
+
+  // Tree build from the current positions and smoothing lengths.
+  void kdk_build() {
+    h_ghost = h;
+    build_tree();
+  }
+
+  // One h solve (+ forces) over the active particles of the current tree.
+  int kdk_pass(bool forces) {
+    int64_t act = 0;
+    for (int64_t i = 0; i < n; i++) act += active[i] ? 1 : 0;
+    active_updates += act;
+    const int st = density();
+    if (st != 0) return st;
+    update_hmax(0);
+    thermal_all();
+    if (forces) {
+      if (p.self_gravity) all_forces(); else hydro_forces();
+      // total acceleration written as the reference sums it (a + atree) by all_forces;
+      // the hydro-only pass leaves atree zero
+    }
+    return 0;
+  }
+
+  void kdk_alloc() {
+    for (int k = 0; k < 3; k++) { r0[k].assign(n, 0.0); v0[k].assign(n, 0.0); a0[k].assign(n, 0.0); }
+    u0 = u; dudt0.assign(n, 0.0); dt.assign(n, 0.0); dt_next.assign(n, 0.0); tlast.assign(n, 0.0);
+    nlast.assign(n, 0); nstep.assign(n, 0); level.assign(n, 0); levelneib.assign(n, 0);
+    active.assign(n, 1); endstep.assign(n, 0);
+    rho.assign(n, 0); invomega.assign(n, 1); zeta.assign(n, 0); hfactor.assign(n, 0);
+    pressure.assign(n, 0); sound.assign(n, 0); div_v.assign(n, 0); dudt.assign(n, 0);
+    gpot.assign(n, 0); hrangesqd.assign(n, 0); gpot_hydro.assign(n, 0);
+    for (int k = 0; k < 3; k++) { a[k].assign(n, 0); ag[k].assign(n, 0); }
+    kn = 0; nresync = 0; level_max = 0; level_step = 1; Nsteps = 0;
+    t = timestep = dt_max = timestep_old = 0.0;
+    active_updates = 0;
+    kdk_status = 0;
+  }
+
+  // Simulation::ComputeBlockTimesteps (Nlevels > 1) / ComputeGlobalTimestep (Nlevels = 1)
+  void block_timesteps() {
+    const bool resync = kn == nresync;
+    double dtmin = 9.9e99;
+    int lmax_new = 0;
+    // particles that start a new step (all of them when resynchronising)
+    for (int64_t i = 0; i < n; i++) {
+      if (kp.nlevels == 1 && !resync) continue;
+      if (resync) {
+        const double d = particle_timestep(i);
+        dt_next[i] = d;
+        dtmin = std::min(dtmin, d);
+        continue;
+      }
+      const int dn = kn - nlast[i];
+      if (dn == nstep[i] && nstep[i] != pow2i(level_step - level[i])) {
+        // step shortened by CheckTimesteps (Saitoh & Makino)
+        const double d = particle_timestep(i);
+        const int lv = std::max(timestep_level(d, dt_max), levelneib[i] - kp.level_diff_max);
+        level[i] = std::max(level[i], lv);
+        levelneib[i] = level[i];
+        nlast[i] = kn;
+        nstep[i] = pow2i(level_step - level[i]);
+        dt_next[i] = (double) nstep[i] * timestep;
+        endstep[i] = 1;
+      } else if (dn == nstep[i]) {
+        const int ns = nstep[i], last_level = level[i];
+        const double d = particle_timestep(i);
+        const int lv = std::max(timestep_level(d, dt_max), levelneib[i] - kp.level_diff_max);
+        int nl;
+        if (lv < last_level && last_level > 1 && kn % (2 * ns) == 0) nl = last_level - 1;
+        else if (lv > last_level) nl = lv;
+        else nl = last_level;
+        level[i] = nl;
+        levelneib[i] = lv;
+        nlast[i] = kn;
+        nstep[i] = pow2i(level_step - nl);
+        dt_next[i] = (double) nstep[i] * timestep;
+        endstep[i] = 1;
+      }
+      lmax_new = std::max(lmax_new, level[i]);
+    }
+    // the integer-time state
+    int up = 0, down = 0;
+    if (kp.nlevels == 1) {
+      if (resync) {
+        kn = 0; level_max = 0; level_step = 0; nresync = 1;
+        timestep = dtmin; timestep_old = timestep;
+      }
+    } else if (resync) {
+      kn = 0;
+      timestep = dtmin;
+      level_max = kp.nlevels - 1;
+      level_step = level_max;
+      dt_max = dtmin * (double) pow2i(level_max);
+      timestep_old = dtmin;
+      nresync = pow2i(level_step);
+      timestep = dt_max / (double) nresync;
+    } else {
+      const int level_max_old = level_max;
+      const int istep = pow2i(level_step - level_max_old + 1);
+      int lm;
+      if (lmax_new > level_max_old) {
+        const int nf = pow2i(lmax_new - level_max_old);
+        kn *= nf; up = nf; lm = lmax_new;
+      } else if (lmax_new <= level_max_old - 1 && level_max_old > 1 && istep > 0 && kn % istep == 0) {
+        lm = level_max_old - 1;
+        const int nf = pow2i(level_max_old - lm);
+        kn /= nf; down = nf;
+      } else {
+        lm = level_max_old;
+      }
+      level_max = lm;
+      level_step = lm;
+      nresync = pow2i(level_step);
+      timestep = dt_max / (double) nresync;
+    }
+    // levels after resynchronisation, or the rescaled integer steps
+    for (int64_t i = 0; i < n; i++) {
+      if (kp.nlevels == 1) {
+        if (!resync) continue;
+        endstep[i] = 1; level[i] = 0; levelneib[i] = 0; nstep[i] = 1; dt_next[i] = timestep_old;
+        continue;
+      }
+      if (resync) {
+        const int lv = std::min(timestep_level(dt_next[i], dt_max), level_max);
+        level[i] = lv; levelneib[i] = lv;
+        nstep[i] = pow2i(level_step - lv);
+        nlast[i] = kn;
+        dt_next[i] = (double) nstep[i] * timestep_old;
+        endstep[i] = 1;
+        continue;
+      }
+      if (up) { nstep[i] *= up; nlast[i] *= up; }
+      if (down) { nlast[i] /= down; nstep[i] /= down; }
+      if (nlast[i] == kn) nstep[i] = pow2i(level_step - level[i]);
+    }
+  }
+
+  // SphLeapfrogKDK::EndTimestep (SphLeapfrogKDK.cpp:219-275)
+  void end_timestep() {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      if (!endstep[i]) continue;
+      const double d = dt[i];
+      for (int k = 0; k < 3; k++) {
+        v[k][i] = v[k][i] + (0.5 * d) * (a[k][i] - a0[k][i]);
+        r0[k][i] = x[k][i];
+        v0[k][i] = v[k][i];
+        a0[k][i] = a[k][i];
+      }
+      if (energy_eq) {
+        double uu = u[i] + (0.5 * (dudt[i] - dudt0[i])) * d;
+        if (uu <= 0.0) uu = u0[i] + dudt0[i] * d;
+        u[i] = uu; u0[i] = uu; dudt0[i] = dudt[i];
+      }
+      nlast[i] = kn;
+      tlast[i] = t;
+      dt[i] = dt_next[i];
+      dt_next[i] = 0.0;
+      endstep[i] = 0;
+      active[i] = 0;
+    }
+  }
+
+  // Initial h solves, force pass and timesteps (PostInitialConditionsSetup with h provided).
+  int kdk_setup() {
+    kdk_alloc();
+    kdk_build();
+    int st = kdk_pass(false);
+    if (st) return st;
+    kdk_build();
+    st = kdk_pass(true);
+    if (st) return st;
+    for (int64_t i = 0; i < n; i++) {
+      for (int k = 0; k < 3; k++) { r0[k][i] = x[k][i]; v0[k][i] = v[k][i]; a0[k][i] = a[k][i]; }
+      active[i] = 0;
+    }
+    block_timesteps();
+    end_timestep();
+    return 0;
+  }
+
+  // One MainLoop step.
+  int kdk_step() {
+    kn += 1; Nsteps += 1; t = t + timestep;
+    // SphLeapfrogKDK::AdvanceParticles + TimeIntegration::CheckBoundaries
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      const double d = t - tlast[i];
+      for (int k = 0; k < 3; k++) {
+        x[k][i] = (r0[k][i] + v0[k][i] * d) + ((0.5 * a0[k][i]) * d) * d;
+        v[k][i] = v0[k][i] + a0[k][i] * d;
+      }
+      if (energy_eq) u[i] = u0[i] + dudt0[i] * d;
+      active[i] = (kn - nlast[i] == nstep[i]) ? 1 : 0;
+      if (p.periodic) {
+        for (int k = 0; k < 3; k++) {
+          const double L = p.boxmax[k] - p.boxmin[k];
+          if (x[k][i] < p.boxmin[k]) { x[k][i] = x[k][i] + L; r0[k][i] = r0[k][i] + L; }
+          if (x[k][i] > p.boxmax[k]) { x[k][i] = x[k][i] - L; r0[k][i] = r0[k][i] - L; }
+        }
+      }
+    }
+    kdk_build();
+    const int kPasses = 3;   // the first pass and up to two CheckTimesteps repeats
+    for (int pass = 0; pass < kPasses; pass++) {
+      const int st = kdk_pass(true);
+      if (st) return st;
+      // unset active, then SphLeapfrogKDK::CheckTimesteps (SphLeapfrogKDK.cpp:284-331)
+      int cnt = 0;
+      for (int64_t i = 0; i < n; i++) {
+        active[i] = 0;
+        if (kp.nlevels <= 1) continue;
+        const int dn = kn - nlast[i];
+        if (dn != nstep[i] && levelneib[i] - level[i] > kp.level_diff_max) {
+          const int level_new = levelneib[i] - kp.level_diff_max;
+          const int nnewstep = pow2i(level_step - level_new);
+          if (nnewstep > 0 && dn % nnewstep == 0) {
+            if (dn > 0) nstep[i] = dn;
+            level[i] = level_new;
+            active[i] = 1;
+            cnt++;
+          }
+        }
+      }
+      if (cnt == 0) break;
+      if (pass == kPasses - 1) kdk_status |= 2u;
+    }
+    block_timesteps();
+    end_timestep();
+    return 0;
+  }
+
   int run(int nthreads) {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
+    active.clear(); level.clear(); levelneib.clear();
     rho.assign(n, 0); invomega.assign(n, 1); zeta.assign(n, 0); hfactor.assign(n, 0);
     pressure.assign(n, 0); sound.assign(n, 0); div_v.assign(n, 0); dudt.assign(n, 0);
     gpot.assign(n, 0); hrangesqd.assign(n, 0); gpot_hydro.assign(n, 0);
@@ -1101,6 +1446,65 @@ void gsph_oracle_stars(void* handle, double* out) {
     }
     r[6] = o->s_gpot.empty() ? 0.0 : o->s_gpot[s_];
   }
+}
+
+// KDK run: SetupSimulation then nsteps main-loop steps of the gas with block timesteps.
+// Inputs in input order.  out_state: n x 24 doubles (x y z vx vy vz ax ay az h rho u level
+// nstep nlast levelneib dt tlast dudt div_v gpot invomega pressure sound); out_global: n t
+// timestep level_max level_step nresync Nsteps dt_max; out_info: setup seconds, seconds of
+// the nsteps steps, active updates of the setup, active updates of the steps, status.
+// Returns 0, or -2 if an h iteration failed to converge.
+int gsph_oracle_kdk(void* handle, int64_t n, const double* x, const double* y, const double* z,
+                    const double* vx, const double* vy, const double* vz, const double* m,
+                    const double* u, const double* h, const double* kdk_params, int nsteps, int nthreads,
+                    double* out_state, double* out_global, double* out_info) {
+  Oracle* o = static_cast<Oracle*>(handle);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  o->n = n;
+  o->x[0].assign(x, x + n); o->x[1].assign(y, y + n); o->x[2].assign(z, z + n);
+  o->v[0].assign(vx, vx + n); o->v[1].assign(vy, vy + n); o->v[2].assign(vz, vz + n);
+  o->m.assign(m, m + n); o->u.assign(u, u + n); o->h.assign(h, h + n);
+  o->want_lists = o->want_summary = false;
+  o->kp = Oracle::KdkParams{};
+  o->kp.nlevels = (int32_t) kdk_params[0];
+  o->kp.level_diff_max = (int32_t) kdk_params[1];
+  o->kp.courant_mult = kdk_params[2];
+  o->kp.accel_mult = kdk_params[3];
+  o->kp.energy_mult = kdk_params[4];
+  o->energy_eq = o->p.eos == 0;
+  o->n_density_pairs = o->n_hydro_pairs = o->n_direct_pairs = o->n_cell_pairs = 0;
+  auto now = [] { return std::chrono::steady_clock::now(); };
+  auto t0 = now();
+  int st = o->kdk_setup();
+  const double t_setup = std::chrono::duration<double>(now() - t0).count();
+  const int64_t upd_setup = o->active_updates;
+  auto t1 = now();
+  for (int q = 0; q < nsteps && st == 0; q++) st = o->kdk_step();
+  const double t_steps = std::chrono::duration<double>(now() - t1).count();
+  if (out_info) {
+    out_info[0] = t_setup; out_info[1] = t_steps;
+    out_info[2] = (double) upd_setup; out_info[3] = (double) (o->active_updates - upd_setup);
+    out_info[4] = (double) o->kdk_status;
+  }
+  if (st) return st;
+  for (int64_t i = 0; i < n && out_state; i++) {
+    double* r = out_state + i * 24;
+    r[0] = o->x[0][i]; r[1] = o->x[1][i]; r[2] = o->x[2][i];
+    r[3] = o->v[0][i]; r[4] = o->v[1][i]; r[5] = o->v[2][i];
+    r[6] = o->a[0][i]; r[7] = o->a[1][i]; r[8] = o->a[2][i];
+    r[9] = o->h[i]; r[10] = o->rho[i]; r[11] = o->u[i];
+    r[12] = o->level[i]; r[13] = o->nstep[i]; r[14] = o->nlast[i]; r[15] = o->levelneib[i];
+    r[16] = o->dt[i]; r[17] = o->tlast[i]; r[18] = o->dudt[i]; r[19] = o->div_v[i];
+    r[20] = o->gpot[i]; r[21] = o->invomega[i]; r[22] = o->pressure[i]; r[23] = o->sound[i];
+  }
+  if (out_global) {
+    out_global[0] = o->kn; out_global[1] = o->t; out_global[2] = o->timestep; out_global[3] = o->level_max;
+    out_global[4] = o->level_step; out_global[5] = o->nresync; out_global[6] = o->Nsteps;
+    out_global[7] = o->dt_max;
+  }
+  return 0;
 }
 
 int gsph_oracle_nleaf(void* handle) { return (int) static_cast<Oracle*>(handle)->leaves.size(); }

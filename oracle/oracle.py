@@ -91,6 +91,8 @@ def _load():
         lib.gsph_oracle_run_given.argtypes = [vp, i64] + [dp] * 15 + [i32, i32]
         lib.gsph_oracle_nleaf.restype = i32
         lib.gsph_oracle_nleaf.argtypes = [vp]
+        lib.gsph_oracle_kdk.restype = i32
+        lib.gsph_oracle_kdk.argtypes = [vp, i64] + [dp] * 10 + [i32, i32, dp, dp, dp]
         lib.gsph_oracle_set_stars.argtypes = [vp, i32] + [dp] * 8
         lib.gsph_oracle_stars.argtypes = [vp, dp]
         _lib = lib
@@ -204,3 +206,40 @@ def run(ics: dict, params: dict, lists: bool = False, nthreads: int = 0, summary
         return res
     finally:
         lib.gsph_oracle_destroy(h)
+
+
+KDK_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "h", "rho", "u", "level", "nstep", "nlast",
+              "levelneib", "dt", "tlast", "dudt", "div_v", "gpot", "invomega", "pressure", "sound"]
+KDK_GLOBAL = ["n", "t", "timestep", "level_max", "level_step", "nresync", "Nsteps", "dt_max"]
+
+
+def kdk(ics: dict, params: dict, kdk_params: dict, nsteps: int, nthreads: int = 0) -> dict:
+    """Setup plus nsteps main-loop steps of the KDK leapfrog with block timesteps.
+
+    Returns the final per-particle state (KDK_FIELDS, input order), the integer-time
+    state (KDK_GLOBAL) and timing: setup and step wall seconds, active particle updates
+    of the setup and of the steps.
+    """
+    lib = _load()
+    prm = make_params(params)
+    hnd = lib.gsph_oracle_create(ctypes.byref(prm))
+    try:
+        arrs = [np.ascontiguousarray(ics[k], dtype=np.float64)
+                for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")]
+        n = len(arrs[0])
+        kp = np.array([kdk_params.get("nlevels", 1), kdk_params.get("level_diff_max", 1),
+                       kdk_params.get("courant_mult", 0.15), kdk_params.get("accel_mult", 0.3),
+                       kdk_params.get("energy_mult", 0.4)], dtype=np.float64)
+        state = np.empty((n, len(KDK_FIELDS)))
+        glob = np.empty(len(KDK_GLOBAL))
+        info = np.zeros(5)
+        st = lib.gsph_oracle_kdk(hnd, n, *[_ptr(a) for a in arrs], _ptr(kp), int(nsteps), int(nthreads),
+                                 _ptr(state), _ptr(glob), _ptr(info))
+        if st != 0:
+            raise RuntimeError(f"oracle KDK run failed with status {st}")
+        return {"state": {k: state[:, i].copy() for i, k in enumerate(KDK_FIELDS)},
+                "global": {k: float(glob[i]) for i, k in enumerate(KDK_GLOBAL)},
+                "setup_s": float(info[0]), "steps_s": float(info[1]),
+                "setup_updates": int(info[2]), "step_updates": int(info[3]), "status": int(info[4])}
+    finally:
+        lib.gsph_oracle_destroy(hnd)
