@@ -1,18 +1,23 @@
-"""Benchmark: particle updates/s of the grad-h SPH + KD-tree gravity step on one GB300.
+"""Benchmark: particle updates/s of the grad-h SPH + KD-tree gravity path on one GB300.
 
-Workload (default): the self-gravitating Plummer sphere, N = 262,144 gas particles,
-geometric opening angle theta = 0.5 (thetamaxsqd = 0.25), quadrupole cells, Nleafmax = 8,
-seeded synthetic particles (gandalf_gb300.ics.plummer_sphere).  One step = KD-tree build
-+ grad-h h-rho solve + tree hmax update + hydro + self-gravity forces for every particle;
-one particle update = one particle through that step.
+Workload (default): the rotating isothermal cloud, N = 1,048,576 gas particles (uniform
+sphere R = M = G = 1, m = 2 density perturbation, solid-body rotation with E_rot/|E_grav| =
+0.16, E_therm/|E_grav| = 0.26), self-gravity with theta = 0.5 (thetamaxsqd = 0.25) and
+quadrupole cells, Nleafmax = 8, 4 block-timestep levels: K steps of the KDK leapfrog main
+loop (default K = 20) replayed from one CUDA graph, in the FP64 and the mixed form.  The
+unit of work is one active particle through one h solve and one force pass (each KDK
+substep counts its active particles, repeats included); seeded synthetic inputs
+(gandalf_gb300.ics.rotating_cloud).  Other workloads: --workload plummer_sphere (one full
+step of the 262,144-particle Plummer sphere), evrard_sphere (8,388,608 + 64 stars),
+kh_ensemble (64 periodic boxes, batched), periodic_cube.
 
 Arms:
-  --impl gsph (default)  the CUDA library; `value` is device-resident throughput, `e2e`
-                         goes through the array-of-structures C ABI with host records
-                         copied in and out every step.
+  --impl gsph (default)  the CUDA library; `value` is device-resident throughput of the
+                         mixed form; `e2e` goes through the C ABI with pinned host arrays
+                         copied in and results copied out.
   --impl reference       the CPU restatement of the reference algorithm (oracle/) on all
-                         host cores (the upstream binary is compiled only where its sources
-                         are available).
+                         host cores, on the same workload: the same K main-loop steps after
+                         the same setup for the rotating cloud.
 Under torchrun each rank runs an independent replica on its own GPU (the step has no
 exchange between simulations); rank 0 prints the line.
 """
@@ -35,19 +40,24 @@ sys.path.insert(0, ROOT)
 METRIC = "particle updates/s (SPH+tree gravity), mixed vs FP64 GPU at ≤1e-4 RMS rel error"
 UNIT = "particle updates/s"
 
-# Algorithmic floating-point operations per interaction, counted from the reference
-# formulas (add/sub/mul = 1, fused multiply-add = 2, sqrt and division = 1 each):
-#   density pair, per h iteration       GradhSph.cpp:197-204          42
-#   hydro pair                          GradhSph.cpp:384-447          80
-#   hydro + softened-gravity pair       GradhSph.cpp:498-571         145
-#   Newtonian direct term               GradhSph.cpp:671-686          24
-#   quadrupole cell term                NeighbourSearch.h:423-449     82
-#   monopole cell term                  NeighbourSearch.h:359-373     24
-FLOPS = dict(density=42, hydro=80, hydro_grav=145, direct=24, quad=82, mono=24)
+# Algorithmic floating-point operations per interaction, counted line by line from the
+# reference formulas as written (add, sub, mul, div, sqrt = 1; a multiply-add = 2), the
+# unconditional operations only: the artificial-viscosity branch of the hydro pairs (about
+# 20 more for approaching pairs) is not counted.
+#   density pair, per h iteration   GradhSph.cpp:197-204 (w0, womega, wzeta of one s)     45
+#   hydro pair                      GradhSph.cpp:384-447                                  60
+#   hydro + softened-gravity pair   GradhSph.cpp:498-571                                 127
+#   Newtonian direct term           GradhSph.cpp:671-686                                  24
+#   quadrupole cell term            NeighbourSearch.h:423-449                             80
+#   monopole cell term              NeighbourSearch.h:359-373                             23
+FLOPS = dict(density=45, hydro=60, hydro_grav=127, direct=24, quad=80, mono=23)
 
-# DRAM bytes (read + write) per force pass, from one-pass ncu captures of the force kernels
-# (profiles/forces_density_mixed_plummer262k_dram.md): (workload, n, form) -> bytes.
-FORCE_TRAFFIC = {("plummer_sphere", 262144, "mixed"): 45.65e6 + 0.55e6 + 5.15e6}
+# DRAM bytes (read + write) of one force pass of the mixed form, from one-pass ncu captures
+# of the force kernels (summed over the kernels of a pass); None where no capture exists.
+FORCE_TRAFFIC = {
+    ("plummer_sphere", 262144, "mixed"): {"bytes": 45.65e6 + 0.55e6 + 5.15e6,
+                                          "source": "profiles/forces_density_mixed_plummer262k_dram.md"},
+}
 
 
 def max_over_ranks(ms, world, device="cuda"):
@@ -69,19 +79,26 @@ def job_throughput(units_per_rank, ms, world):
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=0,
+                    help="timed steps (default: 20 KDK steps for rotating_cloud, 3 for evrard_sphere, else 10)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gsph", choices=["gsph", "reference"])
-    ap.add_argument("--workload", default="plummer_sphere")
+    ap.add_argument("--workload", default="rotating_cloud",
+                    choices=["rotating_cloud", "plummer_sphere", "periodic_cube", "evrard_sphere", "kh_ensemble"])
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--nleafmax", type=int, default=0,
                     help="evrard_sphere: leaf size to use instead of the autotuner's choice")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="rotating_cloud: skip the one-step precision and list comparison of the forms")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="launch each step's kernels on the stream "
                     "instead of replaying the captured CUDA graph")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if not args.steps:
+        args.steps = {"rotating_cloud": 20, "evrard_sphere": 3}.get(args.workload, 10)
+    return args
 
 
 def ensemble_main(args, rank, world, local):
@@ -197,7 +214,7 @@ def evrard_main(args, rank, world, local):
     c = ics_mod.evrard_sphere(n, seed=51 + rank)
     params = c.pop("params")
     form = "mixed" if args.precision == "auto" else args.precision
-    steps = args.steps if args.steps != 10 else 3
+    steps = args.steps
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     with ClockSampler(local) as clk:
         tune = ({"nleafmax": args.nleafmax, "ms_per_step": None} if args.nleafmax > 0 else
@@ -249,108 +266,265 @@ def evrard_main(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
-def kdk_main(args, rank, world, local):
-    """Rotating isothermal cloud (uniform sphere, m = 2 perturbation, solid-body rotation),
-    N = 1,048,576, self-gravity theta = 0.5 quadrupole, 4 block-timestep levels: K KDK main
-    loop steps (default 20) replayed from one CUDA graph, FP64 and mixed forms.  The unit
-    of work is one active particle through one force pass (the metric's unit for
-    block-timestep configurations: active particles per KDK substep)."""
-    import torch
+def kdk_workload(n, rank=0):
     from gandalf_gb300 import ics as ics_mod
-    from gandalf_gb300 import _native
-    from gandalf_gb300 import build as gbuild
-    from gandalf_gb300.sph import GradhSphTree
-    gbuild.build()
-    lib = _native.load()
-    n = args.n or 1048576
     c = ics_mod.rotating_cloud(n, seed=31 + rank)
     params = c.pop("params")
     kdk = c.pop("kdk")
-    K = args.steps if args.steps != 10 else 20
+    return c, params, kdk
+
+
+def kdk_config(n, kdk, K):
+    """The workload keys of the rotating-cloud line (shared by both arms)."""
+    return {"workload": "rotating_cloud", "n": n, "nlevels": kdk["nlevels"], "kdk_steps": K,
+            "level_diff_max": kdk["level_diff_max"], "courant_mult": kdk["courant_mult"],
+            "accel_mult": kdk["accel_mult"], "eos": "isothermal", "thetamaxsqd": 0.25, "multipole": "quadrupole",
+            "gravity_mac": "geometric", "nleafmax": 8, "h_fac": 1.2, "h_converge": 0.01, "kernel": "m4",
+            "unit_of_work": "active particle through one h solve and force pass (per KDK substep)"}
+
+
+def err_stats(a, b):
+    """(RMS, max) of |a - b| / (|b| + 1e-6 rms b) over all particles."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    floor = 1e-6 * np.sqrt(np.mean(b * b)) + 1e-300
+    e = np.abs(a - b) / (np.abs(b) + floor)
+    return {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
+
+
+def vec_err_stats(a, b, keys):
+    A = np.stack([a[k] for k in keys], 1)
+    B = np.stack([b[k] for k in keys], 1)
+    nb = np.linalg.norm(B, axis=1)
+    floor = 1e-6 * np.sqrt(np.mean(nb * nb)) + 1e-300
+    e = np.linalg.norm(A - B, axis=1) / (nb + floor)
+    return {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
+
+
+def all_errors(a, b):
+    """Mixed against FP64 for every per-particle result."""
+    out = {k: err_stats(a[k], b[k]) for k in ("h", "rho", "invomega", "zeta", "pressure", "sound", "gpot",
+                                              "dudt", "div_v") if k in a}
+    out["a"] = vec_err_stats(a, b, ("ax", "ay", "az"))
+    out["a_tree"] = vec_err_stats(a, b, ("agx", "agy", "agz"))
+    return out
+
+
+def csr_differ(oa, ia, ob, ib):
+    """Particles whose neighbour sets (CSR, any order inside a row) differ."""
+    n = len(oa) - 1
+    ca, cb = np.diff(oa), np.diff(ob)
+    differ = ca != cb
+    same = ~differ
+    rows_a = np.repeat(np.arange(n), ca)
+    rows_b = np.repeat(np.arange(n), cb)
+    sa = ia[np.lexsort((ia, rows_a))]
+    sb = ib[np.lexsort((ib, rows_b))]
+    keep_a = same[rows_a]
+    keep_b = same[rows_b]
+    bad = sa[keep_a] != sb[keep_b]
+    if bad.any():
+        differ[np.unique(rows_a[keep_a][bad])] = True
+    return int(differ.sum())
+
+
+def precision_step(c, params, h_converge=None, record=True):
+    """One full step (tree, h solve, forces) of both forms from identical inputs: errors of
+    every quantity, and how many particles' interaction lists differ between the forms."""
+    from gandalf_gb300.sph import GradhSphTree
+    prm = dict(params)
+    if h_converge is not None:
+        prm["h_converge"] = h_converge
+    res, lists = {}, {}
+    for form in ("fp64", "mixed"):
+        t = GradhSphTree(prm, precision=form, device=int(os.environ.get("LOCAL_RANK", "0")))
+        if record:
+            t.set_recording(True, 512)
+        t.set_particles(c)
+        t.step()
+        res[form] = t.results()
+        if record:
+            lists[form] = (t.sph_neighbours_csr(), t.direct_summary(), t.cell_summary())
+        res[form]["exact_checks"] = t.stats()["exact_checks"]
+        t.close()
+    out = {"errors": all_errors(res["mixed"], res["fp64"]),
+           "exact_checks_mixed": int(res["mixed"]["exact_checks"])}
+    if record:
+        (oa, ia), (dca, dha), (_, cca, cha) = lists["mixed"]
+        (ob, ib), (dcb, dhb), (_, ccb, chb) = lists["fp64"]
+        out["list_diff"] = {"sph_particles": csr_differ(oa, ia, ob, ib),
+                            "direct_particles": int(np.sum((dca != dcb) | (dha != dhb))),
+                            "multipole_leaves": int(np.sum((cca != ccb) | (cha != chb))),
+                            "n": len(oa) - 1}
+    return out
+
+
+def run_kdk_form(c, params, kdk, form, K, warm_seq, stream, device):
+    """Warm-up sequences (setup + K graph-replayed steps), then the timed one: setup
+    outside, the K steps between CUDA events on the stream.  Returns the context open."""
+    import torch
+    from gandalf_gb300.sph import GradhSphTree
+    t = GradhSphTree(params, precision=form, device=device)
+    t.set_stream(stream.cuda_stream)
+    for _ in range(warm_seq):
+        t.set_particles(c)
+        t.kdk_setup(**kdk)
+        t.kdk_steps(K, graph=True)          # the first call captures the K-step graph
+    t.set_particles(c)
+    t.kdk_setup(**kdk)
+    torch.cuda.synchronize()
+    u0 = t.kdk_status()["active_updates"]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t.kdk_steps(K, graph=True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    st = t.kdk_status()
+    s2 = t.stats()
+    upd = st["active_updates"] - u0
+    n = len(c["x"])
+    return t, {"value": upd / (ms * 1e-3), "ms_total": ms, "ms_per_step": ms / K, "active_updates": upd,
+               "active_fraction_per_step": upd / (K * n), "level_max": st["level_max"], "t_end": st["t"],
+               "phases_ms": {"build": s2["ms_build"], "density": s2["ms_density"], "forces": s2["ms_forces"]},
+               "counts": {k: s2[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs", "cell_pairs",
+                                             "exact_checks", "heavy_density", "heavy_forces")},
+               "launches": s2["launches"]}
+
+
+def kdk_e2e(t, c, kdk, K):
+    """Through the C ABI on an open context: pinned host arrays in, setup, K steps (the
+    captured graph), positions, velocities and solved fields out into pinned arrays."""
+    import torch
+    keys = ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")
+    pin = {k: torch.from_numpy(np.ascontiguousarray(c[k], dtype=np.float64)).pin_memory().numpy() for k in keys}
+    outs = ("x", "y", "z", "vx", "vy", "vz")
+    fields = ("h", "rho", "u", "ax", "ay", "az", "gpot")
+    n = len(c["x"])
+    obuf = {k: torch.empty(n, dtype=torch.float64).pin_memory().numpy() for k in outs + fields}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    t.set_particles(pin)
+    t.kdk_setup(**kdk)
+    u0 = t.kdk_status()["active_updates"]
+    t.kdk_steps(K, graph=True)
+    for k in outs:
+        t.kdk_state(k, out=obuf[k])
+    for k in fields:
+        t.field(k, out=obuf[k])
+    wall = time.perf_counter() - t0
+    upd = t.kdk_status()["active_updates"] - u0
+    return {"value": upd / wall, "wall_s": wall, "h2d_bytes_per_step": n * 8 * len(keys) / K,
+            "d2h_bytes_per_step": n * 8 * (len(outs) + len(fields)) / K,
+            "path": "gsph_set_particles (pinned host arrays) + gsph_kdk_setup + gsph_kdk_steps(K, graph) + "
+                    "gsph_kdk_get_state / gsph_get_field into pinned arrays; the setup (two h solves and a "
+                    "force pass) is inside the timed span, its updates are not counted"}
+
+
+def kdk_cpu_baseline(c, params, kdk, nsteps=2):
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    r = oracle.kdk(c, params, kdk, nsteps, nthreads=cores)
+    return {"value": r["step_updates"] / r["steps_s"], "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"setup + {nsteps} KDK main-loop steps of the same {len(c['x'])}-particle cloud "
+                      f"(oracle/gsph_oracle.cpp, the C++/OpenMP restatement of the reference path); the "
+                      f"{nsteps} steps timed: {r['step_updates']} active updates in {r['steps_s']:.2f} s"}
+
+
+def kdk_main(args, rank, world, local):
+    """Rotating isothermal cloud, N = 1,048,576, self-gravity theta = 0.5 quadrupole, 4
+    block-timestep levels: K KDK main-loop steps replayed from one CUDA graph, FP64 and
+    mixed forms.  The unit of work is one active particle through one h solve and force
+    pass (the metric's unit for block-timestep configurations)."""
+    import torch
+    from gandalf_gb300 import _native
+    from gandalf_gb300 import build as gbuild
+    gbuild.build()
+    lib = _native.load()
+    n = args.n or 1048576
+    K = args.steps or 20
+    W = args.warmup
+    c, params, kdk = kdk_workload(n, rank)
     stream = torch.cuda.current_stream()
     forms = ["fp64", "mixed"] if args.precision == "auto" else [args.precision]
+    warm_seq = max(1, -(-W // K))           # whole K-step sequences covering >= W warm-up steps
     out, finals = {}, {}
+    ctx_head = None
+    head = "mixed" if "mixed" in forms else forms[0]
     with ClockSampler(local) as clk:
         for form in forms:
-            t = GradhSphTree(params, precision=form, device=local)
-            t.set_stream(stream.cuda_stream)
-            t.set_particles(c)
-            t.kdk_setup(**kdk)
-            t.kdk_steps(K, graph=True)          # capture + warm-up run of the K-step graph
-            torch.cuda.synchronize()
-            u0 = t.kdk_status()["active_updates"]
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            t.kdk_steps(K, graph=True)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            ms = ev0.elapsed_time(ev1)
-            st = t.kdk_status()
-            upd = st["active_updates"] - u0
-            s2 = t.stats()
-            out[form] = {"value": upd / (ms * 1e-3), "ms_total": ms, "ms_per_step": ms / K, "active_updates": upd,
-                         "active_fraction_per_step": upd / (K * n), "particle_steps_per_s": n * K / (ms * 1e-3),
-                         "level_max": st["level_max"], "t_end": st["t"],
-                         "counts": {k: s2[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs", "cell_pairs")},
-                         "launches": s2["launches"]}
+            if world > 1:
+                import torch.distributed as dist
+                dist.barrier()
+            t, R = run_kdk_form(c, params, kdk, form, K, warm_seq, stream, local)
             finals[form] = t.results()
-            t.close()
+            for k in ("x", "y", "z"):
+                finals[form]["pos_" + k] = t.kdk_state(k)
+            out[form] = R
+            if form == head:
+                ctx_head = t
+            else:
+                t.close()
     clocks = clk.summary()
-    head = "mixed" if "mixed" in out else forms[0]
     R = out[head]
-    R["ms_total"] = max_over_ranks(R["ms_total"], world)
-    R["value"] = R["active_updates"] / (R["ms_total"] * 1e-3)
-    line = {"metric": METRIC, "value": job_throughput(R["active_updates"], R["ms_total"], world), "unit": UNIT,
-            "n_gpus": world, "steps": K,
-            "warmup": 1, "ms_per_step": R["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 pairs / f64 positions" if head == "mixed" else "f64",
-            "data": "synthetic",
-            "config": {"workload": "rotating_cloud", "n": n, "nlevels": kdk["nlevels"], "kdk_steps": K,
-                       "level_diff_max": kdk["level_diff_max"], "courant_mult": kdk["courant_mult"],
-                       "accel_mult": kdk["accel_mult"], "eos": "isothermal", "thetamaxsqd": 0.25,
-                       "multipole": "quadrupole", "precision": head, "cuda_graph": "K steps in one graph",
-                       "unit_of_work": "active particle per force pass", "parallelism": f"replicas{world}",
-                       "l2": "working set (1M particles) larger than L2"},
-            "gpu_launches": R["launches"], "forms": out, "clocks": clocks}
+    ms_job = max_over_ranks(R["ms_total"], world)
+    value = job_throughput(R["active_updates"], ms_job, world)
+    cnt = R["counts"]
+    fp64 = head == "fp64"
+    peak_gf = lib.gsph_fma_peak_gflops(local, 1 if fp64 else 0)
+    f_force = (cnt["hydro_pairs"] * FLOPS["hydro_grav"] + cnt["direct_pairs"] * FLOPS["direct"] +
+               cnt["cell_pairs"] * FLOPS["quad"])
+    f_dens = cnt["density_pairs"] * FLOPS["density"]
+    passes = 3 * K
+    ms_f = R["phases_ms"]["forces"]
+    ms_d = R["phases_ms"]["density"]
+    traffic = FORCE_TRAFFIC.get(("rotating_cloud", n, head))
+    roof = {"bound": "fp64" if fp64 else "fp32",
+            "kernel": "force pass (k_all_forces_mixed + heavy-leaf k_all_forces_mixed_wide)" if not fp64
+            else "force pass (k_all_forces_fp64)",
+            "achieved": f_force / (ms_f * 1e-3) / 1e12, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
+            "frac": (f_force / (ms_f * 1e-3) / 1e12) / (peak_gf / 1e3),
+            "traffic": traffic["bytes"] if traffic else None,
+            "traffic_source": traffic["source"] if traffic else None,
+            "peak_source": "FMA-loop throughput measured live on this GPU (gsph_fma_peak_gflops); "
+                           "the pair loops run on the FP32/FP64 pipes, not HBM or tensor cores",
+            "flops_per_launch": f_force / passes, "ms_per_launch": ms_f / passes, "launches": passes,
+            "timing": "CUDA events recorded inside the K-step graph around every force pass, summed"}
+    roof_d = {"bound": roof["bound"], "kernel": "h solve (k_density_mixed + heavy-leaf k_density_mixed_pp, "
+              "with the hmax update and mirror refresh)" if not fp64 else "h solve (k_density_fp64)",
+              "achieved": f_dens / (ms_d * 1e-3) / 1e12, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
+              "frac": (f_dens / (ms_d * 1e-3) / 1e12) / (peak_gf / 1e3), "ms_total": ms_d}
+    cfg = kdk_config(n, kdk, K)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_job / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if fp64 else "f32 pairs / f64 positions, h iteration and moments",
+            "data": "synthetic (seeded rotating-cloud generator, no dataset)", "config": cfg,
+            "run": {"precision": head, "cuda_graph": "K steps in one graph",
+                    "warmup_sequences": warm_seq, "warmup_kdk_steps": warm_seq * K,
+                    "l2": "working set (1M particles, ~0.6 GB) larger than L2; not flushed",
+                    "parallelism": f"replicas{world}"},
+            "gpu_launches": R["launches"], "roofline": roof, "roofline_density": roof_d,
+            "forms": out, "clocks": clocks}
     if "fp64" in out and "mixed" in out:
         line["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
         a, b = finals["mixed"], finals["fp64"]
-        errs = {}
-        for k in ("rho", "h"):
-            e = np.abs(a[k] - b[k]) / np.abs(b[k])
-            errs[k] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
-        A = np.stack([a["ax"], a["ay"], a["az"]], 1)
-        B = np.stack([b["ax"], b["ay"], b["az"]], 1)
-        nb = np.linalg.norm(B, axis=1)
-        e = np.linalg.norm(A - B, axis=1) / nb
-        errs["a"] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
-        line["mixed_vs_fp64_rel_err_after_all_steps"] = errs
-    st = out[head]["counts"]
-    flops = (st["density_pairs"] * FLOPS["density"] + st["hydro_pairs"] * FLOPS["hydro_grav"] +
-             st["direct_pairs"] * FLOPS["direct"] + st["cell_pairs"] * FLOPS["quad"])
-    peak_gf = lib.gsph_fma_peak_gflops(local, 1 if head == "fp64" else 0)
-    achieved = flops / (R["ms_total"] * 1e-3) / 1e12
-    line["roofline"] = {"bound": "fp32" if head == "mixed" else "fp64", "kernel": "whole K-step sequence",
-                        "achieved": achieved, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
-                        "frac": achieved / (peak_gf / 1e3), "traffic": None,
-                        "peak_source": "measured FMA-loop throughput (gsph_fma_peak_gflops)"}
-    if not args.no_e2e:
-        # host particles in, setup, K steps, results out, through the C ABI
-        t = GradhSphTree(params, precision=head, device=local)
-        t0 = time.perf_counter()
-        t.set_particles(c)
-        t.kdk_setup(**kdk)
-        u0 = t.kdk_status()["active_updates"]
-        t.kdk_steps(K, graph=True)
-        res = {k: t.kdk_state(k) for k in ("x", "y", "z", "vx", "vy", "vz")}
-        res.update(t.results())
-        wall = time.perf_counter() - t0
-        upd = t.kdk_status()["active_updates"] - u0
-        t.close()
-        line["e2e"] = {"value": world * upd / wall, "unit": UNIT, "h2d_bytes_per_step": n * 9 * 8 / K,
-                       "d2h_bytes_per_step": n * 8 * (6 + len(res) - 6) / K,
-                       "path": "gsph_set_particles + gsph_kdk_setup + gsph_kdk_steps(K, graph) + field reads; "
-                               "setup (two h solves and a force pass) inside the timed span"}
+        errs = all_errors(a, b)
+        pos = np.sqrt(np.mean(sum((a["pos_" + k] - b["pos_" + k]) ** 2 for k in ("x", "y", "z"))))
+        errs["position_rms_abs"] = float(pos)
+        line["mixed_vs_fp64_after_all_steps"] = errs
+    if not args.no_e2e and ctx_head is not None:
+        e = kdk_e2e(ctx_head, c, kdk, K)
+        line["e2e"] = {"value": world * e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d_bytes_per_step"],
+                       "d2h_bytes_per_step": e["d2h_bytes_per_step"], "path": e["path"], "wall_s": e["wall_s"]}
+    if ctx_head is not None:
+        ctx_head.close()
+    if rank == 0 and not args.no_precision and "fp64" in out and "mixed" in out:
+        # identical inputs, one full step: every quantity and the lists, at the reference's
+        # default h_converge and at 1e-10 (which leaves no room for iteration-path flips)
+        line["precision_one_step"] = {"h_converge_0.01": precision_step(c, params),
+                                      "h_converge_1e-10": precision_step(c, params, 1e-10, record=False)}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = kdk_cpu_baseline(c, params, kdk)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -543,8 +717,36 @@ def cpu_baseline(c, params, budget_s=40.0):
                       f"(tree build + h solve + forces), {wall:.2f} s wall"}
 
 
+def kdk_reference_arm(args):
+    """The same K main-loop steps, after the same setup, by the CPU restatement of the
+    reference on all host threads; the K steps are timed."""
+    from oracle import oracle
+    n = args.n or 1048576
+    K = args.steps or 20
+    c, params, kdk = kdk_workload(n, 0)
+    cores = os.cpu_count() or 1
+    r = oracle.kdk(c, params, kdk, K, nthreads=cores)
+    value = r["step_updates"] / r["steps_s"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
+            "warmup": args.warmup, "ms_per_step": 1e3 * r["steps_s"] / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded rotating-cloud generator, no dataset)", "config": kdk_config(n, kdk, K),
+            "impl": "reference", "status": r["status"],
+            "active_fraction_per_step": r["step_updates"] / (K * n),
+            "setup_s": r["setup_s"],
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"setup (untimed warm-up) + {K} KDK main-loop steps of the {n}-particle "
+                                       f"cloud on {cores} host threads (oracle/gsph_oracle.cpp, the C++/OpenMP "
+                                       f"restatement of the reference path); {r['step_updates']} active updates "
+                                       f"in {r['steps_s']:.1f} s"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def reference_arm(args):
     from oracle import oracle
+    if args.workload == "rotating_cloud":
+        return kdk_reference_arm(args)
     c = workload(args.workload, args.n)
     params = dict(c["params"])
     cores = os.cpu_count() or 1
@@ -649,7 +851,8 @@ def main():
     roof = {"bound": "fp64" if fp64 else "fp32", "kernel": "all-forces" if gravity else "hydro-forces",
             "achieved": achieved, "peak": peak_gf / 1e3, "unit": "TFLOP/s",
             "frac": achieved / (peak_gf / 1e3) if peak_gf > 0 else None,
-            "traffic": FORCE_TRAFFIC.get((args.workload, n, head)),
+            "traffic": (FORCE_TRAFFIC.get((args.workload, n, head)) or {}).get("bytes"),
+            "traffic_source": (FORCE_TRAFFIC.get((args.workload, n, head)) or {}).get("source"),
             "peak_source": "measured FMA-loop throughput of this GPU (gsph_fma_peak_gflops); "
                            "MEASURED_PEAKS.json holds HBM and bf16 figures only",
             "flops_per_launch": f_force, "ms_per_launch": R["per"]["ms_forces"]}
@@ -668,26 +871,20 @@ def main():
                         "heavy_leaves": {"density": Rf["stats"]["heavy_density"],
                                          "forces": Rf["stats"]["heavy_forces"]}}
     if "fp64" in ok and "mixed" in ok:
-        a, b = results["mixed"]["results"], results["fp64"]["results"]
-        errs = {}
-        for k in ("rho", "h"):
-            e = np.abs(a[k] - b[k]) / np.abs(b[k])
-            errs[k] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
-        A = np.stack([a["ax"], a["ay"], a["az"]], 1)
-        B = np.stack([b["ax"], b["ay"], b["az"]], 1)
-        nb = np.linalg.norm(B, axis=1)
-        e = np.linalg.norm(A - B, axis=1) / nb
-        errs["a"] = {"rms": float(np.sqrt(np.mean(e * e))), "max": float(e.max())}
-        forms_out["mixed_vs_fp64_rel_err"] = errs
+        forms_out["mixed_vs_fp64_rel_err"] = all_errors(results["mixed"]["results"], results["fp64"]["results"])
         forms_out["speedup_mixed_over_fp64"] = results["fp64"]["ms_total"] / results["mixed"]["ms_total"]
     cfg = workload_config(args.workload, c)
-    cfg.update(precision=head, cuda_graph=not args.no_graph, l2="flushed between timed steps (256 MiB write, outside the timed span)",
-               parallelism=f"replicas{world}")
+    run = {"precision": head, "cuda_graph": not args.no_graph,
+           "l2": "flushed between timed steps (256 MiB write, outside the timed span)",
+           "parallelism": f"replicas{world}"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if fp64 else "f32 pairs / f64 positions",
-            "data": "synthetic", "config": cfg, "e2e": e2e, "gpu_launches": R["launches"],
+            "data": "synthetic", "config": cfg, "run": run, "e2e": e2e, "gpu_launches": R["launches"],
             "roofline": roof, "forms": forms_out, "clocks": clocks}
+    if rank == 0 and not args.no_precision and "fp64" in ok and "mixed" in ok:
+        line["precision_one_step"] = {"h_converge_0.01": precision_step(c, params),
+                                      "h_converge_1e-10": precision_step(c, params, 1e-10, record=False)}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(c, params)
     if rank == 0:

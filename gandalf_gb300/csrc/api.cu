@@ -116,6 +116,12 @@ struct gsph_ctx {
   cudaGraphExec_t kdk_exec = nullptr;
   int kdk_graph_steps = 0;
   unsigned kdk_graph_launches = 0;
+  // phase timing of gsph_kdk_steps: begin/end event pairs around each tree build, h solve
+  // and force pass (graph nodes when the steps are captured)
+  std::vector<cudaEvent_t> pev;
+  std::vector<int> pkind;
+  size_t pused = 0;
+  bool ptiming = false;
   // CUDA graph of the whole step (gsph_step_graph), valid for one capture key
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -166,6 +172,16 @@ void drop_graph(gsph_ctx* c) {
   c->graph_exec = nullptr;
   c->graph = nullptr;
   c->graph_valid = false;
+}
+
+// The K-step KDK graph: kept across gsph_kdk_setup calls while the buffers, the tree shape,
+// the recording setting and the KDK parameters it captured stay the same.
+void drop_kdk_graph(gsph_ctx* c) {
+  if (c->kdk_exec) cudaGraphExecDestroy(c->kdk_exec);
+  if (c->kdk_graph) cudaGraphDestroy(c->kdk_graph);
+  c->kdk_exec = nullptr;
+  c->kdk_graph = nullptr;
+  c->kdk_graph_steps = 0;
 }
 
 template <class T>
@@ -284,7 +300,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
     c->rec_bytes = 0;   // recording buffers were freed with the rest
     c->rec_sph_cnt = nullptr;
   }
-  if (fresh || n != c->n || ltot != c->ltot) drop_graph(c);
+  if (fresh || n != c->n || ltot != c->ltot) { drop_graph(c); drop_kdk_graph(c); }
   if (fresh || n != c->n) c->kdk = false;   // a new particle set restarts any integration
   if (fresh || n != c->n || ltot != c->ltot || !c->have_particles) {
     Shape s;
@@ -649,6 +665,7 @@ int ensure_recording(gsph_ctx* c) {
                       (size_t) c->nleaf * 2 * sizeof(unsigned long long);
   if (c->rec_sph_cnt && c->rec_bytes >= need) return GSPH_OK;
   drop_graph(c);   // a captured step holds the old recording buffers
+  drop_kdk_graph(c);
   int rc = alloc(c, c->rec_sph_cnt, c->n);
   if (!rc) rc = alloc(c, c->rec_sph_ids, (size_t) c->n * c->rec_max);
   if (!rc) rc = alloc(c, c->rec_dir_cnt, c->n);
@@ -1065,7 +1082,7 @@ int32_t gsph_get_stats(gsph_ctx* c, gsph_stats* out) {
 int32_t gsph_set_recording(gsph_ctx* c, int32_t enable, int32_t max_sph) {
   if (!c) return GSPH_ERR_INVALID;
   if (enable && (max_sph < 1 || max_sph > 4096)) return fail(c, GSPH_ERR_INVALID, "max_sph must be 1..4096");
-  if ((enable ? 1 : 0) != c->record || (enable && max_sph != c->rec_max)) drop_graph(c);
+  if ((enable ? 1 : 0) != c->record || (enable && max_sph != c->rec_max)) { drop_graph(c); drop_kdk_graph(c); }
   c->record = enable ? 1 : 0;
   if (enable && max_sph != c->rec_max) { c->rec_sph_cnt = nullptr; c->rec_bytes = 0; }
   c->rec_max = enable ? max_sph : 0;
@@ -1431,11 +1448,11 @@ const int kKeepField[kKeep] = {kFRho, kFInvOmega, kFZeta, kFHfactor, kFHrangesqd
                                kFAX, kFAY, kFAZ, kFAGX, kFAGY, kFAGZ, kFGpot, kFDudt, kFDivV, kFGpotHydro};
 
 void kdk_free(gsph_ctx* c) {
-  if (c->kdk_exec) cudaGraphExecDestroy(c->kdk_exec);
-  if (c->kdk_graph) cudaGraphDestroy(c->kdk_graph);
-  c->kdk_exec = nullptr;
-  c->kdk_graph = nullptr;
-  c->kdk_graph_steps = 0;
+  drop_kdk_graph(c);
+  for (cudaEvent_t e : c->pev) cudaEventDestroy(e);   // after the graph that records them
+  c->pev.clear();
+  c->pkind.clear();
+  c->pused = 0;
   for (void* q : {(void*) c->kg, (void*) c->kdk_buf, (void*) c->kdk_ibuf, (void*) c->kdk_flags,
                   (void*) c->leaf_active, (void*) c->leaf_level, (void*) c->leaf_lvn})
     if (q) cudaFree(q);
@@ -1493,6 +1510,41 @@ int kdk_pass(gsph_ctx* c, bool forces) {
 }
 
 constexpr int kKdkPasses = 3;   // the first force pass and up to two CheckTimesteps repeats
+enum { kPhBuild = 0, kPhDensity = 1, kPhForces = 2, kPhKinds = 3 };
+constexpr int kPhEventsPerStep = 2 * (1 + 2 * kKdkPasses);
+
+// One phase boundary: the next event of the pool, recorded on the context's stream.
+void pmark(gsph_ctx* c, int kind) {
+  if (!c->ptiming || c->pused >= c->pev.size()) return;
+  cudaEvent_t e = c->pev[c->pused];
+  c->pkind[c->pused] = kind;
+  c->pused++;
+  if (c->capturing) cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal);
+  else cudaEventRecord(e, c->stream);
+}
+
+// Events for nsteps steps of phase timing (created outside any capture).
+int ensure_phase_events(gsph_ctx* c, int nsteps) {
+  const size_t need = (size_t) kPhEventsPerStep * (size_t) nsteps;
+  while (c->pev.size() < need) {
+    cudaEvent_t e = nullptr;
+    GSPH_CUDA(cudaEventCreate(&e));
+    c->pev.push_back(e);
+  }
+  c->pkind.assign(c->pev.size(), -1);
+  c->pused = 0;
+  return GSPH_OK;
+}
+
+// Device time of each phase kind over the recorded pairs (after the stream has finished).
+void sum_phases(gsph_ctx* c, double* ms) {
+  for (int k = 0; k < kPhKinds; k++) ms[k] = 0.0;
+  for (size_t q = 0; q + 1 < c->pused; q += 2) {
+    float t = 0.0f;
+    if (c->pkind[q] >= 0 && cudaEventElapsedTime(&t, c->pev[q], c->pev[q + 1]) == cudaSuccess) ms[c->pkind[q]] += t;
+  }
+  (void) cudaGetLastError();
+}
 
 int kdk_step_body(gsph_ctx* c) {
   const KdkState s = make_kdk_state(c);
@@ -1500,17 +1552,24 @@ int kdk_step_body(gsph_ctx* c) {
   launch_kdk_begin(c->kg, c->stream);
   launch_kdk_advance(s, c->kp, c->kg, c->stream);
   c->launches += 2;
+  pmark(c, kPhBuild);
   int rc = do_build(c);
   if (rc) return rc;
+  pmark(c, kPhBuild);
   for (int pass = 0; pass < kKdkPasses; pass++) {
     // the tree is the same for all passes of a step: the first gathers every persistent
     // field into leaf order, the later ones only refresh the active flags and levels
     if (pass == 0) launch_kdk_gather(s, l, c->kg, c->stream);
     else launch_kdk_refresh(s, l, c->kg, c->stream);
     c->launches += 1;
+    pmark(c, kPhDensity);
     rc = do_props(c);
-    if (!rc) rc = do_forces(c, c->cfg.self_gravity != 0);
     if (rc) return rc;
+    pmark(c, kPhDensity);
+    pmark(c, kPhForces);
+    rc = do_forces(c, c->cfg.self_gravity != 0);
+    if (rc) return rc;
+    pmark(c, kPhForces);
     launch_kdk_scatter_lvn(s, l, c->stream);
     launch_kdk_check(s, c->kp, c->kg, pass == kKdkPasses - 1, c->stream);
     c->launches += pass == kKdkPasses - 1 ? 4 : 3;
@@ -1568,14 +1627,8 @@ int32_t gsph_kdk_setup(gsph_ctx* c, const gsph_kdk_config* k) {
     GSPH_CUDA(cudaMalloc(&c->leaf_lvn, sizeof(int) * k2));
     c->kdk_cap = c->cap;
   }
-  if (c->kdk_exec) cudaGraphExecDestroy(c->kdk_exec);
-  if (c->kdk_graph) cudaGraphDestroy(c->kdk_graph);
-  c->kdk_exec = nullptr;
-  c->kdk_graph = nullptr;
-  c->kdk_graph_steps = 0;
   drop_graph(c);   // the single-step graph was captured without the active flags
-  KdkParams& kp = c->kp;
-  kp = KdkParams{};
+  KdkParams kp{};
   kp.nlevels = k->nlevels;
   kp.level_diff_max = k->level_diff_max;
   kp.energy_integration = c->cfg.eos == GSPH_EOS_ENERGY_EQN;
@@ -1588,6 +1641,9 @@ int32_t gsph_kdk_setup(gsph_ctx* c, const gsph_kdk_config* k) {
     kp.boxmax[q] = c->cfg.boxmax[q];
     kp.boxsize[q] = c->cfg.boxmax[q] - c->cfg.boxmin[q];
   }
+  // the K-step graph holds the parameters by value: a new set needs a new capture
+  if (std::memcmp(&kp, &c->kp, sizeof(kp)) != 0) drop_kdk_graph(c);
+  c->kp = kp;
   c->kdk = true;
   const KdkState s = make_kdk_state(c);
   int rc = begin_counters(c);
@@ -1613,13 +1669,18 @@ int32_t gsph_kdk_setup(gsph_ctx* c, const gsph_kdk_config* k) {
 int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
   if (!c) return GSPH_ERR_INVALID;
   if (!c->kdk) return fail(c, GSPH_ERR_STATE, "gsph_kdk_setup has not been run for these particles");
+  if (c->nstar) return fail(c, GSPH_ERR_UNSUPPORTED, "star particles need the N-body integrator (not implemented)");
   if (nsteps < 1 || nsteps > 100000) return fail(c, GSPH_ERR_INVALID, "nsteps out of range");
   cudaSetDevice(c->device);
   int rc = begin_counters(c);
   if (rc) return rc;
   mark(c, 0);
   if (!use_graph) {
+    rc = ensure_phase_events(c, nsteps);
+    if (rc) return rc;
+    c->ptiming = true;
     for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c);
+    c->ptiming = false;
     if (rc) return rc;
   } else {
     if (!c->kdk_exec || c->kdk_graph_steps != nsteps) {
@@ -1628,12 +1689,16 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
       c->kdk_exec = nullptr;
       c->kdk_graph = nullptr;
       GSPH_CUDA(cudaStreamSynchronize(c->stream));
+      rc = ensure_phase_events(c, nsteps);   // the graph records these events on every replay
+      if (rc) return rc;
       cudaStream_t saved = c->stream;
       c->stream = c->own_stream;
       const unsigned before = c->launches;
       GSPH_CUDA(cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeRelaxed));
       c->capturing = true;
+      c->ptiming = true;
       for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c);
+      c->ptiming = false;
       c->capturing = false;
       cudaGraph_t g = nullptr;
       const cudaError_t e = cudaStreamEndCapture(c->own_stream, &g);
@@ -1654,7 +1719,14 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
   float ms = 0.0f;
   if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]) != cudaSuccess) ms = 0.0f;
   (void) cudaGetLastError();
-  c->last.ms_build = c->last.ms_density = c->last.ms_hmax = c->last.ms_forces = 0.0f;
+  double ph[kPhKinds];
+  sum_phases(c, ph);
+  // summed over the steps; the h solve phase includes the hmax update, the thermal update
+  // and the mixed form's mirror refresh that follow it
+  c->last.ms_build = ph[kPhBuild];
+  c->last.ms_density = ph[kPhDensity];
+  c->last.ms_hmax = 0.0;
+  c->last.ms_forces = ph[kPhForces];
   c->last.ms_total = ms;
   c->have_tree = c->have_props = c->have_forces = true;
   return rc;

@@ -194,14 +194,18 @@ class GradhSphTree:
         self._check(self._lib.gsph_kdk_get_status(self._ctx, ctypes.byref(st)), "kdk_status")
         return {k: getattr(st, k) for k, _ in _native.KdkStatus._fields_}
 
-    def kdk_state(self, name: str) -> np.ndarray:
-        out = np.empty(self.n, dtype=np.float64)
+    def kdk_state(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        """One integration field (input order); ``out``: an n-double array to fill."""
+        if out is None:
+            out = np.empty(self.n, dtype=np.float64)
         self._check(self._lib.gsph_kdk_get_state(self._ctx, _native.KDK_FIELDS.index(name), _dp(out)), "kdk_state")
         return out
 
     # ---- results --------------------------------------------------------------------------
-    def field(self, name: str) -> np.ndarray:
-        out = np.empty(self.n, dtype=np.float64)
+    def field(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        """One result field (input order); ``out``: an n-double array to fill."""
+        if out is None:
+            out = np.empty(self.n, dtype=np.float64)
         self._check(self._lib.gsph_get_field(self._ctx, _native.FIELD_ID[name], _dp(out)), "get_field")
         return out
 
@@ -236,6 +240,19 @@ class GradhSphTree:
         if r < 0:
             self._check(int(r), "sph_neighbours")
         return [ids[off[i]:off[i + 1]] for i in range(self.n)]
+
+    def sph_neighbours_csr(self):
+        """The recorded SPH neighbour lists as CSR arrays (offsets n+1, input ids)."""
+        tot = self._lib.gsph_get_sph_neighbours(self._ctx, None, None)
+        if tot < 0:
+            self._check(int(tot), "sph_neighbours")
+        off = np.zeros(self.n + 1, dtype=np.int64)
+        ids = np.zeros(max(int(tot), 1), dtype=np.int32)
+        r = self._lib.gsph_get_sph_neighbours(self._ctx, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                              ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        if r < 0:
+            self._check(int(r), "sph_neighbours")
+        return off, ids[:int(tot)]
 
     def direct_summary(self):
         cnt = np.zeros(self.n, dtype=np.int64)

@@ -95,3 +95,28 @@ def test_kdk_mixed_tracks_fp64():
         assert np.sqrt(np.mean((a[k] - b[k]) ** 2)) <= 1e-6, k
     e = np.abs(a["rho"] - b["rho"]) / a["rho"]
     assert np.sqrt(np.mean(e * e)) <= 1e-4
+
+
+def test_kdk_matches_oracle_main_loop_on_the_cloud():
+    """The headline configuration's shape at 32,768 particles: setup plus 6 KDK steps of
+    the rotating cloud (4 levels), FP64 GPU form against the oracle's main loop.  Levels,
+    step lengths and neighbour levels exactly; positions and solved fields to FP64
+    summation-order differences."""
+    from oracle import oracle
+    c = ics_mod.rotating_cloud(32768, seed=47)
+    params = c.pop("params")
+    kdk = c.pop("kdk")
+    out, st = run(c, params, kdk, precision="fp64", nsteps=6)
+    r = oracle.kdk(c, params, kdk, 6)
+    ref, glob = r["state"], r["global"]
+    assert st["status"] == 0 and r["status"] == 0
+    assert st["n"] == glob["n"] and st["level_max"] == glob["level_max"] and st["nsteps"] == glob["Nsteps"]
+    assert abs(st["t"] - glob["t"]) <= 1e-12 * abs(glob["t"])
+    for k in ("level", "nstep", "nlast", "levelneib"):
+        np.testing.assert_array_equal(out[k], ref[k], err_msg=k)
+    for k in ("x", "y", "z"):
+        assert np.max(np.abs(out[k] - ref[k])) <= 1e-10, k
+    for k, tol in (("h", 1e-10), ("rho", 1e-10), ("ax", 1e-8), ("gpot", 1e-10)):
+        assert rel(out[k], ref[k]) <= tol, (k, rel(out[k], ref[k]))
+    # the active particle updates agree with the oracle's count
+    assert st["active_updates"] == r["setup_updates"] + r["step_updates"]
