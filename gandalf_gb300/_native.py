@@ -51,7 +51,10 @@ class Config(ctypes.Structure):
 class FieldOffsets(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in (
         "r", "v", "m", "h", "u", "rho", "invomega", "zeta", "hfactor", "hrangesqd", "pressure",
-        "sound", "div_v", "dudt", "a", "atree", "gpot", "gpot_hydro")]
+        "sound", "div_v", "dudt", "a", "atree", "gpot", "gpot_hydro", "flags", "level", "levelneib")]
+
+
+GSPH_FLAG_ACTIVE = 2   # the reference's `active` particle flag bit
 
 
 class Stats(ctypes.Structure):
@@ -90,6 +93,8 @@ SIGNATURES = {
     "gsph_get_field": (_I32, [_P, _I32, _D]),
     "gsph_get_field_device": (_I32, [_P, _I32, _P]),
     "gsph_get_particles_aos": (_I32, [_P, _P, _I64, _I64, ctypes.POINTER(FieldOffsets)]),
+    "gsph_update_active_particle_counters": (_I32, [_P, _P, _I64, _I64, ctypes.POINTER(FieldOffsets)]),
+    "gsph_get_maximum_smoothing_length": (_I32, [_P, _D]),
     "gsph_get_stats": (_I32, [_P, ctypes.POINTER(Stats)]),
     "gsph_set_recording": (_I32, [_P, _I32, _I32]),
     "gsph_get_sph_neighbours": (_I64, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]),
@@ -116,7 +121,7 @@ SIGNATURES = {
     "gsph_batch_stats": (_I32, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)]),
 }
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 _lib = None
 

@@ -77,10 +77,13 @@ struct gsph_ctx {
   double* ibox = nullptr;
   unsigned long long* counters = nullptr;    // [0] status, [1..5] counts
   double* scratch_out = nullptr;             // n doubles for field scatter
-  // array-of-structures staging
-  void* aos = nullptr;
+  // array-of-structures import / export
+  void* aos = nullptr;                 // device copy of records that are not page-locked
   size_t aos_bytes = 0;
   int64_t aos_stride = 0;
+  bool bactive = false;                // records carry flags: block-timestep semantics
+  double* aos_out = nullptr;           // staged write-back: fields x n, input order
+  size_t aos_out_bytes = 0;
   // recording
   int record = 0, rec_max = 0;
   int* rec_sph_cnt = nullptr;
@@ -165,6 +168,9 @@ void free_all(gsph_ctx* c) {
 }
 
 void kdk_free(gsph_ctx* c);
+KdkState make_kdk_state(gsph_ctx* c);
+KdkLeaf make_kdk_leaf(gsph_ctx* c);
+int ensure_kdk_buffers(gsph_ctx* c);
 
 void drop_graph(gsph_ctx* c) {
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
@@ -376,7 +382,7 @@ Particles make_particles(gsph_ctx* c) {
   p.ax = f[kFAX]; p.ay = f[kFAY]; p.az = f[kFAZ]; p.agx = f[kFAGX]; p.agy = f[kFAGY]; p.agz = f[kFAGZ];
   p.gpot = f[kFGpot]; p.dudt = f[kFDudt]; p.div_v = f[kFDivV]; p.gpot_hydro = f[kFGpotHydro];
   p.invh_p = f[kFInvH]; p.invrho_p = f[kFInvRho]; p.fac_p = f[kFFac];
-  if (c->kdk) { p.active = c->leaf_active; p.level = c->leaf_level; p.lvn = c->leaf_lvn; }
+  if (c->kdk || c->bactive) { p.active = c->leaf_active; p.level = c->leaf_level; p.lvn = c->leaf_lvn; }
   return p;
 }
 
@@ -451,7 +457,18 @@ int validate_host(gsph_ctx* c, int64_t n, const double* const* a) {
 
 struct OutPtrs { double* p[9]; };
 
-__global__ void k_unpack_aos(const unsigned char* base, int n, int64_t stride, gsph_field_offsets off, OutPtrs o) {
+// A record field read as a double / int32 (offset -1: absent, the default).
+__device__ __forceinline__ double rec_d(const unsigned char* r, int64_t o, double dflt = 0.0) {
+  return o >= 0 ? *reinterpret_cast<const double*>(r + o) : dflt;
+}
+__device__ __forceinline__ int rec_i(const unsigned char* r, int64_t o, int dflt = 0) {
+  return o >= 0 ? *reinterpret_cast<const int*>(r + o) : dflt;
+}
+
+// Records -> input-order device arrays.  With state: the flags (active bit), levels and the
+// solved state of every particle (kept by the inactive ones) into the block-timestep state.
+__global__ void k_unpack_aos(const unsigned char* base, int n, int64_t stride, gsph_field_offsets off, OutPtrs o,
+                             KdkState s, int with_state) {
   double* const* dst = o.p;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const unsigned char* r = base + (size_t) i * stride;
@@ -462,22 +479,67 @@ __global__ void k_unpack_aos(const unsigned char* base, int n, int64_t stride, g
     dst[6][i] = *reinterpret_cast<const double*>(r + off.m);
     dst[7][i] = *reinterpret_cast<const double*>(r + off.u);
     dst[8][i] = *reinterpret_cast<const double*>(r + off.h);
+    if (!with_state) continue;
+    s.flags[i] = (rec_i(r, off.flags) & (int) GSPH_FLAG_ACTIVE) ? kFlagActive : (unsigned char) 0;
+    s.level[i] = rec_i(r, off.level);
+    s.levelneib[i] = rec_i(r, off.levelneib);
+    // keep[] order: rho invomega zeta hfactor hrangesqd pressure sound ax ay az agx agy agz
+    // gpot dudt div_v gpot_hydro (integrate.cuh)
+    const int64_t ko[kKeep] = {off.rho, off.invomega, off.zeta, off.hfactor, off.hrangesqd, off.pressure, off.sound,
+                               off.a, off.a >= 0 ? off.a + 8 : -1, off.a >= 0 ? off.a + 16 : -1,
+                               off.atree, off.atree >= 0 ? off.atree + 8 : -1, off.atree >= 0 ? off.atree + 16 : -1,
+                               off.gpot, off.dudt, off.div_v, off.gpot_hydro};
+#pragma unroll
+    for (int q = 0; q < kKeep; q++) s.keep[q][i] = rec_d(r, ko[q], q == 1 ? 1.0 : 0.0);
+  }
+}
+
+// Flags and levels only (the records after CheckTimesteps), input order.
+__global__ void k_unpack_flags(const unsigned char* base, int n, int64_t stride, gsph_field_offsets off, KdkState s) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned char* r = base + (size_t) i * stride;
+    s.flags[i] = (rec_i(r, off.flags) & (int) GSPH_FLAG_ACTIVE) ? kFlagActive : (unsigned char) 0;
+    s.level[i] = rec_i(r, off.level);
   }
 }
 
 struct FieldPtrs { const double* f[kNumFields]; };
 
-__global__ void k_pack_aos(unsigned char* base, int n, int64_t stride, gsph_field_offsets off, FieldPtrs fp,
-                           const int* __restrict__ id, int gpot_hydro_field) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-    unsigned char* r = base + (size_t) id[s] * stride;
-    auto put = [&](int64_t o, int fld) { if (o >= 0) *reinterpret_cast<double*>(r + o) = fp.f[fld][s]; };
-    put(off.h, kFH); put(off.u, kFU); put(off.rho, kFRho); put(off.invomega, kFInvOmega);
-    put(off.zeta, kFZeta); put(off.hfactor, kFHfactor); put(off.hrangesqd, kFHrangesqd);
-    put(off.pressure, kFPressure); put(off.sound, kFSound); put(off.div_v, kFDivV); put(off.dudt, kFDudt);
-    put(off.gpot, kFGpot); put(off.gpot_hydro, gpot_hydro_field);
-    if (off.a >= 0) { put(off.a, kFAX); put(off.a + 8, kFAY); put(off.a + 16, kFAZ); }
-    if (off.atree >= 0) { put(off.atree, kFAGX); put(off.atree + 8, kFAGY); put(off.atree + 16, kFAGZ); }
+// The output fields one write-back stores: leaf-order field index and byte offset.
+constexpr int kMaxOut = 24;
+struct OutTable {
+  int nf;
+  int fidx[kMaxOut];
+  int64_t foff[kMaxOut];
+};
+
+// Results straight into page-locked host records (device-visible address), slot order.
+__global__ void k_write_aos_direct(unsigned char* base, int n, int64_t stride, OutTable t, FieldPtrs fp,
+                                   const int* __restrict__ id, const unsigned char* __restrict__ active,
+                                   const int* __restrict__ lvn, int64_t off_lvn) {
+  for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < n; sl += gridDim.x * blockDim.x) {
+    unsigned char* r = base + (size_t) id[sl] * stride;
+    if (lvn && off_lvn >= 0) {
+      int* L = reinterpret_cast<int*>(r + off_lvn);
+      const int v = lvn[sl];
+      if (v > *L) *L = v;
+    }
+    if (active && !active[sl]) continue;
+    for (int q = 0; q < t.nf; q++) *reinterpret_cast<double*>(r + t.foff[q]) = fp.f[t.fidx[q]][sl];
+  }
+}
+
+// Staged write-back: the output fields, the active flags and the neighbour levels in input
+// order into one compact device buffer (fields x n doubles, then n ints, then n bytes).
+__global__ void k_pack_out(int n, OutTable t, FieldPtrs fp, const int* __restrict__ slot_of,
+                           const unsigned char* __restrict__ active, const int* __restrict__ lvn, double* out) {
+  int* lv = reinterpret_cast<int*>(out + (size_t) t.nf * n);
+  unsigned char* ac = reinterpret_cast<unsigned char*>(lv + n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int sl = slot_of[i];
+    for (int q = 0; q < t.nf; q++) out[(size_t) q * n + i] = fp.f[t.fidx[q]][sl];
+    lv[i] = lvn ? lvn[sl] : 0;
+    ac[i] = active ? active[sl] : (unsigned char) 1;
   }
 }
 
@@ -568,6 +630,12 @@ int do_build(gsph_ctx* c) {
   a.tree = make_tree(c);
   a.thetamaxsqd = c->cfg.thetamaxsqd;
   c->launches += (unsigned) launch_build_tree(a, c->stream);
+  if (c->bactive) {
+    // records with flags: active flags, levels and the solved state of every particle
+    // into leaf order (the inactive particles keep theirs)
+    launch_kdk_gather(make_kdk_state(c), make_kdk_leaf(c), c->kg, c->stream);
+    c->launches += 1;
+  }
   if (mixed(c)) {
     launch_mixed_prep_build(a.tree, a.p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
     c->launches += 2;
@@ -598,7 +666,7 @@ int do_props(gsph_ctx* c) {
   mark(c, 2);
   launch_update_hmax(t, p, c->stream);
   c->launches += 1;
-  if (c->kdk) {   // every particle's thermal properties before the force pass
+  if (c->kdk || c->bactive) {   // every particle's thermal properties before the force pass
     launch_kdk_thermal(p, make_params(c), c->stream);
     c->launches += 1;
   }
@@ -677,6 +745,51 @@ int ensure_recording(gsph_ctx* c) {
   return GSPH_OK;
 }
 
+// A new particle set through the structure-of-arrays imports: every particle active, and
+// any KDK integration must be set up again.
+void leave_flag_mode(gsph_ctx* c) {
+  if (c->bactive) drop_graph(c);
+  c->bactive = false;
+  c->kdk = false;
+}
+
+// Device-visible address of host records [p, p + bytes) when they lie in one page-locked
+// (or managed) allocation; nullptr when the records must be staged through a copy.
+unsigned char* device_view(const void* p, size_t bytes) {
+  cudaPointerAttributes a0{}, a1{};
+  const unsigned char* q = static_cast<const unsigned char*>(p);
+  if (cudaPointerGetAttributes(&a0, q) != cudaSuccess || cudaPointerGetAttributes(&a1, q + bytes - 1) != cudaSuccess) {
+    (void) cudaGetLastError();
+    return nullptr;
+  }
+  if (a0.type == cudaMemoryTypeManaged && a1.type == cudaMemoryTypeManaged) return const_cast<unsigned char*>(q);
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  unsigned char* d0 = static_cast<unsigned char*>(a0.devicePointer);
+  unsigned char* d1 = static_cast<unsigned char*>(a1.devicePointer);
+  return (d1 - d0 == (std::ptrdiff_t) (bytes - 1)) ? d0 : nullptr;
+}
+
+// Checks shared by the record imports and exports.
+int check_offsets(gsph_ctx* c, int64_t n, int64_t stride, const gsph_field_offsets* off, bool need_flags) {
+  if (n < 1 || n > (int64_t) 1 << 30 || stride < 8 || (stride % 8) != 0)
+    return fail(c, GSPH_ERR_INVALID, "bad array-of-structures description");
+  const int64_t ins[5] = {off->r, off->v, off->m, off->h, off->u};
+  for (int q = 0; q < 5; q++)
+    if (ins[q] < 0 || ins[q] % 8 != 0 || ins[q] + (q < 2 ? 24 : 8) > stride)
+      return fail(c, GSPH_ERR_INVALID, "input field offset outside the record or misaligned");
+  const int64_t outs[] = {off->rho, off->invomega, off->zeta, off->hfactor, off->hrangesqd, off->pressure,
+                          off->sound, off->div_v, off->dudt, off->gpot, off->gpot_hydro};
+  for (int64_t o : outs)
+    if (o >= 0 && (o % 8 != 0 || o + 8 > stride)) return fail(c, GSPH_ERR_INVALID, "output offset outside the record");
+  for (int64_t o : {off->a, off->atree})
+    if (o >= 0 && (o % 8 != 0 || o + 24 > stride)) return fail(c, GSPH_ERR_INVALID, "output offset outside the record");
+  for (int64_t o : {off->flags, off->level, off->levelneib})
+    if (o >= 0 && (o % 4 != 0 || o + 4 > stride)) return fail(c, GSPH_ERR_INVALID, "integer field offset outside the record");
+  if (need_flags && off->flags < 0) return fail(c, GSPH_ERR_INVALID, "the records' flags offset is needed");
+  return GSPH_OK;
+}
+
 }  // namespace
 
 // ======================================================================================
@@ -740,6 +853,7 @@ void gsph_destroy(gsph_ctx* c) {
   kdk_free(c);
   free_all(c);
   if (c->aos) cudaFree(c->aos);
+  if (c->aos_out) cudaFree(c->aos_out);
   if (c->star_buf) cudaFree(c->star_buf);
   if (c->star_f) cudaFree(c->star_f);
   for (int q = 0; q < 5; q++) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
@@ -770,6 +884,7 @@ int32_t gsph_set_particles(gsph_ctx* c, int64_t n, const double* x, const double
   if (rc) return rc;
   for (int q = 0; q < 9; q++)
     GSPH_CUDA(cudaMemcpyAsync(c->in[q], a[q], sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, c->stream));
+  leave_flag_mode(c);
   c->have_particles = true;
   c->have_tree = c->have_props = c->have_forces = false;
   return GSPH_OK;
@@ -787,6 +902,7 @@ int32_t gsph_set_particles_device(gsph_ctx* c, int64_t n, const double* x, const
   if (rc) return rc;
   for (int q = 0; q < 9; q++)
     GSPH_CUDA(cudaMemcpyAsync(c->in[q], a[q], sizeof(double) * (size_t) n, cudaMemcpyDeviceToDevice, c->stream));
+  leave_flag_mode(c);
   c->have_particles = true;
   c->have_tree = c->have_props = c->have_forces = false;
   return GSPH_OK;
@@ -794,33 +910,82 @@ int32_t gsph_set_particles_device(gsph_ctx* c, int64_t n, const double* x, const
 
 int32_t gsph_set_particles_aos(gsph_ctx* c, const void* base, int64_t n, int64_t stride, const gsph_field_offsets* off) {
   if (!c) return GSPH_ERR_INVALID;
-  if (!base || !off || n < 1 || n > (int64_t) 1 << 30 || stride < 8 || (stride % 8) != 0)
-    return fail(c, GSPH_ERR_INVALID, "bad array-of-structures description");
-  const int64_t ins[5] = {off->r, off->v, off->m, off->h, off->u};
-  for (int q = 0; q < 5; q++)
-    if (ins[q] < 0 || ins[q] % 8 != 0 || ins[q] + (q < 2 ? 24 : 8) > stride)
-      return fail(c, GSPH_ERR_INVALID, "input field offset outside the record or misaligned");
-  cudaSetDevice(c->device);
-  int rc = ensure_capacity(c, (int) n);
+  if (!base || !off) return fail(c, GSPH_ERR_INVALID, "bad array-of-structures description");
+  int rc = check_offsets(c, n, stride, off, false);
   if (rc) return rc;
+  cudaSetDevice(c->device);
+  rc = ensure_capacity(c, (int) n);
+  if (rc) return rc;
+  const bool flags = off->flags >= 0;
+  if (flags) {
+    rc = ensure_kdk_buffers(c);
+    if (rc) return rc;
+  }
+  if (flags != c->bactive) drop_graph(c);   // the step graph gathers the state only with flags
+  c->bactive = flags;
+  c->kdk = false;
   const size_t bytes = (size_t) n * (size_t) stride;
-  if (bytes > c->aos_bytes) {
-    if (c->aos) cudaFree(c->aos);
-    c->aos = nullptr;
-    c->aos_bytes = 0;
-    GSPH_CUDA(cudaMalloc(&c->aos, bytes));
-    c->aos_bytes = bytes;
+  const unsigned char* src = device_view(base, bytes);
+  if (!src) {   // pageable records: one copy of the whole array, unpacked on the device
+    if (bytes > c->aos_bytes) {
+      if (c->aos) cudaFree(c->aos);
+      c->aos = nullptr;
+      c->aos_bytes = 0;
+      GSPH_CUDA(cudaMalloc(&c->aos, bytes));
+      c->aos_bytes = bytes;
+    }
+    GSPH_CUDA(cudaMemcpyAsync(c->aos, base, bytes, cudaMemcpyHostToDevice, c->stream));
+    src = static_cast<const unsigned char*>(c->aos);
   }
   c->aos_stride = stride;
-  GSPH_CUDA(cudaMemcpyAsync(c->aos, base, bytes, cudaMemcpyHostToDevice, c->stream));
   OutPtrs o;
   for (int q = 0; q < 9; q++) o.p[q] = c->in[q];
-  k_unpack_aos<<<grid1((int) n), 256, 0, c->stream>>>(static_cast<const unsigned char*>(c->aos), (int) n, stride,
-                                                      *off, o);
+  KdkState ks{};
+  if (flags) ks = make_kdk_state(c);
+  k_unpack_aos<<<grid1((int) n), 256, 0, c->stream>>>(src, (int) n, stride, *off, o, ks, flags ? 1 : 0);
   rc = check_launch(c, "unpack");
   if (rc) return rc;
+  if (src != c->aos) GSPH_CUDA(cudaStreamSynchronize(c->stream));   // the caller may change the records
   c->have_particles = true;
   c->have_tree = c->have_props = c->have_forces = false;
+  return GSPH_OK;
+}
+
+int32_t gsph_update_active_particle_counters(gsph_ctx* c, const void* base, int64_t n, int64_t stride,
+                                             const gsph_field_offsets* off) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!base || !off) return fail(c, GSPH_ERR_INVALID, "bad array-of-structures description");
+  int rc = check_offsets(c, n, stride, off, true);
+  if (rc) return rc;
+  if (!c->bactive || n != c->n || stride != c->aos_stride)
+    return fail(c, GSPH_ERR_STATE, "records with flags were not imported with gsph_set_particles_aos");
+  if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "tree not built");
+  cudaSetDevice(c->device);
+  const size_t bytes = (size_t) n * (size_t) stride;
+  const unsigned char* src = device_view(base, bytes);
+  if (!src) {
+    if (bytes > c->aos_bytes) return fail(c, GSPH_ERR_STATE, "record staging buffer too small");
+    GSPH_CUDA(cudaMemcpyAsync(c->aos, base, bytes, cudaMemcpyHostToDevice, c->stream));
+    src = static_cast<const unsigned char*>(c->aos);
+  }
+  const KdkState ks = make_kdk_state(c);
+  k_unpack_flags<<<grid1((int) n), 256, 0, c->stream>>>(src, (int) n, stride, *off, ks);
+  launch_kdk_refresh(ks, make_kdk_leaf(c), c->kg, c->stream);   // leaf-order flags, levels; levelneib restarts
+  rc = check_launch(c, "update active counters");
+  if (rc) return rc;
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_props = c->have_forces = false;
+  return GSPH_OK;
+}
+
+int32_t gsph_get_maximum_smoothing_length(gsph_ctx* c, double* hmax) {
+  if (!c || !hmax) return GSPH_ERR_INVALID;
+  if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "tree not built");
+  cudaSetDevice(c->device);
+  CellGeom g{};
+  GSPH_CUDA(cudaMemcpyAsync(&g, c->geom, sizeof(g), cudaMemcpyDeviceToHost, c->stream));
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  *hmax = g.hmax;
   return GSPH_OK;
 }
 
@@ -1051,24 +1216,72 @@ int32_t gsph_get_field(gsph_ctx* c, int32_t field, double* out) {
 
 int32_t gsph_get_particles_aos(gsph_ctx* c, void* base, int64_t n, int64_t stride, const gsph_field_offsets* off) {
   if (!c || !base || !off) return GSPH_ERR_INVALID;
-  if (!c->aos || n != c->n || stride != c->aos_stride)
-    return fail(c, GSPH_ERR_STATE, "records were not imported with gsph_set_particles_aos");
+  int rc = check_offsets(c, n, stride, off, false);
+  if (rc) return rc;
+  if (!c->have_particles || n != c->n) return fail(c, GSPH_ERR_STATE, "record count differs from the imported set");
+  if (c->bactive && off->flags < 0)
+    return fail(c, GSPH_ERR_INVALID, "the particles were imported with flags: pass the same offsets");
   if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "no results yet");
-  const int64_t outs[] = {off->rho, off->invomega, off->zeta, off->hfactor, off->hrangesqd, off->pressure,
-                          off->sound, off->div_v, off->dudt, off->gpot, off->gpot_hydro, off->h, off->u};
-  for (int64_t o : outs)
-    if (o >= 0 && (o % 8 != 0 || o + 8 > stride)) return fail(c, GSPH_ERR_INVALID, "output offset outside the record");
-  for (int64_t o : {off->a, off->atree})
-    if (o >= 0 && (o % 8 != 0 || o + 24 > stride)) return fail(c, GSPH_ERR_INVALID, "output offset outside the record");
   cudaSetDevice(c->device);
+  // the fields computed since the import
+  OutTable t{};
+  auto add = [&](int64_t o, int fld) {
+    if (o >= 0 && t.nf < kMaxOut) { t.fidx[t.nf] = fld; t.foff[t.nf] = o; t.nf++; }
+  };
+  if (c->have_props) {
+    add(off->h, kFH); add(off->u, kFU); add(off->rho, kFRho); add(off->invomega, kFInvOmega);
+    add(off->zeta, kFZeta); add(off->hfactor, kFHfactor); add(off->hrangesqd, kFHrangesqd);
+    add(off->pressure, kFPressure); add(off->sound, kFSound);
+  }
+  if (c->have_forces) {
+    add(off->div_v, kFDivV); add(off->dudt, kFDudt); add(off->gpot, kFGpot);
+    add(off->gpot_hydro, c->nstar ? kFGpotHydro : kFGpot);
+    if (off->a >= 0) { add(off->a, kFAX); add(off->a + 8, kFAY); add(off->a + 16, kFAZ); }
+    if (off->atree >= 0) { add(off->atree, kFAGX); add(off->atree + 8, kFAGY); add(off->atree + 16, kFAGZ); }
+  }
+  const unsigned char* act = c->bactive ? c->leaf_active : nullptr;
+  const int* lvn = (c->bactive && c->have_forces && off->levelneib >= 0) ? c->leaf_lvn : nullptr;
+  if (t.nf == 0 && !lvn) return GSPH_OK;
   FieldPtrs fp;
   for (int q = 0; q < kNumFields; q++) fp.f[q] = c->f[q];
-  k_pack_aos<<<grid1(c->n), 256, 0, c->stream>>>(static_cast<unsigned char*>(c->aos), c->n, stride, *off, fp, c->id,
-                                                  c->nstar ? kFGpotHydro : kFGpot);
-  int rc = check_launch(c, "pack");
+  const size_t bytes = (size_t) n * (size_t) stride;
+  unsigned char* dst = device_view(base, bytes);
+  if (dst) {   // page-locked records: written in place, only the output fields
+    k_write_aos_direct<<<grid1(c->n), 256, 0, c->stream>>>(dst, c->n, stride, t, fp, c->id, act, lvn, off->levelneib);
+    rc = check_launch(c, "write records");
+    if (rc) return rc;
+    GSPH_CUDA(cudaStreamSynchronize(c->stream));
+    return GSPH_OK;
+  }
+  // pageable records: compact buffer (fields, neighbour levels, active flags; input order)
+  const size_t need = sizeof(double) * (size_t) t.nf * (size_t) n + (sizeof(int) + 1) * (size_t) n;
+  if (need > c->aos_out_bytes) {
+    if (c->aos_out) cudaFree(c->aos_out);
+    c->aos_out = nullptr;
+    c->aos_out_bytes = 0;
+    GSPH_CUDA(cudaMalloc(&c->aos_out, need));
+    c->aos_out_bytes = need;
+  }
+  k_pack_out<<<grid1(c->n), 256, 0, c->stream>>>(c->n, t, fp, c->slot_of, act, lvn, c->aos_out);
+  rc = check_launch(c, "pack outputs");
   if (rc) return rc;
-  GSPH_CUDA(cudaMemcpyAsync(base, c->aos, (size_t) n * (size_t) stride, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<unsigned char> h(need);
+  GSPH_CUDA(cudaMemcpyAsync(h.data(), c->aos_out, need, cudaMemcpyDeviceToHost, c->stream));
   GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  const double* fv = reinterpret_cast<const double*>(h.data());
+  const int* lv = reinterpret_cast<const int*>(fv + (size_t) t.nf * n);
+  const unsigned char* ac = reinterpret_cast<const unsigned char*>(lv + n);
+  unsigned char* rec0 = static_cast<unsigned char*>(base);
+  for (int64_t i = 0; i < n; i++) {
+    unsigned char* r = rec0 + (size_t) i * (size_t) stride;
+    if (lvn) {
+      int cur;
+      std::memcpy(&cur, r + off->levelneib, sizeof(int));
+      if (lv[i] > cur) std::memcpy(r + off->levelneib, &lv[i], sizeof(int));
+    }
+    if (!ac[i]) continue;
+    for (int q = 0; q < t.nf; q++) std::memcpy(r + t.foff[q], &fv[(size_t) q * n + i], sizeof(double));
+  }
   return GSPH_OK;
 }
 
@@ -1462,6 +1675,24 @@ void kdk_free(gsph_ctx* c) {
   c->kdk = false;
 }
 
+// Block-timestep state buffers (integration state, keep[] fields, flags, levels) for the
+// current capacity; shared by the KDK integration and the record imports with flags.
+int ensure_kdk_buffers(gsph_ctx* c) {
+  if (c->kdk_cap >= c->cap && c->kg) return GSPH_OK;
+  kdk_free(c);
+  const size_t k2 = (size_t) c->cap;
+  GSPH_CUDA(cudaMalloc(&c->kg, sizeof(KdkGlobal)));
+  GSPH_CUDA(cudaMemsetAsync(c->kg, 0, sizeof(KdkGlobal), c->stream));
+  GSPH_CUDA(cudaMalloc(&c->kdk_buf, sizeof(double) * (14 + kKeep) * k2));
+  GSPH_CUDA(cudaMalloc(&c->kdk_ibuf, sizeof(int) * 4 * k2));
+  GSPH_CUDA(cudaMalloc(&c->kdk_flags, k2));
+  GSPH_CUDA(cudaMalloc(&c->leaf_active, k2));
+  GSPH_CUDA(cudaMalloc(&c->leaf_level, sizeof(int) * k2));
+  GSPH_CUDA(cudaMalloc(&c->leaf_lvn, sizeof(int) * k2));
+  c->kdk_cap = c->cap;
+  return GSPH_OK;
+}
+
 KdkState make_kdk_state(gsph_ctx* c) {
   KdkState s{};
   const size_t k = (size_t) c->kdk_cap;
@@ -1615,19 +1846,10 @@ int32_t gsph_kdk_setup(gsph_ctx* c, const gsph_kdk_config* k) {
   if (c->nstar) return fail(c, GSPH_ERR_UNSUPPORTED, "star particles need the N-body integrator (not implemented)");
   cudaSetDevice(c->device);
   GSPH_CUDA(cudaStreamSynchronize(c->stream));
-  if (c->kdk_cap < c->cap) {
-    kdk_free(c);
-    const size_t k2 = (size_t) c->cap;
-    GSPH_CUDA(cudaMalloc(&c->kg, sizeof(KdkGlobal)));
-    GSPH_CUDA(cudaMalloc(&c->kdk_buf, sizeof(double) * (14 + kKeep) * k2));
-    GSPH_CUDA(cudaMalloc(&c->kdk_ibuf, sizeof(int) * 4 * k2));
-    GSPH_CUDA(cudaMalloc(&c->kdk_flags, k2));
-    GSPH_CUDA(cudaMalloc(&c->leaf_active, k2));
-    GSPH_CUDA(cudaMalloc(&c->leaf_level, sizeof(int) * k2));
-    GSPH_CUDA(cudaMalloc(&c->leaf_lvn, sizeof(int) * k2));
-    c->kdk_cap = c->cap;
-  }
+  int rc0 = ensure_kdk_buffers(c);
+  if (rc0) return rc0;
   drop_graph(c);   // the single-step graph was captured without the active flags
+  c->bactive = false;
   KdkParams kp{};
   kp.nlevels = k->nlevels;
   kp.level_diff_max = k->level_diff_max;

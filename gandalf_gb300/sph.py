@@ -144,10 +144,25 @@ class GradhSphTree:
         self._check(rc, "set_particles_aos")
 
     def get_particles_aos(self, records: np.ndarray, offsets: dict):
+        """Write the computed output fields into the records (only those; with a flags
+        offset only the active particles', plus levelneib of every particle)."""
         off = _native.FieldOffsets(**{k: int(offsets.get(k, -1)) for k, _ in _native.FieldOffsets._fields_})
         rc = self._lib.gsph_get_particles_aos(self._ctx, records.ctypes.data, len(records),
                                               records.dtype.itemsize, ctypes.byref(off))
         self._check(rc, "get_particles_aos")
+
+    def UpdateActiveParticleCounters(self, records: np.ndarray, offsets: dict):
+        """Re-read the records' flags and levels into the current tree (no rebuild)."""
+        off = _native.FieldOffsets(**{k: int(offsets.get(k, -1)) for k, _ in _native.FieldOffsets._fields_})
+        rc = self._lib.gsph_update_active_particle_counters(self._ctx, records.ctypes.data, len(records),
+                                                            records.dtype.itemsize, ctypes.byref(off))
+        self._check(rc, "UpdateActiveParticleCounters")
+
+    def GetMaximumSmoothingLength(self) -> float:
+        out = ctypes.c_double()
+        self._check(self._lib.gsph_get_maximum_smoothing_length(self._ctx, ctypes.byref(out)),
+                    "GetMaximumSmoothingLength")
+        return out.value
 
     # ---- the reference's virtual interface ----------------------------------------------
     def BuildTree(self):

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define GSPH_ABI_VERSION 2
+#define GSPH_ABI_VERSION 3
 
 #define GSPH_OK 0
 #define GSPH_ERR_INVALID -1        /* bad argument or particle data */
@@ -72,13 +72,27 @@ typedef struct gsph_config {
   double boxmax[3];      /* "boxmax[k]" */
 } gsph_config;
 
-/* Byte offsets of the fields inside one array-of-structures particle record.  r, v, a
- * and atree point at 3 consecutive doubles.  An output offset of -1 skips that field. */
+/* Byte offsets of the fields inside one array-of-structures particle record
+ * (GradhSphParticle<3>, src/Headers/Particle.h:133-368).  r, v, a and atree point at 3
+ * consecutive doubles; flags, level and levelneib at 32-bit integers.  An offset of -1
+ * skips that field.
+ *
+ * Without flags (flags = -1) every particle is active: the calls solve and write every
+ * particle.  With flags, the reference's block-timestep semantics hold: a particle is
+ * active when its flags have the `active` bit (1 << 1, src/Headers/Flags.h:33); the h
+ * solve and the force passes compute active particles only (GradhSphTree.cpp:96-102,
+ * :300-305), the other particles keep the solved state their records hold at import
+ * (rho, invomega, zeta, hfactor, hrangesqd, pressure, sound, a, atree, gpot, dudt, div_v,
+ * gpot_hydro are then read as well), and levelneib is maintained as the reference does
+ * (GradhSphTree.cpp:375-417, :619-640). */
 typedef struct gsph_field_offsets {
   int64_t r, v, m, h, u;                                   /* inputs */
   int64_t rho, invomega, zeta, hfactor, hrangesqd, pressure, sound, div_v, dudt, a, atree,
       gpot, gpot_hydro;                                    /* outputs */
+  int64_t flags, level, levelneib;                         /* block timesteps (int32 fields) */
 } gsph_field_offsets;
+
+#define GSPH_FLAG_ACTIVE 2u    /* the reference's `active` particle flag */
 
 /* Per-particle output fields for gsph_get_field (input order). */
 enum gsph_field {
@@ -133,10 +147,21 @@ int32_t gsph_set_particles_device(gsph_ctx* ctx, int64_t n, const double* x, con
                                   const double* vz, const double* m, const double* u,
                                   const double* h);
 /* Host array-of-structures (the reference's GradhSphParticle array): record stride and
- * field offsets in bytes.  The records are kept on the device so gsph_get_particles_aos
- * can write results back without touching other fields. */
+ * field offsets in bytes.  The input fields (and, with flags, the flags, levels and solved
+ * state above) are read from the records; nothing else of a record is read or kept.
+ * Records in page-locked memory (cudaHostAlloc / cudaHostRegister) are read in place by a
+ * kernel; other records are copied to the device whole and unpacked there. */
 int32_t gsph_set_particles_aos(gsph_ctx* ctx, const void* base, int64_t n, int64_t stride,
                                const gsph_field_offsets* off);
+/* KDTree::UpdateActiveParticleCounters (src/Tree/KDTree.cpp:1217; called by MainLoop before
+ * a repeated pass, src/Hydrodynamics/SphSimulation.cpp:643): re-read the flags and levels
+ * of the records (after CheckTimesteps changed them) into the current tree, without a
+ * rebuild.  The records and offsets are those of gsph_set_particles_aos, with flags. */
+int32_t gsph_update_active_particle_counters(gsph_ctx* ctx, const void* base, int64_t n, int64_t stride,
+                                             const gsph_field_offsets* off);
+/* HydroTree::GetMaximumSmoothingLength (src/Tree/HydroTree.cpp:661): the largest h in the
+ * tree (root cell hmax) after the last tree build or h solve. */
+int32_t gsph_get_maximum_smoothing_length(gsph_ctx* ctx, double* hmax);
 
 /* ---- star particles (Simulation::ImportArrayNbody, src/Common/Simulation.cpp:1325-1430;
  *      the stars a Simulation keeps in Nbody::nbodydata) ---------------------------------- */
@@ -227,7 +252,18 @@ int32_t gsph_batch_stats(const gsph_batch* batch, float* ms, int32_t* launches);
 int32_t gsph_get_field(gsph_ctx* ctx, int32_t field, double* out);
 /* Same into device memory. */
 int32_t gsph_get_field_device(gsph_ctx* ctx, int32_t field, double* out);
-/* Write results into the host records passed to gsph_set_particles_aos. */
+/* Write results into host records laid out as for gsph_set_particles_aos: only the output
+ * fields, and only those computed since the last import (h, u, rho, invomega, zeta,
+ * hfactor, hrangesqd, pressure, sound after an h solve; a, atree, gpot, gpot_hydro, dudt,
+ * div_v after a force pass); every other byte of the records is left as the caller has it.
+ * With flags, only the active particles' fields are written, and levelneib of every
+ * particle becomes max(its current value in the record, the neighbour levels the last
+ * force pass found), as the reference's force loops update it (MainLoop zeroes levelneib of
+ * active particles before the force pass, Sph::ZeroAccelerations, src/Hydrodynamics/Sph.cpp:
+ * 126-140).  The force outputs are stored, not added: MainLoop zeroes them for active
+ * particles before every force pass (SphSimulation.cpp:646), so storing equals the
+ * reference's accumulation.  Page-locked records are written in place by a kernel; other
+ * records through a compact device buffer and a host loop. */
 int32_t gsph_get_particles_aos(gsph_ctx* ctx, void* base, int64_t n, int64_t stride,
                                const gsph_field_offsets* off);
 int32_t gsph_get_stats(gsph_ctx* ctx, gsph_stats* out);

@@ -1448,6 +1448,58 @@ void gsph_oracle_stars(void* handle, double* out) {
   }
 }
 
+// One pass with block-timestep semantics, as a Simulation's main loop drives the neighbour
+// search: a tree build (rebuild = 1) or the tree of the previous call (rebuild = 0, the
+// repeated pass after CheckTimesteps, SphSimulation.cpp:641-752), the h solve of the active
+// particles, the hmax update, the thermal update of every particle, and the force pass of
+// the active particles.  Inactive particles keep the solved state given in `state`
+// (n x 7: rho invomega zeta hfactor hrangesqd pressure sound); levelneib holds the values
+// the records have before the force pass (active ones zeroed by Sph::ZeroAccelerations).
+// Results as gsph_oracle_particles (levelneib in column 19).
+int gsph_oracle_run_active(void* handle, int64_t n, const double* x, const double* y, const double* z,
+                           const double* vx, const double* vy, const double* vz, const double* m,
+                           const double* u, const double* h, const unsigned char* active, const int32_t* level,
+                           const int32_t* levelneib, const double* state, int rebuild, int nthreads) {
+  Oracle* o = static_cast<Oracle*>(handle);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  if (!rebuild && (o->n != n || o->cells.empty())) return -1;
+  o->n = n;
+  o->x[0].assign(x, x + n); o->x[1].assign(y, y + n); o->x[2].assign(z, z + n);
+  o->v[0].assign(vx, vx + n); o->v[1].assign(vy, vy + n); o->v[2].assign(vz, vz + n);
+  o->m.assign(m, m + n); o->u.assign(u, u + n); o->h.assign(h, h + n);
+  o->want_lists = o->want_summary = false;
+  o->active.assign(active, active + n);
+  o->level.assign(level, level + n);
+  o->levelneib.assign(levelneib, levelneib + n);
+  std::vector<double>* st[7] = {&o->rho, &o->invomega, &o->zeta, &o->hfactor, &o->hrangesqd, &o->pressure, &o->sound};
+  for (int q = 0; q < 7; q++) {
+    st[q]->resize(n);
+    for (int64_t i = 0; i < n; i++) (*st[q])[i] = state[i * 7 + q];
+  }
+  if (rebuild) {
+    o->div_v.assign(n, 0); o->dudt.assign(n, 0); o->gpot.assign(n, 0); o->gpot_hydro.assign(n, 0);
+    for (int k = 0; k < 3; k++) { o->a[k].assign(n, 0); o->ag[k].assign(n, 0); }
+    o->h_ghost = o->h;
+    o->build_tree();
+  }
+  o->n_density_pairs = o->n_hydro_pairs = o->n_direct_pairs = o->n_cell_pairs = 0;
+  const int stt = o->density();
+  if (stt != 0) return stt;
+  o->update_hmax(0);
+  o->thermal_all();
+  if (o->p.self_gravity) o->all_forces(); else o->hydro_forces();
+  o->gas_from_stars();
+  return 0;
+}
+
+// Neighbour levels of the last run_active / KDK call (n ints).
+void gsph_oracle_levelneib(void* handle, int32_t* out) {
+  Oracle* o = static_cast<Oracle*>(handle);
+  for (int64_t i = 0; i < o->n; i++) out[i] = o->levelneib.empty() ? 0 : o->levelneib[i];
+}
+
 // KDK run: SetupSimulation then nsteps main-loop steps of the gas with block timesteps.
 // Inputs in input order.  out_state: n x 24 doubles (x y z vx vy vz ax ay az h rho u level
 // nstep nlast levelneib dt tlast dudt div_v gpot invomega pressure sound); out_global: n t

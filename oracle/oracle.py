@@ -91,6 +91,10 @@ def _load():
         lib.gsph_oracle_run_given.argtypes = [vp, i64] + [dp] * 15 + [i32, i32]
         lib.gsph_oracle_nleaf.restype = i32
         lib.gsph_oracle_nleaf.argtypes = [vp]
+        u8p, i32p = ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int32)
+        lib.gsph_oracle_run_active.restype = i32
+        lib.gsph_oracle_run_active.argtypes = [vp, i64] + [dp] * 9 + [u8p, i32p, i32p, dp, i32, i32]
+        lib.gsph_oracle_levelneib.argtypes = [vp, i32p]
         lib.gsph_oracle_kdk.restype = i32
         lib.gsph_oracle_kdk.argtypes = [vp, i64] + [dp] * 10 + [i32, i32, dp, dp, dp]
         lib.gsph_oracle_set_stars.argtypes = [vp, i32] + [dp] * 8
@@ -243,3 +247,50 @@ def kdk(ics: dict, params: dict, kdk_params: dict, nsteps: int, nthreads: int = 
                 "setup_updates": int(info[2]), "step_updates": int(info[3]), "status": int(info[4])}
     finally:
         lib.gsph_oracle_destroy(hnd)
+
+
+STATE_FIELDS = ("rho", "invomega", "zeta", "hfactor", "hrangesqd", "pressure", "sound")
+
+
+class ActivePasses:
+    """Passes with block-timestep semantics on one oracle instance (the tree persists
+    between calls, so a repeated pass can reuse it as the reference's main loop does)."""
+
+    def __init__(self, params: dict, nthreads: int = 0):
+        self.lib = _load()
+        self.prm = make_params(params)
+        self.h = self.lib.gsph_oracle_create(ctypes.byref(self.prm))
+        self.nthreads = nthreads
+
+    def run(self, ics: dict, active, level, levelneib, state: dict, rebuild: bool = True) -> dict:
+        """ics: x y z vx vy vz m u h; state: STATE_FIELDS of every particle (the inactive
+        ones keep them).  Returns the per-particle results, levelneib included."""
+        arrs = [np.ascontiguousarray(ics[k], dtype=np.float64)
+                for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u", "h")]
+        n = len(arrs[0])
+        act = np.ascontiguousarray(active, dtype=np.uint8)
+        lv = np.ascontiguousarray(level, dtype=np.int32)
+        lvn = np.ascontiguousarray(levelneib, dtype=np.int32)
+        st = np.ascontiguousarray(np.stack([np.asarray(state[k], dtype=np.float64) for k in STATE_FIELDS], 1))
+        rc = self.lib.gsph_oracle_run_active(self.h, n, *[_ptr(a) for a in arrs],
+                                             act.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                             lv.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                             lvn.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                             _ptr(st), int(rebuild), int(self.nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle pass failed with status {rc}")
+        out = np.empty((n, len(PARTICLE_FIELDS)))
+        self.lib.gsph_oracle_particles(self.h, _ptr(out))
+        res = {k: out[:, i].copy() for i, k in enumerate(PARTICLE_FIELDS)}
+        lvo = np.empty(n, dtype=np.int32)
+        self.lib.gsph_oracle_levelneib(self.h, lvo.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        res["levelneib"] = lvo
+        return res
+
+    def close(self):
+        if self.h:
+            self.lib.gsph_oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

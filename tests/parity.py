@@ -148,3 +148,19 @@ def check_mixed(got: dict, ref: dict):
             bad.append(f"{k}: {v:.2e} > {tol}")
     assert not bad, "; ".join(bad) + f" | all: {errs}"
     return errs
+
+
+def gradh_record_dtype():
+    """A record with GradhSphParticle<3>'s field order (src/Headers/Particle.h:133-368)."""
+    fields = [("flags", "<u4"), ("ptype", "<i4"), ("iorig", "<i4"), ("sinkid", "<i4"),
+              ("levelneib", "<i4"), ("nstep", "<i4"), ("nlast", "<i4"), ("level", "<i4"),
+              ("r", "<f8", 3), ("v", "<f8", 3), ("a", "<f8", 3), ("atree", "<f8", 3),
+              ("r0", "<f8", 3), ("v0", "<f8", 3), ("a0", "<f8", 3), ("m", "<f8"), ("h", "<f8"),
+              ("h_dust", "<f8"), ("hrangesqd", "<f8"), ("hfactor", "<f8"), ("sound", "<f8"),
+              ("rho", "<f8"), ("pressure", "<f8"), ("u", "<f8"), ("u0", "<f8"), ("dudt0", "<f8"),
+              ("dudt", "<f8"), ("gpot", "<f8"), ("gpot_hydro", "<f8"), ("dt", "<f8"),
+              ("dt_next", "<f8"), ("tlast", "<f8"), ("ionfrac", "<f8"), ("Xion", "<f8"),
+              ("ueq", "<f8"), ("dt_therm", "<f8"), ("vsig_max", "<f8"), ("rad_pres", "<f8", 3),
+              ("ionstate", "<i4"), ("pad", "<i4"), ("div_v", "<f8"), ("alpha", "<f8"),
+              ("dalphadt", "<f8"), ("invomega", "<f8"), ("zeta", "<f8")]
+    return np.dtype(fields)

@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(native_lib):
 
 
 def test_abi_version_and_defaults(native_lib):
-    assert native_lib.gsph_abi_version() == _native.ABI_VERSION == 2
+    assert native_lib.gsph_abi_version() == _native.ABI_VERSION == 3
     cfg = _native.Config()
     native_lib.gsph_config_defaults(ctypes.byref(cfg))
     assert cfg.ndim == 3 and cfg.nleafmax == 8 and cfg.h_fac == 1.2 and cfg.h_converge == 0.01
