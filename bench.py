@@ -611,9 +611,8 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def gradh_records(c):
-    """Host records laid out like GradhSphParticle<3> (src/Headers/Particle.h:133-368)."""
-    import torch
+def gradh_record_dtype():
+    """GradhSphParticle<3>'s field order and sizes (src/Headers/Particle.h:133-368)."""
     fields = [("flags", "<u4"), ("ptype", "<i4"), ("iorig", "<i4"), ("sinkid", "<i4"),
               ("levelneib", "<i4"), ("nstep", "<i4"), ("nlast", "<i4"), ("level", "<i4"),
               ("r", "<f8", 3), ("v", "<f8", 3), ("a", "<f8", 3), ("atree", "<f8", 3),
@@ -625,7 +624,13 @@ def gradh_records(c):
               ("ueq", "<f8"), ("dt_therm", "<f8"), ("vsig_max", "<f8"), ("rad_pres", "<f8", 3),
               ("ionstate", "<i4"), ("pad", "<i4"), ("div_v", "<f8"), ("alpha", "<f8"),
               ("dalphadt", "<f8"), ("invomega", "<f8"), ("zeta", "<f8")]
-    dt = np.dtype(fields)
+    return np.dtype(fields)
+
+
+def gradh_records(c):
+    """Page-locked host records laid out like GradhSphParticle<3>."""
+    import torch
+    dt = gradh_record_dtype()
     n = len(c["x"])
     buf = torch.empty(n * dt.itemsize, dtype=torch.uint8, pin_memory=True)
     rec = buf.numpy().view(dt)

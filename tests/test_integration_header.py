@@ -21,3 +21,33 @@ def test_drop_in_subclass_compiles_against_reference_headers():
     res = subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), f"REF={REF}",
                           "integration-check"], capture_output=True, text=True)
     assert res.returncode == 0, res.stdout + res.stderr
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "Headers")), reason="reference sources absent")
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_record_layouts_match_the_reference_compiler_layout():
+    """The numpy record layouts of the tests and of the bench's e2e path are the
+    reference's GradhSphParticle<3> as its compiler lays it out (offsetof, sizeof)."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    from parity import gradh_record_dtype
+    res = subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), f"REF={REF}",
+                          "record-layout"], capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout + res.stderr
+    out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "record_layout")], capture_output=True, text=True,
+                         check=True).stdout.split("\n")
+    layout = {}
+    size = None
+    for ln in out:
+        f = ln.split()
+        if len(f) == 2 and f[0] == "sizeof":
+            size = int(f[1])
+        elif len(f) == 3:
+            layout[f[0]] = (int(f[1]), int(f[2]))
+    assert size == 448 and len(layout) >= 40
+    for dt in (gradh_record_dtype(), bench.gradh_record_dtype()):
+        assert dt.itemsize == size
+        for name, (off, nbytes) in layout.items():
+            assert dt.fields[name][1] == off, name
+            assert dt.fields[name][0].itemsize == nbytes, name
