@@ -88,7 +88,7 @@ def parse():
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--nleafmax", type=int, default=0,
                     help="evrard_sphere: leaf size to use instead of the autotuner's choice")
-    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed", "mixed_compensated"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true",
                     help="rotating_cloud: skip the one-step precision and list comparison of the forms")
@@ -342,18 +342,20 @@ def precision_step(c, params, h_converge=None, record=True):
     if h_converge is not None:
         prm["h_converge"] = h_converge
     res, lists = {}, {}
-    for form in ("fp64", "mixed"):
-        t = GradhSphTree(prm, precision=form, device=int(os.environ.get("LOCAL_RANK", "0")))
+    for form in ("fp64", "mixed", "mixed_compensated"):
+        kw = {"precision": "mixed", "compensated": 1} if form == "mixed_compensated" else {"precision": form}
+        t = GradhSphTree(prm, device=int(os.environ.get("LOCAL_RANK", "0")), **kw)
         if record:
             t.set_recording(True, 512)
         t.set_particles(c)
         t.step()
         res[form] = t.results()
-        if record:
+        if record and form != "mixed_compensated":
             lists[form] = (t.sph_neighbours_csr(), t.direct_summary(), t.cell_summary())
         res[form]["exact_checks"] = t.stats()["exact_checks"]
         t.close()
     out = {"errors": all_errors(res["mixed"], res["fp64"]),
+           "errors_compensated": all_errors(res["mixed_compensated"], res["fp64"]),
            "exact_checks_mixed": int(res["mixed"]["exact_checks"])}
     if record:
         (oa, ia), (dca, dha), (_, cca, cha) = lists["mixed"]
@@ -370,7 +372,10 @@ def run_kdk_form(c, params, kdk, form, K, warm_seq, stream, device):
     outside, the K steps between CUDA events on the stream.  Returns the context open."""
     import torch
     from gandalf_gb300.sph import GradhSphTree
-    t = GradhSphTree(params, precision=form, device=device)
+    if form == "mixed_compensated":
+        t = GradhSphTree(params, precision="mixed", compensated=1, device=device)
+    else:
+        t = GradhSphTree(params, precision=form, device=device)
     t.set_stream(stream.cuda_stream)
     for _ in range(warm_seq):
         t.set_particles(c)
@@ -452,7 +457,7 @@ def kdk_main(args, rank, world, local):
     W = args.warmup
     c, params, kdk = kdk_workload(n, rank)
     stream = torch.cuda.current_stream()
-    forms = ["fp64", "mixed"] if args.precision == "auto" else [args.precision]
+    forms = ["fp64", "mixed", "mixed_compensated"] if args.precision == "auto" else [args.precision]
     warm_seq = max(1, -(-W // K))           # whole K-step sequences covering >= W warm-up steps
     out, finals = {}, {}
     ctx_head = None
@@ -518,6 +523,10 @@ def kdk_main(args, rank, world, local):
         pos = np.sqrt(np.mean(sum((a["pos_" + k] - b["pos_" + k]) ** 2 for k in ("x", "y", "z"))))
         errs["position_rms_abs"] = float(pos)
         line["mixed_vs_fp64_after_all_steps"] = errs
+    if "fp64" in out and "mixed_compensated" in out:
+        a, b = finals["mixed_compensated"], finals["fp64"]
+        line["mixed_compensated_vs_fp64_after_all_steps"] = all_errors(a, b)
+        line["compensated_cost"] = out["mixed_compensated"]["ms_total"] / out["mixed"]["ms_total"] - 1.0
     if not args.no_e2e and ctx_head is not None:
         e = kdk_e2e(ctx_head, c, kdk, K)
         line["e2e"] = {"value": world * e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d_bytes_per_step"],

@@ -45,7 +45,8 @@ class Config(ctypes.Structure):
                 ("alpha_visc", ctypes.c_double), ("beta_visc", ctypes.c_double),
                 ("gamma_eos", ctypes.c_double), ("temp0", ctypes.c_double),
                 ("mu_bar", ctypes.c_double), ("thetamaxsqd", ctypes.c_double),
-                ("boxmin", ctypes.c_double * 3), ("boxmax", ctypes.c_double * 3)]
+                ("boxmin", ctypes.c_double * 3), ("boxmax", ctypes.c_double * 3),
+                ("compensated", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class FieldOffsets(ctypes.Structure):

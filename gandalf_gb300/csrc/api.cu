@@ -367,6 +367,7 @@ SphParams make_params(const gsph_ctx* c) {
     p.boxhalf[k] = 0.5 * p.boxsize[k];
   }
   p.eos = cfg.eos; p.periodic = cfg.periodic; p.multipole = cfg.multipole; p.self_gravity = cfg.self_gravity;
+  p.compensated = cfg.precision == GSPH_PRECISION_MIXED && cfg.compensated ? 1 : 0;
   return p;
 }
 
@@ -430,6 +431,7 @@ int check_config(const gsph_config* cfg, std::string& why) {
   if (cfg->multipole != GSPH_MONOPOLE && cfg->multipole != GSPH_QUADRUPOLE) { why = "unknown multipole"; return GSPH_ERR_UNSUPPORTED; }
   if (cfg->precision != GSPH_PRECISION_FP64 && cfg->precision != GSPH_PRECISION_MIXED) { why = "unknown precision"; return GSPH_ERR_INVALID; }
   if (cfg->self_gravity && cfg->periodic) { why = "periodic self-gravity needs Ewald sums (not implemented)"; return GSPH_ERR_UNSUPPORTED; }
+  if ((cfg->compensated != 0 && cfg->compensated != 1) || cfg->reserved != 0) { why = "compensated must be 0 or 1"; return GSPH_ERR_INVALID; }
   if (!cfg->hydro_forces) { why = "hydro_forces = 0 is not implemented"; return GSPH_ERR_UNSUPPORTED; }
   if (!(cfg->h_fac > 0.0) || !(cfg->h_converge > 0.0) || !(cfg->gamma_eos > 1.0) || !(cfg->thetamaxsqd > 0.0)) {
     why = "h_fac, h_converge, thetamaxsqd must be > 0 and gamma_eos > 1"; return GSPH_ERR_INVALID;

@@ -21,8 +21,18 @@ struct SphParams {
   int periodic;     // 0 open, 1 periodic in x, y and z
   int multipole;    // 0 monopole, 1 quadrupole
   int self_gravity;
+  int compensated;  // mixed form: compensated float sums, lane partials combined in fp64
   StarSet stars;    // n = 0: no stars
 };
+
+// Kahan-compensated float accumulation: s + c carries the sum to about twice float precision
+// (the lost low part of each addition is kept in c and fed back into the next one).
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
 
 // Particles in leaf order (slot = position in the leaf-ordered arrays).
 struct Particles {

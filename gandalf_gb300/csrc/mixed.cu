@@ -421,15 +421,23 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
       const double invhsqd = invh * invh;
       const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
       float srho = 0.0f, som = 0.0f, sze = 0.0f;
+      float crho = 0.0f, com = 0.0f, cze = 0.0f;   // compensation terms (compensated sums)
+      const bool comp = prm.compensated != 0;
       auto add = [&](float d2, float mj) {
         const float ssqd = d2 * invhsqd_f;
         if (ssqd < 4.0f) {
           const float s = fsqrt_pos(ssqd);
           float w0, wom, wze;   // s < 2 here
           m4f_w0_omega_zeta(s, w0, wom, wze);
-          srho = fmaf(mj, w0, srho);
-          som = fmaf(mj * invh_f, wom, som);
-          sze = fmaf(mj, wze, sze);
+          if (comp) {
+            kahan_add(srho, crho, mj * w0);
+            kahan_add(som, com, (mj * invh_f) * wom);
+            kahan_add(sze, cze, mj * wze);
+          } else {
+            srho = fmaf(mj, w0, srho);
+            som = fmaf(mj * invh_f, wom, som);
+            sze = fmaf(mj, wze, sze);
+          }
           pairs++;
         }
       };
@@ -456,22 +464,38 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         walk_all([&]() { consume(L.na); });
         consume(L.na);
       }
+      double drho, dom, dze;
+      if (comp) {   // the lanes' compensated partials combined in fp64
+        drho = (double) srho - (double) crho;
+        dom = (double) som - (double) com;
+        dze = (double) sze - (double) cze;
 #pragma unroll
-      for (int o = 1; o < LPG; o <<= 1) {
-        srho += __shfl_xor_sync(kFull, srho, o);
-        som += __shfl_xor_sync(kFull, som, o);
-        sze += __shfl_xor_sync(kFull, sze, o);
+        for (int o = 1; o < LPG; o <<= 1) {
+          drho += __shfl_xor_sync(kFull, drho, o);
+          dom += __shfl_xor_sync(kFull, dom, o);
+          dze += __shfl_xor_sync(kFull, dze, o);
+        }
+      } else {
+#pragma unroll
+        for (int o = 1; o < LPG; o <<= 1) {
+          srho += __shfl_xor_sync(kFull, srho, o);
+          som += __shfl_xor_sync(kFull, som, o);
+          sze += __shfl_xor_sync(kFull, sze, o);
+        }
+        drho = srho; dom = som; dze = sze;
       }
-      float drho = srho, dom = som, dze = sze;
       if (WARPS > 1) {
-        if (sl == 0) { sm->part[wib][g][0] = drho; sm->part[wib][g][1] = dom; sm->part[wib][g][2] = dze; }
+        if (sl == 0) {
+          sm->part[wib][g][0] = (float) drho; sm->part[wib][g][1] = (float) dom; sm->part[wib][g][2] = (float) dze;
+        }
         __syncthreads();
-        drho = dom = dze = 0.0f;
-        for (int w = 0; w < WARPS; w++) { drho += sm->part[w][g][0]; dom += sm->part[w][g][1]; dze += sm->part[w][g][2]; }
+        float fr = 0.0f, fo = 0.0f, fz = 0.0f;
+        for (int w = 0; w < WARPS; w++) { fr += sm->part[w][g][0]; fo += sm->part[w][g][1]; fz += sm->part[w][g][2]; }
+        drho = fr; dom = fo; dze = fz;
         __syncthreads();
       }
       if (!done)
-        h_update((double) drho, (double) dom, (double) dze, inv_m, inv_hfac, invhsqd, hmax_list, prm, iteration, hi,
+        h_update(drho, dom, dze, inv_m, inv_hfac, invhsqd, hmax_list, prm, iteration, hi,
                  invh, h_lower, h_upper, hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
     }
     double mw = mloc;
@@ -745,7 +769,19 @@ k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams
 // ==========================================================================================
 struct AccF {
   float ah[3], ag[3], gpot, dudt, divv;
+  float cg[4];   // compensation of ag[0..2] and gpot (compensated sums; zero otherwise)
 };
+
+// One gravity contribution: plain float sums, or compensated ones (prm.compensated).
+#define GSPH_ADD_G(A, comp, vx, vy, vz, vp)                                                      \
+  do {                                                                                           \
+    if (comp) {                                                                                  \
+      kahan_add((A).ag[0], (A).cg[0], vx); kahan_add((A).ag[1], (A).cg[1], vy);                  \
+      kahan_add((A).ag[2], (A).cg[2], vz); kahan_add((A).gpot, (A).cg[3], vp);                   \
+    } else {                                                                                     \
+      (A).ag[0] += vx; (A).ag[1] += vy; (A).ag[2] += vz; (A).gpot += vp;                         \
+    }                                                                                            \
+  } while (0)
 
 struct TargetF {
   float4 ph, pl, vel, hyd, aux;   // see MixedParticles
@@ -827,17 +863,15 @@ __device__ __forceinline__ void hydro_grav_pair_f(const SphParams& prm, const Mi
   const float paux = pair_pressure_f(prm, T, wi, wj, hj.y, hj.z, hj.w, mj, dvdr, A.dudt);
   A.ah[0] += mj * ux * paux; A.ah[1] += mj * uy * paux; A.ah[2] += mj * uz * paux;
   const float pg = 0.5f * (T.hyd.x * T.hyd.x * wgi + T.aux.y * wi + hj.x * hj.x * wgj + xj.y * wj);
-  A.ag[0] += mj * ux * pg; A.ag[1] += mj * uy * pg; A.ag[2] += mj * uz * pg;
-  A.gpot += 0.5f * mj * (T.hyd.x * wpi + hj.x * wpj);
+  GSPH_ADD_G(A, prm.compensated, mj * ux * pg, mj * uy * pg, mj * uz * pg, 0.5f * mj * (T.hyd.x * wpi + hj.x * wpj));
   A.divv -= mj * dvdr * wi;
 }
 
-__device__ __forceinline__ void direct_term_f(float dx, float dy, float dz, float mj, AccF& A) {
+__device__ __forceinline__ void direct_term_f(float dx, float dy, float dz, float mj, AccF& A, bool comp) {
   const float r2 = dx * dx + dy * dy + dz * dz + 1.0e-20f;
   const float inv = rsqrtf(r2);
   const float inv3 = inv * inv * inv * mj;
-  A.ag[0] += dx * inv3; A.ag[1] += dy * inv3; A.ag[2] += dz * inv3;
-  A.gpot += mj * inv;
+  GSPH_ADD_G(A, comp, dx * inv3, dy * inv3, dz * inv3, mj * inv);
 }
 
 __device__ __forceinline__ void cell_term_f(const MixedCells& mc, int cc, const TargetF& T, bool quad, AccF& A) {
@@ -932,8 +966,16 @@ __device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Pa
   // the lanes' partial sums added in float (each holds a few hundred float terms already),
   // the per-particle arithmetic after them in float too; results stored as fp64
   float ah[3], ag[3], gp, du, dv;
-  for (int k = 0; k < 3; k++) { ah[k] = gsum_f<LPG>(A.ah[k]); ag[k] = gsum_f<LPG>(A.ag[k]); }
-  gp = gsum_f<LPG>(A.gpot);
+  double agd[3], gpd;
+  for (int k = 0; k < 3; k++) ah[k] = gsum_f<LPG>(A.ah[k]);
+  if (prm.compensated) {   // the lanes' compensated partials combined in fp64
+    for (int k = 0; k < 3; k++) agd[k] = gsum_d<LPG>((double) A.ag[k] - (double) A.cg[k]);
+    gpd = gsum_d<LPG>((double) A.gpot - (double) A.cg[3]);
+  } else {
+    for (int k = 0; k < 3; k++) { ag[k] = gsum_f<LPG>(A.ag[k]); agd[k] = ag[k]; }
+    gp = gsum_f<LPG>(A.gpot);
+    gpd = gp;
+  }
   du = gsum_f<LPG>(A.dudt);
   dv = gsum_f<LPG>(A.divv);
   if (cnt.record) {
@@ -948,11 +990,11 @@ __device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Pa
   const float P = (float) (prm.gamma_eos - 1.0) * rho * (float) p.u[slot];
   p.div_v[slot] = (double) divv;
   p.dudt[slot] = (double) (du - P * divv * invrho * (float) p.invomega[slot]);
-  p.ax[slot] = (double) ah[0] + (double) ag[0];
-  p.ay[slot] = (double) ah[1] + (double) ag[1];
-  p.az[slot] = (double) ah[2] + (double) ag[2];
-  p.agx[slot] = ag[0]; p.agy[slot] = ag[1]; p.agz[slot] = ag[2];
-  p.gpot[slot] = grav ? gpot0 + (double) gp : 0.0;
+  p.ax[slot] = (double) ah[0] + agd[0];
+  p.ay[slot] = (double) ah[1] + agd[1];
+  p.az[slot] = (double) ah[2] + agd[2];
+  p.agx[slot] = agd[0]; p.agy[slot] = agd[1]; p.agz[slot] = agd[2];
+  p.gpot[slot] = grav ? gpot0 + gpd : 0.0;
 }
 
 constexpr int kForceWarps = 4;    // warps per block of the warp-per-leaf force kernels
@@ -1025,8 +1067,13 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
       for (int k = 0; k < 4; k++)
         for (int o = 16; o > 0; o >>= 1) acc[u][k] = __fadd_rn(acc[u][k], __shfl_xor_sync(kFull, acc[u][k], o));
       if (lane == (u0 + u) * LPG) {
-        A.ag[0] = __fadd_rn(A.ag[0], acc[u][0]); A.ag[1] = __fadd_rn(A.ag[1], acc[u][1]);
-        A.ag[2] = __fadd_rn(A.ag[2], acc[u][2]); A.gpot = __fadd_rn(A.gpot, acc[u][3]);
+        if (prm.compensated) {
+          kahan_add(A.ag[0], A.cg[0], acc[u][0]); kahan_add(A.ag[1], A.cg[1], acc[u][1]);
+          kahan_add(A.ag[2], A.cg[2], acc[u][2]); kahan_add(A.gpot, A.cg[3], acc[u][3]);
+        } else {
+          A.ag[0] = __fadd_rn(A.ag[0], acc[u][0]); A.ag[1] = __fadd_rn(A.ag[1], acc[u][1]);
+          A.ag[2] = __fadd_rn(A.ag[2], acc[u][2]); A.gpot = __fadd_rn(A.gpot, acc[u][3]);
+        }
       }
     }
   };
@@ -1133,7 +1180,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
             if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
           }
         } else {
-          direct_term_f(dx, dy, dz, pjh.w, A);
+          direct_term_f(dx, dy, dz, pjh.w, A, prm.compensated != 0);
           ndir++;
           if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
         }
@@ -1217,8 +1264,9 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   }
   // sliced: reduce each particle inside the warp, then across slices in slice order
   double v[9];
-  for (int k = 0; k < 3; k++) { v[k] = (double) A.ah[k]; v[3 + k] = (double) A.ag[k]; }
-  v[6] = A.gpot; v[7] = A.dudt; v[8] = A.divv;
+  // (the compensation terms are zero unless the sums are compensated)
+  for (int k = 0; k < 3; k++) { v[k] = (double) A.ah[k]; v[3 + k] = (double) A.ag[k] - (double) A.cg[k]; }
+  v[6] = (double) A.gpot - (double) A.cg[3]; v[7] = A.dudt; v[8] = A.divv;
   unsigned long long dc = ndir, dh = dhash;
   for (int o = 1; o < LPG; o <<= 1) {
     for (int k = 0; k < 9; k++) v[k] += __shfl_xor_sync(kFull, v[k], o);

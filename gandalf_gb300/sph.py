@@ -45,7 +45,8 @@ def make_config(params: dict | None = None, **kw) -> _native.Config:
         p["precision"] = PRECISION[p["precision"]]
     if "Nleafmax" in p:
         p["nleafmax"] = p["Nleafmax"]
-    for k in ("ndim", "nleafmax", "hydro_forces", "self_gravity", "eos", "multipole", "periodic", "precision"):
+    for k in ("ndim", "nleafmax", "hydro_forces", "self_gravity", "eos", "multipole", "periodic", "precision",
+              "compensated"):
         if k in p:
             setattr(cfg, k, int(p[k]))
     for k in ("h_fac", "h_converge", "alpha_visc", "beta_visc", "gamma_eos", "temp0", "mu_bar",

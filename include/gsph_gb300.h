@@ -70,6 +70,9 @@ typedef struct gsph_config {
   double thetamaxsqd;    /* "thetamaxsqd" (geometric opening angle squared) */
   double boxmin[3];      /* "boxmin[k]" (periodic box) */
   double boxmax[3];      /* "boxmax[k]" */
+  int32_t compensated;   /* mixed form: 1 = compensated (Kahan) float sums for the density and
+                            gravity accumulations, the lanes' partials combined in FP64 */
+  int32_t reserved;      /* must be 0 */
 } gsph_config;
 
 /* Byte offsets of the fields inside one array-of-structures particle record
