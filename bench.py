@@ -217,9 +217,11 @@ def evrard_main(args, rank, world, local):
     steps = args.steps
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     with ClockSampler(local) as clk:
-        tune = ({"nleafmax": args.nleafmax, "ms_per_step": None} if args.nleafmax > 0 else
+        tune = ({"nleafmax": args.nleafmax} if args.nleafmax > 0 else
                 tune_leaf_size(c, params, precision=form, steps=1, device=local))
         t = GradhSphTree(params, precision=form, nleafmax=tune["nleafmax"], device=local)
+        if args.nleafmax <= 0:
+            t.set_tuning(**{k: tune[k] for k in ("near_depth", "cell_depth", "gather_depth")})
         stream = torch.cuda.current_stream()
         t.set_stream(stream.cuda_stream)
         t.set_particles(c)
@@ -250,7 +252,7 @@ def evrard_main(args, rank, world, local):
             "data": "synthetic",
             "config": {"workload": "evrard_sphere", "n": n, "nstar": 64, "star_mass": 1e-3, "star_h": 0.01,
                        "thetamaxsqd": 0.25, "multipole": "quadrupole", "precision": form,
-                       ("nleafmax" if args.nleafmax > 0 else "nleafmax_autotuned"): tune, "cuda_graph": True, "parallelism": f"replicas{world}",
+                       ("nleafmax" if args.nleafmax > 0 else "autotuned"): tune, "cuda_graph": True, "parallelism": f"replicas{world}",
                        "l2": "flushed between timed steps (256 MiB write)"},
             "gpu_launches": st["launches"],
             "counts": {k: st[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs", "cell_pairs")},

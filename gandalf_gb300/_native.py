@@ -58,6 +58,11 @@ class FieldOffsets(ctypes.Structure):
 GSPH_FLAG_ACTIVE = 2   # the reference's `active` particle flag bit
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("nleafmax", ctypes.c_int32), ("near_depth", ctypes.c_int32), ("cell_depth", ctypes.c_int32),
+                ("gather_depth", ctypes.c_int32)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("ncell", ctypes.c_int64), ("nleaf", ctypes.c_int64),
                 ("ltot", ctypes.c_int64), ("density_pairs", ctypes.c_int64),
@@ -105,6 +110,10 @@ SIGNATURES = {
     "gsph_set_stream": (_I32, [_P, _P]),
     "gsph_fma_peak_gflops": (ctypes.c_double, [_I32, _I32]),
     "gsph_kdtree_order_noalloc": (_I32, [_P, _P, _P, _P, _I32, _I32, _P, _P]),
+    "gsph_get_tuning": (_I32, [_P, ctypes.POINTER(Tuning)]),
+    "gsph_set_tuning": (_I32, [_P, ctypes.POINTER(Tuning)]),
+    "gsph_autotune": (_I32, [_P, _I32, ctypes.POINTER(Tuning), ctypes.POINTER(Tuning), _D, _I32,
+                             ctypes.POINTER(ctypes.c_int32)]),
     "gsph_get_tree": (_I32, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                              ctypes.POINTER(ctypes.c_int32), _D]),
     "gsph_set_stars": (_I32, [_P, _I64] + [_D] * 8),

@@ -131,6 +131,8 @@ struct gsph_ctx {
   bool graph_valid = false;
   bool capturing = false;
   unsigned graph_launches = 0;
+  // tuned list depths of the mixed kernels (0: compiled maxima)
+  int near_depth = 0, cell_depth = 0, gather_depth = 0;
   // timing
   cudaEvent_t ev[5] = {};
   gsph_stats last{};
@@ -368,6 +370,7 @@ SphParams make_params(const gsph_ctx* c) {
   }
   p.eos = cfg.eos; p.periodic = cfg.periodic; p.multipole = cfg.multipole; p.self_gravity = cfg.self_gravity;
   p.compensated = cfg.precision == GSPH_PRECISION_MIXED && cfg.compensated ? 1 : 0;
+  p.near_depth = c->near_depth; p.cell_depth = c->cell_depth; p.gather_depth = c->gather_depth;
   return p;
 }
 
@@ -1392,6 +1395,146 @@ int32_t gsph_get_tree(gsph_ctx* c, int32_t* cell_n, int32_t* cell_first, int32_t
       r[29] = cf[q]; r[30] = 0;
     }
   }
+  return GSPH_OK;
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// Autotuning (gsph_get_tuning / gsph_set_tuning / gsph_autotune)
+// ======================================================================================
+extern "C" {
+
+int32_t gsph_get_tuning(gsph_ctx* c, gsph_tuning* out) {
+  if (!c || !out) return GSPH_ERR_INVALID;
+  out->nleafmax = c->cfg.nleafmax;
+  out->near_depth = c->near_depth;
+  out->cell_depth = c->cell_depth;
+  out->gather_depth = c->gather_depth;
+  return GSPH_OK;
+}
+
+int32_t gsph_set_tuning(gsph_ctx* c, const gsph_tuning* t) {
+  if (!c || !t) return GSPH_ERR_INVALID;
+  if (t->nleafmax < 1 || t->nleafmax > 32) return fail(c, GSPH_ERR_INVALID, "nleafmax must be 1..32");
+  if ((t->near_depth && (t->near_depth < 64 || t->near_depth > 256)) ||
+      (t->cell_depth && (t->cell_depth < 64 || t->cell_depth > 512)) ||
+      (t->gather_depth && (t->gather_depth < 64 || t->gather_depth > 256)))
+    return fail(c, GSPH_ERR_INVALID, "depth outside its range");
+  cudaSetDevice(c->device);
+  if (t->nleafmax != c->cfg.nleafmax) {
+    if (c->bactive) return fail(c, GSPH_ERR_STATE, "set the leaf size before importing records with flags");
+    GSPH_CUDA(cudaStreamSynchronize(c->stream));
+    const int n = c->n;
+    double* save = nullptr;
+    if (c->have_particles) {   // a new shape may reallocate the particle arrays: keep the inputs
+      GSPH_CUDA(cudaMalloc(&save, sizeof(double) * 9 * (size_t) n));
+      for (int q = 0; q < 9; q++)
+        GSPH_CUDA(cudaMemcpyAsync(save + (size_t) q * n, c->in[q], sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+    }
+    const int old = c->cfg.nleafmax;
+    c->cfg.nleafmax = t->nleafmax;
+    int rc = GSPH_OK;
+    if (c->have_particles) {
+      c->have_particles = false;   // recompute the tree shape for the new leaf size
+      rc = ensure_capacity(c, n);
+      if (rc == GSPH_OK)
+        for (int q = 0; q < 9; q++) {
+          const cudaError_t e = cudaMemcpyAsync(c->in[q], save + (size_t) q * n, sizeof(double) * n,
+                                                cudaMemcpyDeviceToDevice, c->stream);
+          if (e != cudaSuccess) { rc = cuda_fail(c, e, "restore particles"); break; }
+        }
+      cudaStreamSynchronize(c->stream);
+      cudaFree(save);
+      if (rc != GSPH_OK) { c->cfg.nleafmax = old; return rc; }
+      c->have_particles = true;
+    }
+    drop_graph(c);
+    drop_kdk_graph(c);
+    c->kdk = false;
+    c->have_tree = c->have_props = c->have_forces = false;
+  }
+  if (t->near_depth != c->near_depth || t->cell_depth != c->cell_depth || t->gather_depth != c->gather_depth) {
+    drop_graph(c);       // the captured launches hold the parameters by value
+    drop_kdk_graph(c);
+  }
+  c->near_depth = t->near_depth;
+  c->cell_depth = t->cell_depth;
+  c->gather_depth = t->gather_depth;
+  return GSPH_OK;
+}
+
+int32_t gsph_autotune(gsph_ctx* c, int32_t steps, gsph_tuning* best, gsph_tuning* tried, double* ms,
+                      int32_t max_tried, int32_t* ntried) {
+  if (!c || !best) return GSPH_ERR_INVALID;
+  if (!c->have_particles) return fail(c, GSPH_ERR_STATE, "no particles imported");
+  if (c->bactive) return fail(c, GSPH_ERR_STATE, "tune on structure-of-arrays imports");
+  if (steps < 1 || steps > 1000) return fail(c, GSPH_ERR_INVALID, "steps out of range");
+  cudaSetDevice(c->device);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  GSPH_CUDA(cudaEventCreate(&e0));
+  GSPH_CUDA(cudaEventCreate(&e1));
+  int count = 0;
+  auto time_one = [&](const gsph_tuning& t, double& out_ms) -> int {
+    int rc = gsph_set_tuning(c, &t);
+    if (rc) return rc;
+    rc = gsph_step_graph(c);   // capture and a first run, untimed
+    if (rc) return rc;
+    if (cudaEventRecord(e0, c->stream) != cudaSuccess) return cuda_fail(c, cudaGetLastError(), "event");
+    for (int q = 0; q < steps && !rc; q++) rc = gsph_step_graph(c);
+    if (rc) return rc;
+    if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+      return cuda_fail(c, cudaGetLastError(), "event");
+    float f = 0.0f;
+    cudaEventElapsedTime(&f, e0, e1);
+    out_ms = f / steps;
+    if (tried && ms && count < max_tried) { tried[count] = t; ms[count] = out_ms; }
+    count++;
+    return GSPH_OK;
+  };
+  gsph_tuning cur{};
+  gsph_get_tuning(c, &cur);
+  gsph_tuning bestt = cur;
+  double best_ms = 1e300;
+  int rc = GSPH_OK;
+  // leaf size with the current depths, then each depth in turn
+  const int leaves[] = {4, 6, 8, 12, 16};
+  for (int nl : leaves) {
+    gsph_tuning t = bestt;
+    t.nleafmax = nl;
+    double m = 0.0;
+    if (time_one(t, m) == GSPH_OK && m < best_ms) { best_ms = m; bestt = t; }
+  }
+  const bool mix = c->cfg.precision == GSPH_PRECISION_MIXED;
+  if (mix && best_ms < 1e300) {
+    const int nears[] = {64, 128, 256}, cells[] = {128, 256, 512}, gathers[] = {64, 128, 256};
+    for (int v : nears) {
+      gsph_tuning t = bestt;
+      t.near_depth = v;
+      double m = 0.0;
+      if (time_one(t, m) == GSPH_OK && m < best_ms) { best_ms = m; bestt = t; }
+    }
+    for (int v : cells) {
+      gsph_tuning t = bestt;
+      t.cell_depth = v;
+      double m = 0.0;
+      if (time_one(t, m) == GSPH_OK && m < best_ms) { best_ms = m; bestt = t; }
+    }
+    for (int v : gathers) {
+      gsph_tuning t = bestt;
+      t.gather_depth = v;
+      double m = 0.0;
+      if (time_one(t, m) == GSPH_OK && m < best_ms) { best_ms = m; bestt = t; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ntried) *ntried = count;
+  if (best_ms >= 1e300) return fail(c, GSPH_ERR_STATE, "no candidate ran");
+  rc = gsph_set_tuning(c, &bestt);
+  if (rc) return rc;
+  *best = bestt;
   return GSPH_OK;
 }
 

@@ -22,8 +22,18 @@ struct SphParams {
   int multipole;    // 0 monopole, 1 quadrupole
   int self_gravity;
   int compensated;  // mixed form: compensated float sums, lane partials combined in fp64
+  // Tuned list depths of the mixed warp-per-leaf kernels (0: the compiled maximum): the
+  // near-list depth a force warp keeps before its leaf goes to the 8-warp kernel, the
+  // multipole-list depth consumed per flush, and the density gather-list depth before a
+  // leaf goes to the per-particle kernel.
+  int near_depth, cell_depth, gather_depth;
   StarSet stars;    // n = 0: no stars
 };
+
+// A tuned depth clamped to [lo, max] (0 selects max).
+__host__ __device__ __forceinline__ int tuned_depth(int v, int lo, int max) {
+  return v <= 0 ? max : (v < lo ? lo : (v > max ? max : v));
+}
 
 // Kahan-compensated float accumulation: s + c carries the sum to about twice float precision
 // (the lost low part of each addition is kept in c and fed back into the next one).

@@ -755,8 +755,9 @@ k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams
   const int leaf = blockIdx.x;
   if (leaf >= t.nleaf) return;
   const int kcap = compact_stride<LPG>();
-  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack, s_list, kDensListNormal, s_compact,
-                                       kcap, handover, nullptr);
+  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack, s_list,
+                                       tuned_depth(prm.gather_depth, 64, kDensListNormal), s_compact, kcap, handover,
+                                       nullptr);
   if (!ok && (threadIdx.x & 31) == 0) {
     const int k = atomicAdd(heavy.count, 1);
     heavy.leaves[k] = leaf;
@@ -1323,7 +1324,8 @@ k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphPar
   const int leaf = blockIdx.x * kForceWarps + wib;
   if (leaf >= t.nleaf) return;
   const bool ok = all_forces_leaf<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, 0, s_stack[wib], s_a[wib], s_b[wib],
-                                          s_c[wib], kFListA, kFListB, kFListC, true);
+                                          s_c[wib], tuned_depth(prm.near_depth, 64, kFListA), kFListB,
+                                          tuned_depth(prm.cell_depth, 64, kFListC), true);
   if (!ok && (threadIdx.x & 31) == 0) {
     const int k = atomicAdd(heavy.count, 1);
     heavy.leaves[k] = leaf;
@@ -1507,7 +1509,8 @@ __global__ void __launch_bounds__(kDensWarps * 32, 3) k_batch_density(BatchQueue
     const SimDesc& d = q.sims[s];
     const int leaf = item - q.leaf_start[s];
     const bool ok = density_cell<LPG, 1>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, leaf, s_stack + wib * kDensStack,
-                                         s_list + wib * kDensListNormal, kDensListNormal,
+                                         s_list + wib * kDensListNormal,
+                                         tuned_depth(d.prm.gather_depth, 64, kDensListNormal),
                                          s_compact + wib * kCompactPerWarp, kcap, true, nullptr);
     if (!ok && (threadIdx.x & 31) == 0) {
       const int k = atomicAdd(d.heavy.count, 1);
@@ -1560,7 +1563,8 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_batch_forces(BatchQueue q)
     const SimDesc& d = q.sims[s];
     const int leaf = item - q.leaf_start[s];
     const bool ok = all_forces_leaf<LPG, 1>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, leaf, 0, s_stack[wib], s_a[wib],
-                                            s_b[wib], s_c[wib], kFListA, kFListB, kFListC, true);
+                                            s_b[wib], s_c[wib], tuned_depth(d.prm.near_depth, 64, kFListA), kFListB,
+                                            tuned_depth(d.prm.cell_depth, 64, kFListC), true);
     if (!ok && (threadIdx.x & 31) == 0) {
       const int k = atomicAdd(d.heavy.count, 1);
       d.heavy.leaves[k] = leaf;

@@ -237,6 +237,31 @@ class GradhSphTree:
         self._check(self._lib.gsph_get_stats(self._ctx, ctypes.byref(s)), "get_stats")
         return {k: getattr(s, k) for k, _ in _native.Stats._fields_}
 
+    # ---- autotuning (gsph_autotune) -------------------------------------------------------
+    def tuning(self) -> dict:
+        t = _native.Tuning()
+        self._check(self._lib.gsph_get_tuning(self._ctx, ctypes.byref(t)), "get_tuning")
+        return {k: getattr(t, k) for k, _ in _native.Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        t = _native.Tuning(**{**self.tuning(), **kw})
+        self._check(self._lib.gsph_set_tuning(self._ctx, ctypes.byref(t)), "set_tuning")
+
+    def autotune(self, steps: int = 2) -> dict:
+        """Leaf size, warps per cell (near-list depth before the 8-warp kernel) and list tile
+        depths chosen by timing the imported particles' step; the best is applied."""
+        best = _native.Tuning()
+        cap = 32
+        tried = (_native.Tuning * cap)()
+        ms = (ctypes.c_double * cap)()
+        nt = ctypes.c_int32()
+        self._check(self._lib.gsph_autotune(self._ctx, int(steps), ctypes.byref(best), tried, ms, cap,
+                                            ctypes.byref(nt)), "autotune")
+        fields = [k for k, _ in _native.Tuning._fields_]
+        return {**{k: getattr(best, k) for k in fields},
+                "tried": [dict({k: getattr(tried[i], k) for k in fields}, ms_per_step=ms[i])
+                          for i in range(min(nt.value, cap))]}
+
     def set_stream(self, stream_ptr: int | None):
         """Run on the given cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
         self._check(self._lib.gsph_set_stream(self._ctx, ctypes.c_void_p(stream_ptr or 0)), "set_stream")

@@ -287,6 +287,34 @@ int32_t gsph_get_cell_summary(gsph_ctx* ctx, int32_t* leaf_cells, int64_t* count
 int32_t gsph_get_tree(gsph_ctx* ctx, int32_t* cell_n, int32_t* cell_first, int32_t* order,
                       double* cell_data /* ncell x 31, layout of oracle cells */);
 
+/* ---- autotuning ---------------------------------------------------------------------------
+ * No counterpart in the reference (whose Nleafmax is a fixed run parameter).  Three knobs
+ * set how the pair kernels map a leaf cell onto the GPU:
+ *   nleafmax      leaf size: particles per leaf cell, hence per warp of the pair kernels,
+ *                 the tree depth and the length of every interaction list;
+ *   near_depth    the near-list depth (leaf cells, 64..256) a force warp holds in shared
+ *                 memory; a leaf whose near list is deeper goes to the 8-warp kernel, so
+ *                 this sets how many warps work on one cell;
+ *   cell_depth    the multipole-list tile (64..512 cells) a force warp consumes per flush;
+ *   gather_depth  the density gather-list depth (64..256 leaf cells) a warp holds; deeper
+ *                 leaves go to the per-particle kernel (one warp per particle).
+ * Depths apply to the mixed form; 0 selects the compiled maximum.  Changing nleafmax keeps
+ * the imported particles (structure-of-arrays imports only) and rebuilds nothing until the
+ * next step; every value is a valid reference configuration, results differ between leaf
+ * sizes only as the reference's own results do. */
+typedef struct gsph_tuning {
+  int32_t nleafmax, near_depth, cell_depth, gather_depth;
+} gsph_tuning;
+int32_t gsph_get_tuning(gsph_ctx* ctx, gsph_tuning* out);
+int32_t gsph_set_tuning(gsph_ctx* ctx, const gsph_tuning* tuning);
+/* Times `steps` graph-replayed steps of the imported particles for candidate tunings — a
+ * coordinate search: leaf sizes 4, 6, 8, 12, 16, then each depth over its range — and keeps
+ * the fastest.  tried / ms (capacity max_tried, may be NULL) receive every candidate and
+ * its time per step; *ntried their count.  The context's graphs and any KDK integration are
+ * reset; results of the last step are those of the last candidate. */
+int32_t gsph_autotune(gsph_ctx* ctx, int32_t steps, gsph_tuning* best, gsph_tuning* tried, double* ms,
+                      int32_t max_tried, int32_t* ntried);
+
 /* ---- allocation-free KD-tree ordering --------------------------------------------------- */
 /* No counterpart in the reference: an extra entry point for callers that cannot allocate
  * device memory — e.g. a host code whose device memory is all owned by its own pool
