@@ -395,13 +395,18 @@ def run_kdk_form(c, params, kdk, form, K, warm_seq, stream, device):
     ms = ev0.elapsed_time(ev1)
     st = t.kdk_status()
     s2 = t.stats()
+    tm = t.kdk_timing()
     upd = st["active_updates"] - u0
     n = len(c["x"])
     return t, {"value": upd / (ms * 1e-3), "ms_total": ms, "ms_per_step": ms / K, "active_updates": upd,
                "active_fraction_per_step": upd / (K * n), "level_max": st["level_max"], "t_end": st["t"],
-               "phases_ms": {"build": s2["ms_build"], "density": s2["ms_density"], "forces": s2["ms_forces"]},
+               "phases_ms_first_passes": {"build": tm["ms_build"], "density": tm["ms_density"],
+                                          "forces": tm["ms_forces"]},
+               "repeat_passes_run": tm["repeat_passes"],
                "counts": {k: s2[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs", "cell_pairs",
                                              "exact_checks", "heavy_density", "heavy_forces")},
+               "counts_first_passes": {k: tm[k] for k in ("density_pairs", "hydro_pairs", "direct_pairs",
+                                                           "cell_pairs")},
                "launches": s2["launches"]}
 
 
@@ -482,15 +487,15 @@ def kdk_main(args, rank, world, local):
     R = out[head]
     ms_job = max_over_ranks(R["ms_total"], world)
     value = job_throughput(R["active_updates"], ms_job, world)
-    cnt = R["counts"]
+    cnt = R["counts_first_passes"]
     fp64 = head == "fp64"
     peak_gf = lib.gsph_fma_peak_gflops(local, 1 if fp64 else 0)
     f_force = (cnt["hydro_pairs"] * FLOPS["hydro_grav"] + cnt["direct_pairs"] * FLOPS["direct"] +
                cnt["cell_pairs"] * FLOPS["quad"])
     f_dens = cnt["density_pairs"] * FLOPS["density"]
-    passes = 3 * K
-    ms_f = R["phases_ms"]["forces"]
-    ms_d = R["phases_ms"]["density"]
+    passes = K                        # the first force pass of every step, event-timed
+    ms_f = R["phases_ms_first_passes"]["forces"]
+    ms_d = R["phases_ms_first_passes"]["density"]
     traffic = FORCE_TRAFFIC.get(("rotating_cloud", n, head))
     roof = {"bound": "fp64" if fp64 else "fp32",
             "kernel": "force pass (k_all_forces_mixed + heavy-leaf k_all_forces_mixed_wide)" if not fp64
@@ -502,7 +507,9 @@ def kdk_main(args, rank, world, local):
             "peak_source": "FMA-loop throughput measured live on this GPU (gsph_fma_peak_gflops); "
                            "the pair loops run on the FP32/FP64 pipes, not HBM or tensor cores",
             "flops_per_launch": f_force / passes, "ms_per_launch": ms_f / passes, "launches": passes,
-            "timing": "CUDA events recorded inside the K-step graph around every force pass, summed"}
+            "timing": "CUDA events recorded inside the K-step graph around the first force pass of every "
+                      "step, summed; flops from the interaction counts of those passes (the CheckTimesteps "
+                      "repeat passes are conditional graph nodes, which hold no events)"}
     roof_d = {"bound": roof["bound"], "kernel": "h solve (k_density_mixed + heavy-leaf k_density_mixed_pp, "
               "with the hmax update and mirror refresh)" if not fp64 else "h solve (k_density_fp64)",
               "achieved": f_dens / (ms_d * 1e-3) / 1e12, "peak": peak_gf / 1e3, "unit": "TFLOP/s",

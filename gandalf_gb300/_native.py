@@ -33,6 +33,12 @@ class KdkStatus(ctypes.Structure):
                 ("status", ctypes.c_uint32)]
 
 
+class KdkTiming(ctypes.Structure):
+    _fields_ = [("ms_build", ctypes.c_double), ("ms_density", ctypes.c_double), ("ms_forces", ctypes.c_double),
+                ("density_pairs", ctypes.c_int64), ("hydro_pairs", ctypes.c_int64), ("direct_pairs", ctypes.c_int64),
+                ("cell_pairs", ctypes.c_int64), ("steps", ctypes.c_int64), ("repeat_passes", ctypes.c_int64)]
+
+
 KDK_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "u", "dt", "tlast", "level", "nstep", "nlast", "levelneib"]
 
 
@@ -124,6 +130,7 @@ SIGNATURES = {
     "gsph_kdk_steps": (_I32, [_P, _I32, _I32]),
     "gsph_kdk_get_status": (_I32, [_P, ctypes.POINTER(KdkStatus)]),
     "gsph_kdk_get_state": (_I32, [_P, _I32, _D]),
+    "gsph_kdk_get_timing": (_I32, [_P, ctypes.POINTER(KdkTiming)]),
     "gsph_batch_create": (_P, [ctypes.POINTER(_P), _I32]),
     "gsph_batch_destroy": (None, [_P]),
     "gsph_batch_step": (_I32, [_P]),

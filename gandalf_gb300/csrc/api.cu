@@ -125,6 +125,14 @@ struct gsph_ctx {
   std::vector<int> pkind;
   size_t pused = 0;
   bool ptiming = false;
+  // CheckTimesteps repeat passes: captured as conditional graph nodes, nested two deep
+  cudaStream_t cond_stream[2] = {};
+  cudaStream_t cond_saved[2] = {};
+  int in_body = 0;                       // > 0 while capturing a conditional body
+  unsigned long long* kdk_snap = nullptr;   // first-pass counter snapshots, 8 per step
+  int kdk_snap_steps = 0;
+  unsigned kdk_cond_launches = 0;        // kernels of one repeat pass
+  gsph_kdk_timing kdk_timing{};          // of the last gsph_kdk_steps
   // CUDA graph of the whole step (gsph_step_graph), valid for one capture key
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -612,6 +620,7 @@ int read_status(gsph_ctx* c) {
 
 // Phase timestamps; inside a graph capture they become event-record nodes of the graph.
 void mark(gsph_ctx* c, int q) {
+  if (c->in_body) return;   // conditional graph bodies hold no event records
   if (c->capturing) cudaEventRecordWithFlags(c->ev[q], c->stream, cudaEventRecordExternal);
   else cudaEventRecord(c->ev[q], c->stream);
 }
@@ -859,6 +868,8 @@ void gsph_destroy(gsph_ctx* c) {
   free_all(c);
   if (c->aos) cudaFree(c->aos);
   if (c->aos_out) cudaFree(c->aos_out);
+  if (c->kdk_snap) cudaFree(c->kdk_snap);
+  for (int q = 0; q < 2; q++) if (c->cond_stream[q]) cudaStreamDestroy(c->cond_stream[q]);
   if (c->star_buf) cudaFree(c->star_buf);
   if (c->star_f) cudaFree(c->star_f);
   for (int q = 0; q < 5; q++) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
@@ -1922,7 +1933,62 @@ void sum_phases(gsph_ctx* c, double* ms) {
   (void) cudaGetLastError();
 }
 
-int kdk_step_body(gsph_ctx* c) {
+// The interaction counters (density, hydro, direct, cell pairs) copied to a snapshot slot.
+__global__ void k_snap_counters(const unsigned long long* counters, unsigned long long* dst) {
+  if (threadIdx.x < 4 && blockIdx.x == 0) dst[threadIdx.x] = counters[1 + threadIdx.x];
+}
+
+// Opens the conditional graph node of a CheckTimesteps repeat pass on the capturing stream:
+// a kernel sets the condition from the count of particles the last check activated, and
+// the pass is captured into the node's body on a stream of its own (nested for the third
+// pass), so that the graph skips a pass that would find no active particle.
+int cond_begin(gsph_ctx* c, int depth) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  GSPH_CUDA(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphConditionalHandle h;
+  GSPH_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+  launch_kdk_set_cond(h, c->kg, c->stream);
+  c->launches += 1;
+  GSPH_CUDA(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  GSPH_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+  GSPH_CUDA(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  GSPH_CUDA(cudaStreamBeginCaptureToGraph(c->cond_stream[depth], p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+  c->cond_saved[depth] = c->stream;
+  c->stream = c->cond_stream[depth];
+  c->in_body = depth + 1;
+  return GSPH_OK;
+}
+
+int cond_end(gsph_ctx* c, int depth) {
+  cudaGraph_t b = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->stream, &b);
+  c->stream = c->cond_saved[depth];
+  c->in_body = depth;
+  if (e != cudaSuccess) return cuda_fail(c, e, "conditional body capture");
+  return GSPH_OK;
+}
+
+// Stream launches only: whether the last CheckTimesteps activated particles (a host read).
+int host_activecount(gsph_ctx* c, int& count) {
+  KdkGlobal g{};
+  GSPH_CUDA(cudaMemcpyAsync(&g, c->kg, sizeof(g), cudaMemcpyDeviceToHost, c->stream));
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  count = g.activecount;
+  return GSPH_OK;
+}
+
+// One main-loop step.  step: index inside the current gsph_kdk_steps call (snapshot slots).
+int kdk_step_body(gsph_ctx* c, int step) {
   const KdkState s = make_kdk_state(c);
   const KdkLeaf l = make_kdk_leaf(c);
   launch_kdk_begin(c->kg, c->stream);
@@ -1932,24 +1998,48 @@ int kdk_step_body(gsph_ctx* c) {
   int rc = do_build(c);
   if (rc) return rc;
   pmark(c, kPhBuild);
+  int opened = 0;
   for (int pass = 0; pass < kKdkPasses; pass++) {
+    if (pass > 0) {
+      // a repeat pass runs only when CheckTimesteps activated particles: a conditional
+      // node in a captured graph, a host read otherwise (an empty pass changes nothing)
+      if (c->capturing) {
+        rc = cond_begin(c, pass - 1);
+        if (rc) break;
+        opened = pass;
+      } else {
+        int cnt = 0;
+        rc = host_activecount(c, cnt);
+        if (rc || cnt == 0) break;
+      }
+    }
+    const unsigned before = c->launches;
     // the tree is the same for all passes of a step: the first gathers every persistent
     // field into leaf order, the later ones only refresh the active flags and levels
     if (pass == 0) launch_kdk_gather(s, l, c->kg, c->stream);
     else launch_kdk_refresh(s, l, c->kg, c->stream);
     c->launches += 1;
-    pmark(c, kPhDensity);
+    const bool first = pass == 0 && c->kdk_snap && step < c->kdk_snap_steps;
+    if (first) k_snap_counters<<<1, 32, 0, c->stream>>>(c->counters, c->kdk_snap + 8 * step);
+    if (pass == 0) pmark(c, kPhDensity);
     rc = do_props(c);
-    if (rc) return rc;
-    pmark(c, kPhDensity);
-    pmark(c, kPhForces);
+    if (rc) break;
+    if (pass == 0) { pmark(c, kPhDensity); pmark(c, kPhForces); }
     rc = do_forces(c, c->cfg.self_gravity != 0);
-    if (rc) return rc;
-    pmark(c, kPhForces);
+    if (rc) break;
+    if (pass == 0) pmark(c, kPhForces);
+    if (first) k_snap_counters<<<1, 32, 0, c->stream>>>(c->counters, c->kdk_snap + 8 * step + 4);
     launch_kdk_scatter_lvn(s, l, c->stream);
     launch_kdk_check(s, c->kp, c->kg, pass == kKdkPasses - 1, c->stream);
     c->launches += pass == kKdkPasses - 1 ? 4 : 3;
+    if (pass > 0) c->kdk_cond_launches = c->launches - before;
   }
+  // close the bodies, innermost first
+  for (int d = opened; d > 0; d--) {
+    const int r2 = cond_end(c, d - 1);
+    if (!rc) rc = r2;
+  }
+  if (rc) return rc;
   launch_kdk_scatter_fields(s, l, c->stream);
   c->launches += 1;
   launch_kdk_timesteps(s, c->kp, c->kg, c->stream);
@@ -2039,6 +2129,16 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
   if (c->nstar) return fail(c, GSPH_ERR_UNSUPPORTED, "star particles need the N-body integrator (not implemented)");
   if (nsteps < 1 || nsteps > 100000) return fail(c, GSPH_ERR_INVALID, "nsteps out of range");
   cudaSetDevice(c->device);
+  for (int q = 0; q < 2; q++)
+    if (!c->cond_stream[q]) GSPH_CUDA(cudaStreamCreateWithFlags(&c->cond_stream[q], cudaStreamNonBlocking));
+  if (c->kdk_snap_steps < nsteps) {
+    if (c->kdk_snap) cudaFree(c->kdk_snap);
+    c->kdk_snap = nullptr;
+    c->kdk_snap_steps = 0;
+    drop_kdk_graph(c);   // a captured graph writes the old snapshot buffer
+    GSPH_CUDA(cudaMalloc(&c->kdk_snap, sizeof(unsigned long long) * 8 * (size_t) nsteps));
+    c->kdk_snap_steps = nsteps;
+  }
   int rc = begin_counters(c);
   if (rc) return rc;
   mark(c, 0);
@@ -2046,7 +2146,7 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
     rc = ensure_phase_events(c, nsteps);
     if (rc) return rc;
     c->ptiming = true;
-    for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c);
+    for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c, q);
     c->ptiming = false;
     if (rc) return rc;
   } else {
@@ -2064,7 +2164,7 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
       GSPH_CUDA(cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeRelaxed));
       c->capturing = true;
       c->ptiming = true;
-      for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c);
+      for (int q = 0; q < nsteps && !rc; q++) rc = kdk_step_body(c, q);
       c->ptiming = false;
       c->capturing = false;
       cudaGraph_t g = nullptr;
@@ -2088,6 +2188,28 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
   (void) cudaGetLastError();
   double ph[kPhKinds];
   sum_phases(c, ph);
+  {
+    gsph_kdk_timing& T = c->kdk_timing;
+    T = gsph_kdk_timing{};
+    T.ms_build = ph[kPhBuild];
+    T.ms_density = ph[kPhDensity];
+    T.ms_forces = ph[kPhForces];
+    T.steps = nsteps;
+    std::vector<unsigned long long> sn(8 * (size_t) nsteps);
+    if (cudaMemcpy(sn.data(), c->kdk_snap, sizeof(unsigned long long) * sn.size(), cudaMemcpyDeviceToHost) ==
+        cudaSuccess) {
+      for (int q = 0; q < nsteps; q++) {
+        const unsigned long long* a = &sn[8 * (size_t) q];
+        T.density_pairs += (int64_t) (a[4] - a[0]);
+        T.hydro_pairs += (int64_t) (a[5] - a[1]);
+        T.direct_pairs += (int64_t) (a[6] - a[2]);
+        T.cell_pairs += (int64_t) (a[7] - a[3]);
+      }
+    }
+    KdkGlobal g{};
+    if (cudaMemcpy(&g, c->kg, sizeof(g), cudaMemcpyDeviceToHost) == cudaSuccess) T.repeat_passes = (int64_t) g.repeat_passes;
+    (void) cudaGetLastError();
+  }
   // summed over the steps; the h solve phase includes the hmax update, the thermal update
   // and the mixed form's mirror refresh that follow it
   c->last.ms_build = ph[kPhBuild];
@@ -2097,6 +2219,12 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
   c->last.ms_total = ms;
   c->have_tree = c->have_props = c->have_forces = true;
   return rc;
+}
+
+int32_t gsph_kdk_get_timing(gsph_ctx* c, gsph_kdk_timing* out) {
+  if (!c || !out) return GSPH_ERR_INVALID;
+  *out = c->kdk_timing;
+  return GSPH_OK;
 }
 
 int32_t gsph_kdk_get_status(gsph_ctx* c, gsph_kdk_status* out) {

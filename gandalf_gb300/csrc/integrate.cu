@@ -115,6 +115,7 @@ __global__ void k_kdk_scatter(KdkState s, KdkLeaf l) {
 // Later passes of a step reuse the leaf-order fields in place: only the active flags, levels
 // and the levelneib accumulators are refreshed.
 __global__ void k_kdk_refresh(KdkState s, KdkLeaf l, KdkGlobal* g) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&g->repeat_passes, 1ull);
   unsigned long long act = 0;
   for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
     const int i = l.id[slot];
@@ -407,6 +408,10 @@ __global__ void k_kdk_thermal(Particles p, SphParams prm) {
   }
 }
 
+__global__ void k_kdk_set_cond(cudaGraphConditionalHandle h, const KdkGlobal* g) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, g->activecount > 0 ? 1u : 0u);
+}
+
 int grid_for(int n) { return n < 1 ? 1 : ((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8); }
 
 }  // namespace
@@ -460,6 +465,10 @@ void launch_kdk_setup_state(const KdkState& s, KdkGlobal* g, cudaStream_t st) {
 
 void launch_kdk_thermal(const Particles& p, const SphParams& prm, cudaStream_t st) {
   k_kdk_thermal<<<grid_for(p.n), 256, 0, st>>>(p, prm);
+}
+
+void launch_kdk_set_cond(cudaGraphConditionalHandle h, const KdkGlobal* g, cudaStream_t st) {
+  k_kdk_set_cond<<<1, 32, 0, st>>>(h, g);
 }
 
 void launch_kdk_setup_finish(const KdkState& s, cudaStream_t st) {

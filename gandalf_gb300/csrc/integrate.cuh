@@ -21,6 +21,7 @@ struct KdkGlobal {
   double t, timestep, dt_max, timestep_old;
   unsigned long long dtmin_bits;     // atomicMin over the bits of positive doubles
   unsigned long long active_updates; // active particles summed over all passes and steps
+  unsigned long long repeat_passes;  // CheckTimesteps repeat passes executed
 };
 
 enum KdkStatus : unsigned {
@@ -75,5 +76,7 @@ void launch_kdk_end(const KdkState& s, const KdkParams& kp, KdkGlobal* g, cudaSt
 void launch_kdk_setup_state(const KdkState& s, KdkGlobal* g, cudaStream_t st);
 void launch_kdk_setup_finish(const KdkState& s, cudaStream_t st);
 void launch_kdk_thermal(const Particles& p, const SphParams& prm, cudaStream_t st);
+// Sets a graph conditional to (particles were activated by the last CheckTimesteps).
+void launch_kdk_set_cond(cudaGraphConditionalHandle h, const KdkGlobal* g, cudaStream_t st);
 
 }  // namespace gsph

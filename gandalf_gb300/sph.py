@@ -210,6 +210,11 @@ class GradhSphTree:
         self._check(self._lib.gsph_kdk_get_status(self._ctx, ctypes.byref(st)), "kdk_status")
         return {k: getattr(st, k) for k, _ in _native.KdkStatus._fields_}
 
+    def kdk_timing(self) -> dict:
+        st = _native.KdkTiming()
+        self._check(self._lib.gsph_kdk_get_timing(self._ctx, ctypes.byref(st)), "kdk_timing")
+        return {k: getattr(st, k) for k, _ in _native.KdkTiming._fields_}
+
     def kdk_state(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
         """One integration field (input order); ``out``: an n-double array to fill."""
         if out is None:

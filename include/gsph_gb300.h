@@ -226,6 +226,17 @@ typedef struct gsph_kdk_status {
   uint32_t status;            /* 1: invalid timestep, 2: timestep checks did not settle */
 } gsph_kdk_status;
 int32_t gsph_kdk_get_status(gsph_ctx* ctx, gsph_kdk_status* out);
+/* Device time and interaction counts of the last gsph_kdk_steps call, for roofline
+ * accounting: tree builds, and the first h solve and force pass of every step (timed with
+ * CUDA events on the context's stream); the CheckTimesteps repeat passes run as conditional
+ * graph nodes, which hold no events, and are counted in repeat_passes only (the repeat
+ * passes found no active particle are skipped altogether). */
+typedef struct gsph_kdk_timing {
+  double ms_build, ms_density, ms_forces;
+  int64_t density_pairs, hydro_pairs, direct_pairs, cell_pairs;   /* of the first passes */
+  int64_t steps, repeat_passes;
+} gsph_kdk_timing;
+int32_t gsph_kdk_get_timing(gsph_ctx* ctx, gsph_kdk_timing* out);
 enum gsph_kdk_field {
   GSPH_KDK_X = 0, GSPH_KDK_Y, GSPH_KDK_Z, GSPH_KDK_VX, GSPH_KDK_VY, GSPH_KDK_VZ, GSPH_KDK_U, GSPH_KDK_DT,
   GSPH_KDK_TLAST, GSPH_KDK_LEVEL, GSPH_KDK_NSTEP, GSPH_KDK_NLAST, GSPH_KDK_LEVELNEIB, GSPH_KDK_COUNT

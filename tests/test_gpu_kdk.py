@@ -74,12 +74,30 @@ def test_kdk_matches_reference(name):
 
 
 def test_kdk_graph_equals_stream_launches():
+    """The graph (CheckTimesteps repeat passes as conditional nodes, set on the device) and
+    stream launches (the host reads whether a repeat pass has work) give identical states."""
     c, params, kdk, _, _ = load("rotating_kdk2048")
     a, sa = run(c, params, kdk, graph=True)
     b, sb = run(c, params, kdk, graph=False)
     for k in a:
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
     assert sa == sb
+
+
+def test_kdk_timing_of_first_passes():
+    c = ics_mod.rotating_cloud(16384, seed=44)
+    params = c.pop("params")
+    kdk = c.pop("kdk")
+    t = GradhSphTree(params, precision="mixed")
+    t.set_particles(c)
+    t.kdk_setup(**kdk)
+    t.kdk_steps(4, graph=True)
+    tm = t.kdk_timing()
+    st = t.stats()
+    t.close()
+    assert tm["steps"] == 4 and tm["ms_forces"] > 0 and tm["ms_density"] > 0 and tm["ms_build"] > 0
+    assert 0 < tm["hydro_pairs"] <= st["hydro_pairs"] and 0 < tm["cell_pairs"] <= st["cell_pairs"]
+    assert 0 <= tm["repeat_passes"] <= 8
 
 
 def test_kdk_mixed_tracks_fp64():
