@@ -304,15 +304,17 @@ def vec_err_stats(a, b, keys):
 
 
 def all_errors(a, b):
-    """Mixed against FP64 for every per-particle result.  du/dt and div v scatter about
-    zero (solid-body rotation and isothermal gas give zero, up to the SPH noise), so their
-    errors are taken relative to |b| + rms(b)."""
+    """Mixed against FP64 for every per-particle result.  div v and du/dt can be zero up to
+    rounding noise (solid-body rotation), so their errors are taken against their natural
+    scales, the sound-crossing rate c_s / h and u c_s / h (RMS over particles)."""
     out = {k: err_stats(a[k], b[k]) for k in ("h", "rho", "invomega", "zeta", "pressure", "sound", "gpot")
            if k in a}
-    for k in ("dudt", "div_v"):
+    rate = b["sound"] / b["h"]
+    for k, scale in (("div_v", rate), ("dudt", b["u"] * rate)):
         if k in a:
-            out[k] = err_stats(a[k], b[k], floor_frac=1.0)
-            out[k]["normalised_by"] = "|b| + rms(b)"
+            d = np.abs(np.asarray(a[k]) - np.asarray(b[k])) / np.sqrt(np.mean(scale * scale))
+            out[k] = {"rms": float(np.sqrt(np.mean(d * d))), "max": float(d.max()),
+                      "normalised_by": "rms of c_s/h" if k == "div_v" else "rms of u c_s/h"}
     out["a"] = vec_err_stats(a, b, ("ax", "ay", "az"))
     out["a_tree"] = vec_err_stats(a, b, ("agx", "agy", "agz"))
     return out

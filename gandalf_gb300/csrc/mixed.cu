@@ -114,6 +114,12 @@ __device__ __forceinline__ float gsum_f(float v) {
 
 __device__ __forceinline__ float fsqrt_pos(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
 
+// Index of the k-th set bit of m (k < popc(m)).
+__device__ __forceinline__ int nth_bit(unsigned m, int k) {
+  for (int i = 0; i < k; i++) m &= m - 1u;
+  return __ffs(m) - 1;
+}
+
 __device__ __forceinline__ bool fbox_overlap(const float* amin, const float* amax, float4 bmin, float4 bmax) {
   if (amin[0] > bmax.x || bmin.x > amax[0]) return false;
   if (amin[1] > bmax.y || bmin.y > amax[1]) return false;
@@ -230,15 +236,41 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   const bool mine = g < ncell && is_active(p, first + g);
   if (!__any_sync(kFull, mine)) return true;   // no active particle in this leaf
   const int slot = first + (g < ncell ? g : 0);
+  // active particles of the leaf, one bit each (warp-uniform)
+  constexpr int G = 32 / LPG;
+  unsigned amask = 0;
+  {
+    const unsigned gm = __ballot_sync(kFull, mine && sl == 0);
+#pragma unroll
+    for (int q = 0; q < G; q++)
+      if ((gm >> (q * LPG)) & 1u) amask |= 1u << q;
+  }
+  const int nact = __popc(amask);
+  // Lanes of the h iteration.  When every active particle's compact list fits (leaves
+  // that do not are handed over, give_up), the active particles share the warp evenly —
+  // 32 / p lanes each, p the power of two at or above their count — instead of LPG lanes
+  // per particle, so the lanes of inactive particles (block timesteps) do not idle.
+  const bool remap = give_up && WARPS == 1;
+  int it_g = g, it_sl = sl, it_L = LPG;
+  if (remap) {
+    int p2 = 1;
+    while (p2 < nact) p2 <<= 1;
+    it_L = 32 / p2;
+    const int k = lane / it_L;
+    it_sl = lane % it_L;
+    it_g = k < nact ? nth_bit(amask, k) : -1;
+  }
+  const bool it_mine = remap ? it_g >= 0 : mine;
+  const int it_slot = first + (it_g >= 0 && it_g < ncell ? it_g : 0);
+  const double it_m = p.m[it_slot], it_h0 = p.h[it_slot];
   const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
-  const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
-  const double h_start = p.h[slot];
+  const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot];
   const CellBox bb = t.bb[c];
   const double hmax0 = t.geom[c].hmax;
   unsigned long long pairs = 0;
   bool fail = false, stack_ok = true;
   double mcheck = 0.0;
-  double h_out = h_start, rho_out = 0.0, om_out = 0.0, zeta_out = 0.0;
+  double h_out = it_h0, rho_out = 0.0, om_out = 0.0, zeta_out = 0.0;
 
   // returns 1 if the cell aborts (some h > hmax_list), 2 if the warp gives up (gather or
   // compact list too long for a warp on its own; only when give_up), 0 when solved
@@ -342,22 +374,21 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     // particle whose list does not fit loops over the candidates instead.  The build runs
     // one candidate per lane (LPG leaves of up to 32/LPG particles per round, coalesced
     // loads) against every particle of the cell, eight at a time from registers.
-    constexpr int G = 32 / LPG;
     const unsigned ltm = (1u << lane) - 1u;
-    float2* clist = compact + g * kcap;
     int ccount = 0;
     const float lim2 = (float) (kKernRangeSqd * hmax_list * hmax_list) * (1.0f + kMargin);
     if (!overflow) {
-      const int ntgt = ncell < G ? ncell : G;
+      const int ntgt = nact;   // the active particles only: the others solve nothing
       // positions relative to the leaf centre (hi + lo pairs): a few float ulps of the
       // separation, three registers a target
       const float4 lch = mc.geo_hi[c], lcl = mc.geo_lo[c];
       for (int gc = 0; gc < ntgt; gc += 8) {
         float tx[8], ty[8], tz[8];
-        int tc[8];
+        int tc[8], tgi[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-          const int tg = gc + u < ntgt ? gc + u : ntgt - 1;
+          const int tg = nth_bit(amask, gc + u < ntgt ? gc + u : ntgt - 1);
+          tgi[u] = tg;
           const float4 h = mp.pos_hi[first + tg], l = mp.pos_lo[first + tg];
           tx[u] = (h.x - lch.x) + (l.x - lcl.x);
           ty[u] = (h.y - lch.y) + (l.y - lcl.y);
@@ -388,30 +419,34 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
             const unsigned b = __ballot_sync(kFull, keep);
             if (keep) {
               const int pos = tc[u] + __popc(b & ltm);
-              if (pos < kcap) compact[(gc + u) * kcap + pos] = make_float2(d2, ch.w);
+              if (pos < kcap) compact[tgi[u] * kcap + pos] = make_float2(d2, ch.w);
             }
             tc[u] += __popc(b);
           }
         }
 #pragma unroll
         for (int u = 0; u < 8; u++)
-          if (gc + u == g) ccount = tc[u];
+          if (gc + u < ntgt && tgi[u] == g) ccount = tc[u];
       }
     }
     // A particle whose compact list does not fit would rescan every candidate in every
     // iteration, and its warp with it (such leaves took 5-10x the mean): hand the leaf to
     // the heavy-leaf kernel instead.
     if (give_up && __any_sync(kFull, mine && !overflow && ccount > kcap)) return 2;
-    const bool use_compact = !overflow && ccount <= kcap;
+    // the iteration lane's particle: its compact list and count (held by its group's lanes)
+    const int cg = it_g >= 0 ? it_g : 0;
+    const int ccount_it = __shfl_sync(kFull, ccount, cg * LPG);
+    float2* clist = compact + cg * kcap;
+    const bool use_compact = remap || (!overflow && ccount <= kcap);
 
     // The iteration state (h, its bracket, the h(rho) target) and the convergence test are
     // fp64, as in the reference (GradhSph.cpp:206-254); the kernel sums are float.
-    double hi = h_start, h_lower = 0.0, h_upper = hmax_list;
+    double hi = it_h0, h_lower = 0.0, h_upper = hmax_list;
     double invh = 1.0 / hi, hrho_last = hi;
-    const double inv_m = 1.0 / mi, inv_hfac = 1.0 / prm.h_fac;
+    const double inv_m = 1.0 / it_m, inv_hfac = 1.0 / prm.h_fac;
     double rho = 0.0, om = 0.0, zeta = 0.0;
     int iteration = 0;
-    bool done = !mine, abort_cell = false;
+    bool done = !it_mine, abort_cell = false;
     double mloc = 0.0;
     for (;;) {
       bool any_active = __any_sync(kFull, !done);
@@ -455,7 +490,7 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         }
       };
       if (use_compact) {
-        if (!done) for (int e = sl; e < ccount; e += LPG) { const float2 v = clist[e]; add(v.x, v.y); }
+        if (!done) for (int e = it_sl; e < ccount_it; e += it_L) { const float2 v = clist[e]; add(v.x, v.y); }
       } else if (!overflow) {
         consume(ncached);
       } else {
@@ -469,15 +504,13 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         drho = (double) srho - (double) crho;
         dom = (double) som - (double) com;
         dze = (double) sze - (double) cze;
-#pragma unroll
-        for (int o = 1; o < LPG; o <<= 1) {
+        for (int o = 1; o < it_L; o <<= 1) {
           drho += __shfl_xor_sync(kFull, drho, o);
           dom += __shfl_xor_sync(kFull, dom, o);
           dze += __shfl_xor_sync(kFull, dze, o);
         }
       } else {
-#pragma unroll
-        for (int o = 1; o < LPG; o <<= 1) {
+        for (int o = 1; o < it_L; o <<= 1) {
           srho += __shfl_xor_sync(kFull, srho, o);
           som += __shfl_xor_sync(kFull, som, o);
           sze += __shfl_xor_sync(kFull, sze, o);
@@ -503,7 +536,7 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     bool any_abort = __any_sync(kFull, abort_cell);
     if (WARPS > 1) any_abort = __syncthreads_or(any_abort);
     mcheck = fmax(mcheck, mw);
-    if (!any_abort && mine) {
+    if (!any_abort && it_mine) {
       h_out = fmax(hrho_last, h_lower);
       rho_out = rho; om_out = om; zeta_out = zeta;
     }
@@ -532,11 +565,10 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   // the SPH-star zeta term, the particle's LPG lanes sharing the stars
   float zs = 0.0f;
   if (prm.stars.n) {
-    if (mine) zs = star_zeta_part_f(prm.stars, pih, pil, (float) h_out, sl, LPG);
-#pragma unroll
-    for (int o = 1; o < LPG; o <<= 1) zs += __shfl_xor_sync(kFull, zs, o);
+    if (it_mine) zs = star_zeta_part_f(prm.stars, mp.pos_hi[it_slot], mp.pos_lo[it_slot], (float) h_out, it_sl, it_L);
+    for (int o = 1; o < it_L; o <<= 1) zs += __shfl_xor_sync(kFull, zs, o);
   }
-  if (mine && sl == 0 && wib == 0) finish_density(p, prm, slot, h_out, rho_out, om_out, zeta_out, (double) zs);
+  if (it_mine && it_sl == 0 && wib == 0) finish_density(p, prm, it_slot, h_out, rho_out, om_out, zeta_out, (double) zs);
   return true;
 }
 
@@ -1064,6 +1096,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
 #pragma unroll
     for (int u = 0; u < 8; u++) {
       if (u0 + u >= GT) break;
+      if (tgt[u0 + u].w == 0.0f) continue;   // inactive target: nothing was summed (warp-uniform)
 #pragma unroll
       for (int k = 0; k < 4; k++)
         for (int o = 16; o > 0; o >>= 1) acc[u][k] = __fadd_rn(acc[u][k], __shfl_xor_sync(kFull, acc[u][k], o));
