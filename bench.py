@@ -371,7 +371,7 @@ def precision_step(c, params, h_converge=None, record=True):
     return out
 
 
-def run_kdk_form(c, params, kdk, form, K, warm_seq, stream, device):
+def run_kdk_form(c, params, kdk, form, K, warm_seq, stream, device, graph=True):
     """Warm-up sequences (setup + K graph-replayed steps), then the timed one: setup
     outside, the K steps between CUDA events on the stream.  Returns the context open."""
     import torch
@@ -384,14 +384,14 @@ def run_kdk_form(c, params, kdk, form, K, warm_seq, stream, device):
     for _ in range(warm_seq):
         t.set_particles(c)
         t.kdk_setup(**kdk)
-        t.kdk_steps(K, graph=True)          # the first call captures the K-step graph
+        t.kdk_steps(K, graph=graph)         # the first call captures the K-step graph
     t.set_particles(c)
     t.kdk_setup(**kdk)
     torch.cuda.synchronize()
     u0 = t.kdk_status()["active_updates"]
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    t.kdk_steps(K, graph=True)
+    t.kdk_steps(K, graph=graph)
     ev1.record(stream)
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -476,7 +476,7 @@ def kdk_main(args, rank, world, local):
             if world > 1:
                 import torch.distributed as dist
                 dist.barrier()
-            t, R = run_kdk_form(c, params, kdk, form, K, warm_seq, stream, local)
+            t, R = run_kdk_form(c, params, kdk, form, K, warm_seq, stream, local, graph=not args.no_graph)
             finals[form] = t.results()
             for k in ("x", "y", "z"):
                 finals[form]["pos_" + k] = t.kdk_state(k)
@@ -521,7 +521,7 @@ def kdk_main(args, rank, world, local):
             "ms_per_step": ms_job / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if fp64 else "f32 pairs / f64 positions, h iteration and moments",
             "data": "synthetic (seeded rotating-cloud generator, no dataset)", "config": cfg,
-            "run": {"precision": head, "cuda_graph": "K steps in one graph",
+            "run": {"precision": head, "cuda_graph": "stream launches" if args.no_graph else "K steps in one graph",
                     "warmup_sequences": warm_seq, "warmup_kdk_steps": warm_seq * K,
                     "l2": "working set (1M particles, ~0.6 GB) larger than L2; not flushed",
                     "parallelism": f"replicas{world}"},

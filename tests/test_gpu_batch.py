@@ -64,3 +64,22 @@ def test_kh_box_against_oracle():
     check_mixed(t.results(), ref)
     b.close()
     t.close()
+
+
+def test_largest_ensemble_box_inside_a_batch_against_oracle():
+    """The largest box of the 64-box ensemble (about 129k particles) stepped inside a batch
+    with the smallest and a middle-sized box, against the oracle."""
+    boxes = ics_mod.kh_ensemble(64, 4096, 131072, seed=2024)
+    sizes = [len(b["x"]) for b in boxes]
+    order = np.argsort(sizes)
+    pick = [boxes[order[0]], boxes[order[len(order) // 2]], boxes[order[-1]]]
+    trees = [make(dict(c))[0] for c in pick]
+    b = GradhSphBatch(trees)
+    b.step()
+    big = pick[-1]
+    assert len(big["x"]) > 120000
+    ref = oracle.run({k: v for k, v in big.items() if k != "params"}, dict(big["params"]))["particles"]
+    print(len(big["x"]), check_mixed(trees[-1].results(), ref))
+    b.close()
+    for t in trees:
+        t.close()

@@ -78,3 +78,21 @@ def test_removing_stars_restores_the_gas_only_result():
     ref = oracle.run(gas, params)["particles"]
     check_fp64(without, ref, True)
     assert np.abs(with_stars["gpot"] - without["gpot"]).max() > 1e-6
+
+
+def test_evrard_sphere_with_stars_against_oracle():
+    """The Evrard configuration's shape at a seeded smaller N: a rho ~ 1/r gas sphere of
+    65,536 particles with 64 stars (m = 1e-3, uniform in r < 0.5), FP64 form against the
+    oracle at the FP64 tolerances, mixed form within MIXED_TOL and its star <- gas forces
+    within 1e-5."""
+    c = ics_mod.evrard_sphere(65536, seed=53, nstar=64)
+    params = c.pop("params")
+    r = oracle.run(c, params)
+    out, stars = run(c, params)
+    check_fp64(out, r["particles"], True)
+    assert_close("gpot_hydro", out["gpot_hydro"], r["particles"]["gpot_hydro"], 1e-11)
+    check_stars(stars, r["stars"])
+    mo, ms = run(c, params, precision="mixed")
+    print(check_mixed(mo, r["particles"]))
+    for k in ("ax", "ay", "az", "gpot"):
+        assert_close("mixed star " + k, ms[k], r["stars"][k], 1e-5)
