@@ -111,6 +111,9 @@ SIGNATURES = {
     "gsph_set_recording": (_I32, [_P, _I32, _I32]),
     "gsph_get_sph_neighbours": (_I64, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]),
     "gsph_get_direct_summary": (_I32, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint64)]),
+    "gsph_set_list_recording": (_I32, [_P, _I32, _I32]),
+    "gsph_get_direct_lists": (_I64, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]),
+    "gsph_get_cell_lists": (_I64, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]),
     "gsph_get_cell_summary": (_I32, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
                                      ctypes.POINTER(ctypes.c_uint64)]),
     "gsph_set_stream": (_I32, [_P, _P]),

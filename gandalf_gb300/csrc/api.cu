@@ -91,6 +91,10 @@ struct gsph_ctx {
   unsigned long long *rec_dir_cnt = nullptr, *rec_dir_hash = nullptr, *rec_cell_cnt = nullptr,
                      *rec_cell_hash = nullptr;
   size_t rec_bytes = 0;
+  // full direct-sum and multipole-cell lists (gsph_set_list_recording)
+  int rec_dir_max = 0, rec_cell_max = 0;
+  int *rec_dir_n = nullptr, *rec_dir_ids = nullptr, *rec_cell_n = nullptr, *rec_cell_ids = nullptr;
+  size_t rec_full_bytes = 0;
   // mixed-precision mirrors and the heavy-leaf hand-over list
   float4 *mp_pos_hi = nullptr, *mp_pos_lo = nullptr, *mp_vel = nullptr, *mp_hyd = nullptr, *mp_aux = nullptr;
   float4 *mc_geo_hi = nullptr, *mc_geo_lo = nullptr, *mc_com_hi = nullptr, *mc_com_lo = nullptr, *mc_quad = nullptr,
@@ -314,6 +318,8 @@ int ensure_capacity(gsph_ctx* c, int n) {
     c->cap = capn;
     c->cap_ncell = capc;
     c->rec_bytes = 0;   // recording buffers were freed with the rest
+    c->rec_full_bytes = 0;
+    c->rec_dir_n = c->rec_dir_ids = c->rec_cell_n = c->rec_cell_ids = nullptr;
     c->rec_sph_cnt = nullptr;
   }
   if (fresh || n != c->n || ltot != c->ltot) { drop_graph(c); drop_kdk_graph(c); }
@@ -431,6 +437,11 @@ DeviceCounters make_counters(gsph_ctx* c) {
   d.rec_sph_cnt = c->rec_sph_cnt; d.rec_sph_ids = c->rec_sph_ids;
   d.rec_dir_cnt = c->rec_dir_cnt; d.rec_dir_hash = c->rec_dir_hash;
   d.rec_cell_cnt = c->rec_cell_cnt; d.rec_cell_hash = c->rec_cell_hash;
+  if (d.record && c->rec_dir_max > 0 && c->rec_dir_n) {
+    d.rec_dir_max = c->rec_dir_max; d.rec_cell_max = c->rec_cell_max;
+    d.rec_dir_n = c->rec_dir_n; d.rec_dir_ids = c->rec_dir_ids;
+    d.rec_cell_n = c->rec_cell_n; d.rec_cell_ids = c->rec_cell_ids;
+  }
   return d;
 }
 
@@ -679,7 +690,7 @@ int do_props(gsph_ctx* c) {
   GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
   mark(c, 2);
   launch_update_hmax(t, p, c->stream);
-  c->launches += 1;
+  c->launches += 2;
   if (c->kdk || c->bactive) {   // every particle's thermal properties before the force pass
     launch_kdk_thermal(p, make_params(c), c->stream);
     c->launches += 1;
@@ -702,6 +713,10 @@ int do_forces(gsph_ctx* c, bool gravity) {
     GSPH_CUDA(cudaMemsetAsync(c->rec_dir_hash, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));
     GSPH_CUDA(cudaMemsetAsync(c->rec_cell_cnt, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
     GSPH_CUDA(cudaMemsetAsync(c->rec_cell_hash, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
+    if (c->rec_dir_max > 0 && c->rec_dir_n) {
+      GSPH_CUDA(cudaMemsetAsync(c->rec_dir_n, 0, sizeof(int) * (size_t) c->n, c->stream));
+      GSPH_CUDA(cudaMemsetAsync(c->rec_cell_n, 0, sizeof(int) * (size_t) c->nleaf, c->stream));
+    }
   }
   HeavyList heavy{c->heavy_leaves, c->heavy_count};
   if (mixed(c)) {
@@ -741,11 +756,13 @@ int begin_counters(gsph_ctx* c) {
   return GSPH_OK;
 }
 
+int ensure_full_lists(gsph_ctx* c);
+
 int ensure_recording(gsph_ctx* c) {
   if (!c->record) return GSPH_OK;
   const size_t need = (size_t) c->n * (sizeof(int) * (1 + c->rec_max) + 2 * sizeof(unsigned long long)) +
                       (size_t) c->nleaf * 2 * sizeof(unsigned long long);
-  if (c->rec_sph_cnt && c->rec_bytes >= need) return GSPH_OK;
+  if (c->rec_sph_cnt && c->rec_bytes >= need) return ensure_full_lists(c);
   drop_graph(c);   // a captured step holds the old recording buffers
   drop_kdk_graph(c);
   int rc = alloc(c, c->rec_sph_cnt, c->n);
@@ -756,6 +773,22 @@ int ensure_recording(gsph_ctx* c) {
   if (!rc) rc = alloc(c, c->rec_cell_hash, c->nleaf);
   if (rc) return rc;
   c->rec_bytes = need;
+  return ensure_full_lists(c);
+}
+
+// Full-list buffers for the current particle count (gsph_set_list_recording).
+int ensure_full_lists(gsph_ctx* c) {
+  if (!c->record || c->rec_dir_max <= 0) return GSPH_OK;
+  const size_t need = (size_t) c->n * (1 + (size_t) c->rec_dir_max) + (size_t) c->nleaf * (1 + (size_t) c->rec_cell_max);
+  if (c->rec_dir_n && c->rec_full_bytes >= need) return GSPH_OK;
+  drop_graph(c);
+  drop_kdk_graph(c);
+  int rc = alloc(c, c->rec_dir_n, c->n);
+  if (!rc) rc = alloc(c, c->rec_dir_ids, (size_t) c->n * c->rec_dir_max);
+  if (!rc) rc = alloc(c, c->rec_cell_n, c->nleaf);
+  if (!rc) rc = alloc(c, c->rec_cell_ids, (size_t) c->nleaf * c->rec_cell_max);
+  if (rc) return rc;
+  c->rec_full_bytes = need;
   return GSPH_OK;
 }
 
@@ -1373,6 +1406,72 @@ int32_t gsph_get_cell_summary(gsph_ctx* c, int32_t* leaf_cells, int64_t* counts,
   return GSPH_OK;
 }
 
+int32_t gsph_set_list_recording(gsph_ctx* c, int32_t max_direct, int32_t max_cells) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (max_direct < 0 || max_cells < 0 || max_direct > (1 << 20) || max_cells > (1 << 20) ||
+      (max_direct > 0) != (max_cells > 0))
+    return fail(c, GSPH_ERR_INVALID, "list capacities must both be 0 or both in 1..2^20");
+  if (max_direct != c->rec_dir_max || max_cells != c->rec_cell_max) {
+    drop_graph(c);
+    drop_kdk_graph(c);
+    c->rec_dir_n = c->rec_dir_ids = c->rec_cell_n = c->rec_cell_ids = nullptr;   // reallocated on demand
+    c->rec_full_bytes = 0;
+  }
+  c->rec_dir_max = max_direct;
+  c->rec_cell_max = max_cells;
+  return GSPH_OK;
+}
+
+int64_t gsph_get_direct_lists(gsph_ctx* c, int64_t* offsets, int32_t* ids) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->record || !c->rec_dir_n || !c->have_forces) return fail(c, GSPH_ERR_STATE, "no recorded force pass with full lists");
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  const int n = c->n, mx = c->rec_dir_max;
+  std::vector<int> cnt(n), idv(n), all((size_t) n * mx);
+  GSPH_CUDA(cudaMemcpy(cnt.data(), c->rec_dir_n, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(idv.data(), c->id, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(all.data(), c->rec_dir_ids, sizeof(int) * all.size(), cudaMemcpyDeviceToHost));
+  std::vector<int64_t> cin(n);
+  int64_t total = 0;
+  for (int s = 0; s < n; s++) {
+    if (cnt[s] > mx) return fail(c, GSPH_ERR_CAPACITY, "a direct-sum list exceeded max_direct");
+    cin[idv[s]] = cnt[s];
+    total += cnt[s];
+  }
+  if (!ids) return total;
+  if (!offsets) return GSPH_ERR_INVALID;
+  offsets[0] = 0;
+  for (int i = 0; i < n; i++) offsets[i + 1] = offsets[i] + cin[i];
+  for (int s = 0; s < n; s++)
+    for (int k = 0; k < cnt[s]; k++) ids[offsets[idv[s]] + k] = all[(size_t) s * mx + k];
+  return total;
+}
+
+int64_t gsph_get_cell_lists(gsph_ctx* c, int64_t* offsets, int32_t* cells) {
+  if (!c) return GSPH_ERR_INVALID;
+  if (!c->record || !c->rec_cell_n || !c->have_forces) return fail(c, GSPH_ERR_STATE, "no recorded force pass with full lists");
+  cudaSetDevice(c->device);
+  GSPH_CUDA(cudaStreamSynchronize(c->stream));
+  const int nl = c->nleaf, mx = c->rec_cell_max;
+  std::vector<int> cnt(nl), all((size_t) nl * mx);
+  GSPH_CUDA(cudaMemcpy(cnt.data(), c->rec_cell_n, sizeof(int) * nl, cudaMemcpyDeviceToHost));
+  GSPH_CUDA(cudaMemcpy(all.data(), c->rec_cell_ids, sizeof(int) * all.size(), cudaMemcpyDeviceToHost));
+  int64_t total = 0;
+  for (int q = 0; q < nl; q++) {
+    if (cnt[q] > mx) return fail(c, GSPH_ERR_CAPACITY, "a multipole-cell list exceeded max_cells");
+    total += cnt[q];
+  }
+  if (!cells) return total;
+  if (!offsets) return GSPH_ERR_INVALID;
+  offsets[0] = 0;
+  for (int q = 0; q < nl; q++) {
+    offsets[q + 1] = offsets[q] + cnt[q];
+    for (int k = 0; k < cnt[q]; k++) cells[offsets[q] + k] = all[(size_t) q * mx + k];
+  }
+  return total;
+}
+
 int32_t gsph_get_tree(gsph_ctx* c, int32_t* cell_n, int32_t* cell_first, int32_t* order, double* cell_data) {
   if (!c) return GSPH_ERR_INVALID;
   if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "tree not built");
@@ -1664,13 +1763,17 @@ int batch_body(gsph_batch* b) {
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count, 0, sizeof(int), c->stream));
     launch_update_hmax(t, p, c->stream);
     launch_mixed_prep_hydro(t, p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
-    c->launches += 3;
+    c->launches += 4;
     if (c->record && c->rec_sph_cnt) {
       GSPH_CUDA(cudaMemsetAsync(c->rec_sph_cnt, 0, sizeof(int) * (size_t) c->n, c->stream));
       GSPH_CUDA(cudaMemsetAsync(c->rec_dir_cnt, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));
       GSPH_CUDA(cudaMemsetAsync(c->rec_dir_hash, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));
       GSPH_CUDA(cudaMemsetAsync(c->rec_cell_cnt, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
       GSPH_CUDA(cudaMemsetAsync(c->rec_cell_hash, 0, sizeof(unsigned long long) * (size_t) c->nleaf, c->stream));
+      if (c->rec_dir_max > 0 && c->rec_dir_n) {
+        GSPH_CUDA(cudaMemsetAsync(c->rec_dir_n, 0, sizeof(int) * (size_t) c->n, c->stream));
+        GSPH_CUDA(cudaMemsetAsync(c->rec_cell_n, 0, sizeof(int) * (size_t) c->nleaf, c->stream));
+      }
     }
     return check_launch(c, "batch hmax update");
   });

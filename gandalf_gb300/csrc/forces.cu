@@ -334,7 +334,7 @@ k_all_forces_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
         if (drsqd >= T.hrangesqd && drsqd >= p.hrangesqd[j]) {
           direct_term(dx, dy, dz, p.m[j], A);
           ndir++;
-          if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
+          if (cnt.record) { dhash += mix64((unsigned long long) p.id[j]); rec_direct_id(cnt, slot, p.id[j]); }
         } else {
           hydro_grav_pair(prm, p, T, j, dx, dy, dz, drsqd, A);
           lvn_pair(p, slot, j, lvn_own);
@@ -354,14 +354,18 @@ k_all_forces_fp64(Tree t, Particles p, SphParams prm, DeviceCounters cnt) {
         const int j = f + q;
         direct_term(p.x[j] - T.x, p.y[j] - T.y, p.z[j] - T.z, p.m[j], A);
         ndir++;
-        if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
+        if (cnt.record) { dhash += mix64((unsigned long long) p.id[j]); rec_direct_id(cnt, slot, p.id[j]); }
       }
     }
     // accepted cells: multipole terms
     for (int e = sl; e < L.nc; e += LPG) {
       cell_term(t.mom[L.c[e]], T, quad, A);
       ncellp++;
-      if (cnt.record && g == 0) { chash += mix64((unsigned long long) L.c[e]); ccount++; }
+      if (cnt.record && g == 0) {
+        chash += mix64((unsigned long long) L.c[e]);
+        ccount++;
+        rec_cell_id(cnt, leaf, L.c[e]);
+      }
     }
   };
   const bool ok = warp_walk(0, t.ltot, t.cell_level, s_stack[wib], kForceStack, L, decide, tag, consume);

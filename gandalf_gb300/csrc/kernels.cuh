@@ -21,7 +21,23 @@ struct DeviceCounters {
   unsigned long long* rec_dir_hash;    // per slot: sum of mix64(input id)
   unsigned long long* rec_cell_cnt;    // per leaf index
   unsigned long long* rec_cell_hash;   // per leaf index: sum of mix64(cell id)
+  // optional full lists (nullptr: not kept): direct-sum partners per slot (input ids) and
+  // multipole cells per leaf index (depth-first ids), rec_*_max entries each
+  int rec_dir_max, rec_cell_max;
+  int *rec_dir_n, *rec_dir_ids;
+  int *rec_cell_n, *rec_cell_ids;
 };
+
+__device__ __forceinline__ void rec_direct_id(const DeviceCounters& c, int slot, int id) {
+  if (!c.rec_dir_ids) return;
+  const int k = atomicAdd(&c.rec_dir_n[slot], 1);
+  if (k < c.rec_dir_max) c.rec_dir_ids[(size_t) slot * c.rec_dir_max + k] = id;
+}
+__device__ __forceinline__ void rec_cell_id(const DeviceCounters& c, int leaf, int cell) {
+  if (!c.rec_cell_ids) return;
+  const int k = atomicAdd(&c.rec_cell_n[leaf], 1);
+  if (k < c.rec_cell_max) c.rec_cell_ids[(size_t) leaf * c.rec_cell_max + k] = cell;
+}
 
 __host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
   x += 0x9E3779B97F4A7C15ull;

@@ -1152,7 +1152,11 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           acc[u][2] = __fadd_rn(acc[u][2], az); acc[u][3] = __fadd_rn(acc[u][3], pot);
           ncellp++;
         }
-        if (u0 == 0 && cnt.record) { chash += mix64((unsigned long long) cc); ccount++; }
+        if (u0 == 0 && cnt.record) {
+          chash += mix64((unsigned long long) cc);
+          ccount++;
+          rec_cell_id(cnt, leaf, cc);
+        }
       }
       add_to_targets(acc, u0);
     }
@@ -1187,6 +1191,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
             const int ts = first + pfirst + u0 + u;
             atomicAdd(&cnt.rec_dir_cnt[ts], 1ull);
             atomicAdd(&cnt.rec_dir_hash[ts], mix64((unsigned long long) p.id[j]));
+            rec_direct_id(cnt, ts, p.id[j]);
           }
         }
       }
@@ -1216,7 +1221,10 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         } else {
           direct_term_f(dx, dy, dz, pjh.w, A, prm.compensated != 0);
           ndir++;
-          if (cnt.record) dhash += mix64((unsigned long long) p.id[j]);
+          if (cnt.record) {
+            dhash += mix64((unsigned long long) p.id[j]);
+            rec_direct_id(cnt, slot, p.id[j]);
+          }
         }
       }
     }
@@ -1271,7 +1279,11 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
       consume_ab(); consume_b(); L.na = 0; L.nb = 0; __syncwarp();
     }
   }
-  if (gave_up) return false;
+  if (gave_up) {
+    // cells already consumed are recorded again by the kernel that takes the leaf over
+    if (cnt.rec_cell_ids && lane == 0) cnt.rec_cell_n[leaf] = 0;
+    return false;
+  }
   consume_ab();
   consume_b();
   consume_c();

@@ -574,7 +574,8 @@ __device__ void stock_parent(const Tree& t, int c, int level, double theta2) {
 // in turn with coalesced loads, and the sums, minima and maxima meet by shuffles within
 // the 8 lanes.  The sums' order therefore differs from the reference's sequential loop
 // (rounding only); minima, maxima and with them every box, rmax and cdistsqd are exact.
-// The first lane of each leaf then climbs: the second child to arrive at a parent stocks it.
+// The parents follow in k_stock_climb, one climbing thread per leaf (a climb by one lane of
+// eight would leave most of each warp idle through the serial parent updates).
 constexpr int kStockLanes = 8;
 
 __device__ __forceinline__ double red_sum8(double v) {
@@ -669,7 +670,14 @@ __global__ void k_stock(Tree t, Particles p, double theta2) {
   for (int k = 0; k < 5; k++) mo.q[k] = q[k];
   mo.pad = 0.0;
   t.mom[c] = mo;
-  climb_stock(t, c, theta2);
+}
+
+// The parents, bottom-up: one thread per leaf climbs while it is the second child to
+// arrive at a parent (arrival counters), stocking that parent from its two children.
+__global__ void k_stock_climb(Tree t, double theta2) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= t.nleaf) return;
+  climb_stock(t, t.leaf_cell[s], theta2);
 }
 
 // KDTree::UpdateHmaxValues: hmax and hbox from the solved h; cdistsqd keeps its value.
@@ -697,11 +705,16 @@ __global__ void k_update_hmax(Tree t, Particles p) {
   for (int k = 0; k < 3; k++) { hbmin[k] = red_min8(hbmin[k]); hbmax[k] = red_max8(hbmax[k]); }
   if (!has || sub != 0) return;
   t.geom[c].hmax = hmax;
-  {
-    CellBox hb;
-    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
-    t.hbox[c] = hb;
-  }
+  CellBox hb;
+  for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
+  t.hbox[c] = hb;
+}
+
+// The parents' hmax and hbox, bottom-up as in k_stock_climb.
+__global__ void k_update_hmax_climb(Tree t) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= t.nleaf) return;
+  int c = t.leaf_cell[s];
   int level = t.ltot;
   while (level > 0) {
     const int parent = t.cell_parent[c];
@@ -807,12 +820,14 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
   k_gather_leaf_order<<<grid_for(n, 256), 256, 0, st>>>(n, cur.l[0], a.in, a.p, a.id_out, a.slot_of);
   cudaMemsetAsync(a.tree.climb, 0, sizeof(unsigned) * (size_t) a.tree.ncell, st);
   k_stock<<<(a.tree.nleaf * kStockLanes + 127) / 128, 128, 0, st>>>(a.tree, a.p, a.thetamaxsqd);
-  return launches + 2;
+  k_stock_climb<<<(a.tree.nleaf + 127) / 128, 128, 0, st>>>(a.tree, a.thetamaxsqd);
+  return launches + 3;
 }
 
 void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st) {
   cudaMemsetAsync(t.climb, 0, sizeof(unsigned) * (size_t) t.ncell, st);
   k_update_hmax<<<(t.nleaf * kStockLanes + 127) / 128, 128, 0, st>>>(t, p);
+  k_update_hmax_climb<<<(t.nleaf + 127) / 128, 128, 0, st>>>(t);
 }
 
 }  // namespace gsph

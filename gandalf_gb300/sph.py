@@ -300,6 +300,30 @@ class GradhSphTree:
             self._check(int(r), "sph_neighbours")
         return off, ids[:int(tot)]
 
+    def set_list_recording(self, max_direct: int, max_cells: int):
+        self._check(self._lib.gsph_set_list_recording(self._ctx, int(max_direct), int(max_cells)),
+                    "set_list_recording")
+
+    def _csr(self, fn, count):
+        tot = fn(self._ctx, None, None)
+        if tot < 0:
+            self._check(int(tot), "lists")
+        off = np.zeros(count + 1, dtype=np.int64)
+        ids = np.zeros(max(int(tot), 1), dtype=np.int32)
+        r = fn(self._ctx, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+               ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        if r < 0:
+            self._check(int(r), "lists")
+        return [ids[off[i]:off[i + 1]] for i in range(count)]
+
+    def direct_lists(self) -> list:
+        """Direct-sum partners (input ids) of every particle, input order."""
+        return self._csr(self._lib.gsph_get_direct_lists, self.n)
+
+    def cell_lists(self) -> list:
+        """Multipole cells (depth-first ids) of every leaf, in cell_summary's leaf order."""
+        return self._csr(self._lib.gsph_get_cell_lists, int(self.stats()["nleaf"]))
+
     def direct_summary(self):
         cnt = np.zeros(self.n, dtype=np.int64)
         hsh = np.zeros(self.n, dtype=np.uint64)

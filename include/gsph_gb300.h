@@ -293,6 +293,14 @@ int64_t gsph_get_sph_neighbours(gsph_ctx* ctx, int64_t* offsets, int32_t* ids);
  * ids), and multipole cells per leaf cell as (count, hash of depth-first cell ids). */
 int32_t gsph_get_direct_summary(gsph_ctx* ctx, int64_t* counts, uint64_t* hashes);
 int32_t gsph_get_cell_summary(gsph_ctx* ctx, int32_t* leaf_cells, int64_t* counts, uint64_t* hashes);
+/* Full lists (tests at small N): with recording on, also keep up to max_direct direct-sum
+ * partners (input ids) per particle and up to max_cells multipole cells (depth-first ids)
+ * per leaf cell in the next force passes; 0, 0 stops.  The getters return CSR arrays —
+ * per particle in input order, per leaf in the leaf order of gsph_get_cell_summary — and
+ * with ids == NULL the total count. */
+int32_t gsph_set_list_recording(gsph_ctx* ctx, int32_t max_direct, int32_t max_cells);
+int64_t gsph_get_direct_lists(gsph_ctx* ctx, int64_t* offsets, int32_t* ids);
+int64_t gsph_get_cell_lists(gsph_ctx* ctx, int64_t* offsets, int32_t* cells);
 /* The KD-tree: per depth-first cell N, and leaf membership as input ids in slot order
  * (slot s holds input id order[s]; leaf cell c holds slots [first[c], first[c]+N[c])). */
 int32_t gsph_get_tree(gsph_ctx* ctx, int32_t* cell_n, int32_t* cell_first, int32_t* order,

@@ -188,3 +188,30 @@ def test_gpu_aos_records_roundtrip():
     assert np.array_equal(rec["dudt"], soa["dudt"])
     assert np.array_equal(rec["iorig"], np.arange(len(rec)))
     assert np.all(rec["alpha"] == 1.0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gravity_lists_as_full_sets(precision):
+    """Direct-sum partners per particle and multipole cells per leaf compared as full sets
+    with the oracle's lists (beside the count-and-hash summaries used at large N).  The
+    mixed form is compared with the oracle run on its own smoothing lengths."""
+    c = ics_mod.plummer_sphere(3000, seed=3001)
+    params = c["params"]
+    t = GradhSphTree(params, precision=precision)
+    t.set_particles(c)
+    t.set_recording(True, 1024)
+    t.set_list_recording(4096, 4096)
+    t.step()
+    got = t.results()
+    dl = t.direct_lists()
+    leaves, _, _ = t.cell_summary()
+    cl = t.cell_lists()
+    t.close()
+    given = None if precision == "fp64" else {k: got[k] for k in ("h", "rho", "invomega", "zeta", "pressure", "sound")}
+    r = oracle.run(c, params, lists=True, given=given)
+    assert same_lists(dl, r["grav_direct"]) == []
+    ref_cells = {int(l): np.sort(g) for l, g in zip(r["gcell_leaf"], r["gcell_lists"])}
+    assert len(ref_cells) == len(leaves)
+    for leaf, cells in zip(leaves, cl):
+        np.testing.assert_array_equal(np.sort(cells), ref_cells[int(leaf)])
+    assert sum(len(x) for x in dl) > 0 and sum(len(x) for x in cl) > 0
