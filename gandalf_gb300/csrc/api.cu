@@ -111,6 +111,7 @@ struct gsph_ctx {
   bool have_star_forces = false;
   // KDK integration with block timesteps (gsph_kdk_*)
   bool kdk = false;
+  bool keep_current = false;          // results live in the KDK state (input order), complete
   KdkParams kp{};
   KdkGlobal* kg = nullptr;
   double* kdk_buf = nullptr;          // r0 v0 a0 (9), u0 dudt0 dt dt_next tlast (5), keep (17): x cap
@@ -185,6 +186,7 @@ void kdk_free(gsph_ctx* c);
 KdkState make_kdk_state(gsph_ctx* c);
 KdkLeaf make_kdk_leaf(gsph_ctx* c);
 int ensure_kdk_buffers(gsph_ctx* c);
+const double* kdk_field_source(gsph_ctx* c, int leaf_field);
 
 void drop_graph(gsph_ctx* c) {
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
@@ -667,6 +669,7 @@ int do_build(gsph_ctx* c) {
   }
   c->have_tree = true;
   c->have_props = c->have_forces = false;
+  c->keep_current = false;
   return check_launch(c, "build tree");
 }
 
@@ -1250,6 +1253,15 @@ int32_t gsph_get_field_device(gsph_ctx* c, int32_t field, double* out) {
   if (fi < 0) return fail(c, GSPH_ERR_INVALID, "unknown field");
   if (!c->have_tree) return fail(c, GSPH_ERR_STATE, "no results yet");
   cudaSetDevice(c->device);
+  if (c->kdk && c->keep_current) {
+    // after KDK steps every particle's fields are in the integration state, input order
+    // (the leaf-order arrays hold only what the last passes solved)
+    const double* src = kdk_field_source(c, fi);
+    if (src) {
+      GSPH_CUDA(cudaMemcpyAsync(out, src, sizeof(double) * (size_t) c->n, cudaMemcpyDeviceToDevice, c->stream));
+      return GSPH_OK;
+    }
+  }
   k_scatter_field<<<grid1(c->n), 256, 0, c->stream>>>(c->f[fi], c->slot_of, c->n, out);
   return check_launch(c, "scatter field");
 }
@@ -1952,6 +1964,16 @@ int ensure_kdk_buffers(gsph_ctx* c) {
   return GSPH_OK;
 }
 
+// The input-order array of the KDK state that holds a leaf-order field (nullptr: none).
+const double* kdk_field_source(gsph_ctx* c, int leaf_field) {
+  const KdkState s = make_kdk_state(c);
+  if (leaf_field == kFH) return s.h;
+  if (leaf_field == kFU) return s.u;
+  for (int q = 0; q < kKeep; q++)
+    if (kKeepField[q] == leaf_field) return s.keep[q];
+  return nullptr;
+}
+
 KdkState make_kdk_state(gsph_ctx* c) {
   KdkState s{};
   const size_t k = (size_t) c->kdk_cap;
@@ -2223,6 +2245,7 @@ int32_t gsph_kdk_setup(gsph_ctx* c, const gsph_kdk_config* k) {
   if (rc) { c->kdk = false; return rc; }
   rc = kdk_read(c);
   if (rc) c->kdk = false;
+  c->keep_current = rc == GSPH_OK;
   return rc;
 }
 
@@ -2321,6 +2344,7 @@ int32_t gsph_kdk_steps(gsph_ctx* c, int32_t nsteps, int32_t use_graph) {
   c->last.ms_forces = ph[kPhForces];
   c->last.ms_total = ms;
   c->have_tree = c->have_props = c->have_forces = true;
+  c->keep_current = rc == GSPH_OK;
   return rc;
 }
 

@@ -81,15 +81,18 @@ __global__ void k_kdk_advance(KdkState s, KdkParams kp, KdkGlobal* g) {
 }
 
 // Persistent fields into leaf order after a build; active flags and levels per slot.
+// Only what the pass reads of a particle it does not solve: the neighbour fields (h, u and
+// the positions come with the tree build's own gather); the solved particles' fields are
+// all written by the pass.
 __global__ void k_kdk_gather(KdkState s, KdkLeaf l, KdkGlobal* g) {
   unsigned long long act = 0;
   for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
     const int i = l.id[slot];
 #pragma unroll
-    for (int q = 0; q < kKeep; q++) l.f[q][slot] = s.keep[q][i];
-    l.h[slot] = s.h[i];
-    l.u[slot] = s.u[i];
-    const unsigned char a = s.flags[i] & kFlagActive;
+    for (int q = 0; q < kKeepNeighbour; q++) l.f[q][slot] = s.keep[q][i];
+    const unsigned char f = s.flags[i];
+    const unsigned char a = f & kFlagActive;
+    if (a) s.flags[i] = f | kFlagTouched;
     l.active[slot] = a;
     l.level[slot] = s.level[i];
     l.lvn[slot] = 0;
@@ -109,6 +112,7 @@ __global__ void k_kdk_scatter(KdkState s, KdkLeaf l) {
     s.u[i] = l.u[slot];
     const int base = l.active[slot] ? 0 : s.levelneib[i];
     s.levelneib[i] = max(base, l.lvn[slot]);
+    s.flags[i] &= (unsigned char) ~kFlagTouched;
   }
 }
 
@@ -119,7 +123,9 @@ __global__ void k_kdk_refresh(KdkState s, KdkLeaf l, KdkGlobal* g) {
   unsigned long long act = 0;
   for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < l.n; slot += gridDim.x * blockDim.x) {
     const int i = l.id[slot];
-    const unsigned char a = s.flags[i] & kFlagActive;
+    const unsigned char f = s.flags[i];
+    const unsigned char a = f & kFlagActive;
+    if (a) s.flags[i] = f | kFlagTouched;
     l.active[slot] = a;
     l.level[slot] = s.level[i];
     l.lvn[slot] = 0;
@@ -139,13 +145,23 @@ __global__ void k_kdk_scatter_lvn(KdkState s, KdkLeaf l) {
 }
 
 // Solved fields back to input order, once per step after the last pass.
+// Particles solved in some pass of the step get all their fields back; the others only
+// the pressure and sound speed the thermal update recomputed (their other fields are
+// unchanged, and the leaf-order copies of those were not gathered).
 __global__ void k_kdk_scatter_fields(KdkState s, KdkLeaf l) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l.n; i += gridDim.x * blockDim.x) {
     const int slot = l.slot_of[i];
+    const unsigned char f = s.flags[i];
+    if (f & kFlagTouched) {
 #pragma unroll
-    for (int q = 0; q < kKeep; q++) s.keep[q][i] = l.f[q][slot];
-    s.h[i] = l.h[slot];
-    s.u[i] = l.u[slot];
+      for (int q = 0; q < kKeep; q++) s.keep[q][i] = l.f[q][slot];
+      s.h[i] = l.h[slot];
+      s.u[i] = l.u[slot];
+      s.flags[i] = f & (unsigned char) ~kFlagTouched;
+    } else {
+      s.keep[kKPressure][i] = l.f[kKPressure][slot];
+      s.keep[kKSound][i] = l.f[kKSound][slot];
+    }
   }
 }
 

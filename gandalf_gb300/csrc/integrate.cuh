@@ -50,6 +50,11 @@ struct KdkState {
   double* keep[kKeep];
 };
 constexpr unsigned char kFlagActive = 1, kFlagEndStep = 2;
+constexpr unsigned char kFlagTouched = 4;   // active in some pass of the current step
+// keep[] fields an inactive particle's neighbours read in a pass (rho invomega zeta hfactor
+// hrangesqd); pressure and sound are recomputed for every particle before each force pass
+constexpr int kKeepNeighbour = 5;
+constexpr int kKPressure = 5;
 
 // Leaf-order views the gather / scatter kernels fill.
 struct KdkLeaf {
