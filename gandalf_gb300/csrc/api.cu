@@ -693,7 +693,7 @@ int do_props(gsph_ctx* c) {
   GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
   mark(c, 2);
   launch_update_hmax(t, p, c->stream);
-  c->launches += 2;
+  c->launches += 1;
   if (c->kdk || c->bactive) {   // every particle's thermal properties before the force pass
     launch_kdk_thermal(p, make_params(c), c->stream);
     c->launches += 1;
@@ -1743,7 +1743,9 @@ int batch_prepare(gsph_batch* b) {
 // fork from and join the batch stream around each batched pass.
 int batch_body(gsph_batch* b) {
   const int ns = (int) b->ctx.size();
-  BatchQueue q{ns, b->d_sims, b->d_start, b->d_hstart, b->d_next};
+  bool any_record = false;
+  for (int i = 0; i < ns; i++) any_record = any_record || (b->ctx[i]->record && b->ctx[i]->rec_sph_cnt != nullptr);
+  BatchQueue q{ns, b->d_sims, b->d_start, b->d_hstart, b->d_next, any_record};
   cudaStream_t o = b->stream;
   b->launches = 0;
   cudaEventRecordWithFlags(b->ev[0], o, cudaEventRecordExternal);
@@ -1775,7 +1777,7 @@ int batch_body(gsph_batch* b) {
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count, 0, sizeof(int), c->stream));
     launch_update_hmax(t, p, c->stream);
     launch_mixed_prep_hydro(t, p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
-    c->launches += 4;
+    c->launches += 3;
     if (c->record && c->rec_sph_cnt) {
       GSPH_CUDA(cudaMemsetAsync(c->rec_sph_cnt, 0, sizeof(int) * (size_t) c->n, c->stream));
       GSPH_CUDA(cudaMemsetAsync(c->rec_dir_cnt, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));

@@ -31,6 +31,7 @@ struct BatchQueue {
   const int* leaf_start;   // nsim + 1 prefix sums of the simulations' leaf counts
   int* heavy_start;        // nsim + 1 prefix sums of the heavy-leaf counts (device-filled)
   int* next;               // work counters: normal density, heavy density, normal forces, heavy forces
+  bool record;             // some simulation records its pair lists: the recording kernels run
 };
 
 // Each returns the number of kernels it launched.  lpg: lanes per particle, chosen for the

@@ -1046,7 +1046,9 @@ struct ForceSmem {
 
 // SLICES > 1: the block's SLICES warps share the leaf, each keeping every SLICES-th
 // emitted list entry (sel = its slice), and their partial sums are added in slice order.
-template <int LPG, int SLICES>
+// REC: the list-recording build (counts, hashes and full lists of every pair kind); the
+// production build has none of that code in its pair loops.
+template <int LPG, int SLICES, bool REC>
 __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& p, const MixedParticles& mp,
                                                 const MixedCells& mc, const SphParams& prm, const DeviceCounters& cnt,
                                                 int leaf, int pfirst, int* stack, int* la, int* lb, int* lc, int capa,
@@ -1058,6 +1060,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   const int first = t.cell_first[c], ncell = t.cell_n[c];
   const int pidx = pfirst + g;
   const bool mine = pidx < ncell && is_active(p, first + pidx);
+  const bool rec = REC && cnt.record;
   if (SLICES == 1 && !__any_sync(kFull, mine)) return true;   // no active particle in this leaf
   const int slot = first + (pidx < ncell ? pidx : 0);
   int lvn_own = 0;
@@ -1152,7 +1155,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           acc[u][2] = __fadd_rn(acc[u][2], az); acc[u][3] = __fadd_rn(acc[u][3], pot);
           ncellp++;
         }
-        if (u0 == 0 && cnt.record) {
+        if (u0 == 0 && rec) {
           chash += mix64((unsigned long long) cc);
           ccount++;
           rec_cell_id(cnt, leaf, cc);
@@ -1187,7 +1190,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           acc[u][0] = __fmaf_rn(dx, inv3, acc[u][0]); acc[u][1] = __fmaf_rn(dy, inv3, acc[u][1]);
           acc[u][2] = __fmaf_rn(dz, inv3, acc[u][2]); acc[u][3] = __fmaf_rn(mj, inv, acc[u][3]);
           ndir_b++;
-          if (cnt.record) {
+          if (rec) {
             const int ts = first + pfirst + u0 + u;
             atomicAdd(&cnt.rec_dir_cnt[ts], 1ull);
             atomicAdd(&cnt.rec_dir_hash[ts], mix64((unsigned long long) p.id[j]));
@@ -1214,14 +1217,14 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
           lvn_pair(p, slot, j, lvn_own);
           nsph++;
-          if (cnt.record) {
+          if (rec) {
             const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
             if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
           }
         } else {
           direct_term_f(dx, dy, dz, pjh.w, A, prm.compensated != 0);
           ndir++;
-          if (cnt.record) {
+          if (rec) {
             dhash += mix64((unsigned long long) p.id[j]);
             rec_direct_id(cnt, slot, p.id[j]);
           }
@@ -1281,7 +1284,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   }
   if (gave_up) {
     // cells already consumed are recorded again by the kernel that takes the leaf over
-    if (cnt.rec_cell_ids && lane == 0) cnt.rec_cell_n[leaf] = 0;
+    if (rec && cnt.rec_cell_ids && lane == 0) cnt.rec_cell_n[leaf] = 0;
     return false;
   }
   consume_ab();
@@ -1299,12 +1302,12 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     atomicAdd(cnt.cell_pairs, a3); atomicAdd(cnt.exact_checks, a4);
   }
   unsigned long long cc = ccount, ch = chash;
-  if (cnt.record) {
+  if (rec) {
     for (int o = 16; o > 0; o >>= 1) { cc += __shfl_xor_sync(kFull, cc, o); ch += __shfl_xor_sync(kFull, ch, o); }
   }
   const double gpot0 = (double) (T.ph.w * T.hyd.x * (float) m4_wpot(0.0));   // (m / h) wpot(0)
   if (SLICES == 1) {
-    if (cnt.record && pfirst == 0 && lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
+    if (rec && pfirst == 0 && lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
     finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, gpot0, ndir, dhash, true);
     return true;
   }
@@ -1335,7 +1338,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         tdc += fs->dcnt[w][g];
         tdh += fs->dhash[w][g];
       }
-      if (cnt.record) { atomicAdd(&cnt.rec_dir_cnt[slot], tdc); atomicAdd(&cnt.rec_dir_hash[slot], tdh); }
+      if (rec) { atomicAdd(&cnt.rec_dir_cnt[slot], tdc); atomicAdd(&cnt.rec_dir_hash[slot], tdh); }
       const double rho = p.rho[slot];
       const double invrho = 1.0 / rho;
       const double divv = tot[8] * invrho;
@@ -1346,7 +1349,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
       p.agx[slot] = tot[3]; p.agy[slot] = tot[4]; p.agz[slot] = tot[5];
       p.gpot[slot] = gpot0 + tot[6];
     }
-    if (cnt.record && lane == 0) {
+    if (rec && lane == 0) {
       unsigned long long tc = 0, th = 0;
       for (int w = 0; w < SLICES; w++) { tc += fs->ccnt[w]; th += fs->chash[w]; }
       cnt.rec_cell_cnt[leaf] = tc;
@@ -1357,7 +1360,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   return true;
 }
 
-template <int LPG>
+template <int LPG, bool REC>
 __global__ void __launch_bounds__(kForceWarps * 32)
 k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
                    HeavyList heavy) {
@@ -1368,9 +1371,9 @@ k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphPar
   const int wib = threadIdx.x >> 5;
   const int leaf = blockIdx.x * kForceWarps + wib;
   if (leaf >= t.nleaf) return;
-  const bool ok = all_forces_leaf<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, 0, s_stack[wib], s_a[wib], s_b[wib],
-                                          s_c[wib], tuned_depth(prm.near_depth, 64, kFListA), kFListB,
-                                          tuned_depth(prm.cell_depth, 64, kFListC), true);
+  const bool ok = all_forces_leaf<LPG, 1, REC>(t, p, mp, mc, prm, cnt, leaf, 0, s_stack[wib], s_a[wib], s_b[wib],
+                                               s_c[wib], tuned_depth(prm.near_depth, 64, kFListA), kFListB,
+                                               tuned_depth(prm.cell_depth, 64, kFListC), true);
   if (!ok && (threadIdx.x & 31) == 0) {
     const int k = atomicAdd(heavy.count, 1);
     heavy.leaves[k] = leaf;
@@ -1379,7 +1382,7 @@ k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphPar
 
 // Heavy leaves: the block's 8 warps share each leaf, each taking an eighth of its
 // near-leaf, direct-leaf and cell lists for all of its particles.
-template <int LPG>
+template <int LPG, bool REC>
 __global__ void __launch_bounds__(256)
 k_all_forces_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
                         HeavyList heavy) {
@@ -1390,7 +1393,7 @@ k_all_forces_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, S
   ForceSmem* fs = reinterpret_cast<ForceSmem*>(s_dyn + 8 * per);
   const int nh = *heavy.count;
   for (int k = blockIdx.x; k < nh; k += gridDim.x) {
-    all_forces_leaf<LPG, 8>(t, p, mp, mc, prm, cnt, heavy.leaves[k], 0, base, base + kFStack, base + kFStack + kWListA,
+    all_forces_leaf<LPG, 8, REC>(t, p, mp, mc, prm, cnt, heavy.leaves[k], 0, base, base + kFStack, base + kFStack + kWListA,
                             base + kFStack + kWListA + kWListB, kWListA, kWListB, kWListC, false, wib, fs);
   }
 }
@@ -1593,7 +1596,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_batch_hydro(BatchQueue q) 
   }
 }
 
-template <int LPG>
+template <int LPG, bool REC>
 __global__ void __launch_bounds__(kForceWarps * 32) k_batch_forces(BatchQueue q) {
   __shared__ int s_stack[kForceWarps][kFStack];
   __shared__ int s_a[kForceWarps][kFListA];
@@ -1607,7 +1610,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_batch_forces(BatchQueue q)
     const int s = find_sim(q.leaf_start, q.nsim, item);
     const SimDesc& d = q.sims[s];
     const int leaf = item - q.leaf_start[s];
-    const bool ok = all_forces_leaf<LPG, 1>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, leaf, 0, s_stack[wib], s_a[wib],
+    const bool ok = all_forces_leaf<LPG, 1, REC>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, leaf, 0, s_stack[wib], s_a[wib],
                                             s_b[wib], s_c[wib], tuned_depth(d.prm.near_depth, 64, kFListA), kFListB,
                                             tuned_depth(d.prm.cell_depth, 64, kFListC), true);
     if (!ok && (threadIdx.x & 31) == 0) {
@@ -1617,7 +1620,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_batch_forces(BatchQueue q)
   }
 }
 
-template <int LPG>
+template <int LPG, bool REC>
 __global__ void __launch_bounds__(256) k_batch_forces_wide(BatchQueue q) {
   extern __shared__ int s_dyn[];
   __shared__ int s_item;
@@ -1631,7 +1634,7 @@ __global__ void __launch_bounds__(256) k_batch_forces_wide(BatchQueue q) {
     if (item >= total) break;
     const int s = find_sim(q.heavy_start, q.nsim, item);
     const SimDesc& d = q.sims[s];
-    all_forces_leaf<LPG, 8>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, d.heavy.leaves[item - q.heavy_start[s]], 0, base,
+    all_forces_leaf<LPG, 8, REC>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, d.heavy.leaves[item - q.heavy_start[s]], 0, base,
                             base + kFStack, base + kFStack + kWListA, base + kFStack + kWListA + kWListB, kWListA,
                             kWListB, kWListC, false, wib, fs);
   }
@@ -1663,6 +1666,30 @@ void launch_mixed_prep_hydro(const Tree& t, const Particles& p, const MixedParti
     default: KERNEL<1><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;                   \
   }
 
+// Kernels with a recording variant: REC is a compile-time constant at each call.
+#define GSPH_MIXED_LPG_REC(KERNEL, REC, LPG, GRID, BLOCK, SMEM, ...)                      \
+  switch (LPG) {                                                                         \
+    case 32: KERNEL<32, REC><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;             \
+    case 16: KERNEL<16, REC><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;             \
+    case 8: KERNEL<8, REC><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;               \
+    case 4: KERNEL<4, REC><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;               \
+    case 2: KERNEL<2, REC><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;               \
+    default: KERNEL<1, REC><<<GRID, BLOCK, SMEM, st>>>(__VA_ARGS__); break;              \
+  }
+
+template <bool REC>
+void set_wide_smem(bool batch, size_t smem) {
+  if (batch) {
+    for (auto f : {k_batch_forces_wide<1, REC>, k_batch_forces_wide<2, REC>, k_batch_forces_wide<4, REC>,
+                   k_batch_forces_wide<8, REC>, k_batch_forces_wide<16, REC>, k_batch_forces_wide<32, REC>})
+      cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  } else {
+    for (auto f : {k_all_forces_mixed_wide<1, REC>, k_all_forces_mixed_wide<2, REC>, k_all_forces_mixed_wide<4, REC>,
+                   k_all_forces_mixed_wide<8, REC>, k_all_forces_mixed_wide<16, REC>, k_all_forces_mixed_wide<32, REC>})
+      cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  }
+}
+
 int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
                          const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
                          int lanes_per_particle, int max_leaf, cudaStream_t st) {
@@ -1681,13 +1708,21 @@ int launch_all_forces_mixed(const Tree& t, const Particles& p, const MixedPartic
                             int lanes_per_particle, int max_leaf, cudaStream_t st) {
   cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
   const int blocks = (t.nleaf + kForceWarps - 1) / kForceWarps;
-  GSPH_MIXED_LPG(k_all_forces_mixed, lanes_per_particle, blocks, kForceWarps * 32, 0, t, p, mp, mc, prm, cnt, heavy)
   const size_t smem = sizeof(int) * 8 * (kFStack + kWListA + kWListB + kWListC) + sizeof(ForceSmem);
-  for (auto f : {k_all_forces_mixed_wide<1>, k_all_forces_mixed_wide<2>, k_all_forces_mixed_wide<4>,
-                 k_all_forces_mixed_wide<8>, k_all_forces_mixed_wide<16>, k_all_forces_mixed_wide<32>})
-    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
   (void) max_leaf;
-  GSPH_MIXED_LPG(k_all_forces_mixed_wide, lanes_per_particle, 152 * 2, 256, smem, t, p, mp, mc, prm, cnt, heavy)
+  if (cnt.record) {
+    GSPH_MIXED_LPG_REC(k_all_forces_mixed, true, lanes_per_particle, blocks, kForceWarps * 32, 0, t, p, mp, mc, prm,
+                       cnt, heavy)
+    set_wide_smem<true>(false, smem);
+    GSPH_MIXED_LPG_REC(k_all_forces_mixed_wide, true, lanes_per_particle, 152 * 2, 256, smem, t, p, mp, mc, prm, cnt,
+                       heavy)
+  } else {
+    GSPH_MIXED_LPG_REC(k_all_forces_mixed, false, lanes_per_particle, blocks, kForceWarps * 32, 0, t, p, mp, mc, prm,
+                       cnt, heavy)
+    set_wide_smem<false>(false, smem);
+    GSPH_MIXED_LPG_REC(k_all_forces_mixed_wide, false, lanes_per_particle, 152 * 2, 256, smem, t, p, mp, mc, prm, cnt,
+                       heavy)
+  }
   return 2;
 }
 
@@ -1715,13 +1750,18 @@ int launch_batch_forces(const BatchQueue& q, bool gravity, int lpg, cudaStream_t
     GSPH_MIXED_LPG(k_batch_hydro, lpg, 152 * 4, kForceWarps * 32, 0, q)
     return 1;
   }
-  GSPH_MIXED_LPG(k_batch_forces, lpg, 152 * 4, kForceWarps * 32, 0, q)
-  k_batch_heavy_prefix<<<1, 32, 0, st>>>(q);
   const size_t smem = sizeof(int) * 8 * (kFStack + kWListA + kWListB + kWListC) + sizeof(ForceSmem);
-  for (auto f : {k_batch_forces_wide<1>, k_batch_forces_wide<2>, k_batch_forces_wide<4>,
-                 k_batch_forces_wide<8>, k_batch_forces_wide<16>, k_batch_forces_wide<32>})
-    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-  GSPH_MIXED_LPG(k_batch_forces_wide, lpg, 152 * 2, 256, smem, q)
+  if (q.record) {
+    GSPH_MIXED_LPG_REC(k_batch_forces, true, lpg, 152 * 4, kForceWarps * 32, 0, q)
+    k_batch_heavy_prefix<<<1, 32, 0, st>>>(q);
+    set_wide_smem<true>(true, smem);
+    GSPH_MIXED_LPG_REC(k_batch_forces_wide, true, lpg, 152 * 2, 256, smem, q)
+  } else {
+    GSPH_MIXED_LPG_REC(k_batch_forces, false, lpg, 152 * 4, kForceWarps * 32, 0, q)
+    k_batch_heavy_prefix<<<1, 32, 0, st>>>(q);
+    set_wide_smem<false>(true, smem);
+    GSPH_MIXED_LPG_REC(k_batch_forces_wide, false, lpg, 152 * 2, 256, smem, q)
+  }
   return 3;
 }
 

@@ -505,6 +505,57 @@ __device__ void finish_geometry(int n, const double* bmin, const double* bmax, d
   g.hmax = hmax;
 }
 
+__device__ void stock_leaf(const Tree& t, const Particles& p, int c, double theta2) {
+  const int first = t.cell_first[c], n = t.cell_n[c];
+  double m = 0.0, r[3] = {0.0, 0.0, 0.0}, hmax = 0.0;
+  double bmin[3] = {kBig, kBig, kBig}, bmax[3] = {-kBig, -kBig, -kBig};
+  double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+  for (int j = 0; j < n; j++) {
+    const int s = first + j;
+    const double xs[3] = {p.x[s], p.y[s], p.z[s]};
+    const double hh = p.h[s], mm = p.m[s];
+    hmax = fmax(hmax, hh);
+    m += mm;
+    const double h2 = __dmul_rn(kKernRange, hh);
+    for (int k = 0; k < 3; k++) {
+      r[k] = fma(mm, xs[k], r[k]);
+      bmin[k] = fmin(bmin[k], xs[k]);
+      bmax[k] = fmax(bmax[k], xs[k]);
+      hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
+      hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
+    }
+  }
+  if (m > 0.0) {
+    const double im = 1.0 / m;   // one division for the three components
+    for (int k = 0; k < 3; k++) r[k] *= im;
+  }
+  CellGeom g;
+  finish_geometry(n, bmin, bmax, hmax, theta2, g);
+  double q[5] = {0, 0, 0, 0, 0};
+  for (int j = 0; j < n; j++) {
+    const int s = first + j;
+    const double mm = p.m[s];
+    const double dx = p.x[s] - r[0], dy = p.y[s] - r[1], dz = p.z[s] - r[2];
+    const double drsqd = dx * dx + dy * dy + dz * dz;
+    q[0] += mm * (3.0 * dx * dx - drsqd);
+    q[1] += mm * 3.0 * dx * dy;
+    q[2] += mm * (3.0 * dy * dy - drsqd);
+    q[3] += mm * 3.0 * dz * dx;
+    q[4] += mm * 3.0 * dz * dy;
+  }
+  t.geom[c] = g;
+  CellBox b, hb;
+  for (int k = 0; k < 3; k++) { b.bbmin[k] = bmin[k]; b.bbmax[k] = bmax[k]; hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
+  t.bb[c] = b;
+  t.hbox[c] = hb;
+  CellMoment mo;
+  for (int k = 0; k < 3; k++) mo.r[k] = r[k];
+  mo.m = m;
+  for (int k = 0; k < 5; k++) mo.q[k] = q[k];
+  mo.pad = 0.0;
+  t.mom[c] = mo;
+}
+
 __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
 
 __device__ void stock_parent(const Tree& t, int c, int level, double theta2) {
@@ -570,31 +621,11 @@ __device__ void stock_parent(const Tree& t, int c, int level, double theta2) {
 }
 
 // Bottom-up climb: the second child to finish stocks the parent.
-// Leaf stocking, 8 lanes per leaf (four leaves a warp): the lanes take the leaf's particles
-// in turn with coalesced loads, and the sums, minima and maxima meet by shuffles within
-// the 8 lanes.  The sums' order therefore differs from the reference's sequential loop
-// (rounding only); minima, maxima and with them every box, rmax and cdistsqd are exact.
-// The parents follow in k_stock_climb, one climbing thread per leaf (a climb by one lane of
-// eight would leave most of each warp idle through the serial parent updates).
-constexpr int kStockLanes = 8;
-
-__device__ __forceinline__ double red_sum8(double v) {
-#pragma unroll
-  for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ double red_min8(double v) {
-#pragma unroll
-  for (int o = 4; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-__device__ __forceinline__ double red_max8(double v) {
-#pragma unroll
-  for (int o = 4; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-__device__ void climb_stock(const Tree& t, int c, double theta2) {
+__global__ void k_stock(Tree t, Particles p, double theta2) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= t.nleaf) return;
+  int c = t.leaf_cell[s];
+  stock_leaf(t, p, c, theta2);
   int level = t.ltot;
   while (level > 0) {
     const int parent = t.cell_parent[c];
@@ -608,113 +639,31 @@ __device__ void climb_stock(const Tree& t, int c, double theta2) {
   }
 }
 
-__global__ void k_stock(Tree t, Particles p, double theta2) {
-  const int sub = threadIdx.x & (kStockLanes - 1);
-  const int leaf = (blockIdx.x * blockDim.x + threadIdx.x) / kStockLanes;
-  const bool has = leaf < t.nleaf;   // whole 8-lane groups agree
-  const int c = has ? t.leaf_cell[leaf] : 0;
-  const int first = has ? t.cell_first[c] : 0, n = has ? t.cell_n[c] : 0;
-  double m = 0.0, r[3] = {0.0, 0.0, 0.0}, hmax = 0.0;
-  double bmin[3] = {kBig, kBig, kBig}, bmax[3] = {-kBig, -kBig, -kBig};
-  double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
-  for (int j = sub; j < n; j += kStockLanes) {
-    const int q = first + j;
-    const double xs[3] = {p.x[q], p.y[q], p.z[q]};
-    const double hh = p.h[q], mm = p.m[q];
-    hmax = fmax(hmax, hh);
-    m += mm;
-    const double h2 = __dmul_rn(kKernRange, hh);
-    for (int k = 0; k < 3; k++) {
-      r[k] = fma(mm, xs[k], r[k]);
-      bmin[k] = fmin(bmin[k], xs[k]);
-      bmax[k] = fmax(bmax[k], xs[k]);
-      hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
-      hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
-    }
-  }
-  m = red_sum8(m);
-  hmax = red_max8(hmax);
-  for (int k = 0; k < 3; k++) {
-    r[k] = red_sum8(r[k]);
-    bmin[k] = red_min8(bmin[k]); bmax[k] = red_max8(bmax[k]);
-    hbmin[k] = red_min8(hbmin[k]); hbmax[k] = red_max8(hbmax[k]);
-  }
-  if (m > 0.0) {
-    const double im = 1.0 / m;   // one division for the three components
-    for (int k = 0; k < 3; k++) r[k] *= im;
-  }
-  double q[5] = {0, 0, 0, 0, 0};
-  for (int j = sub; j < n; j += kStockLanes) {
-    const int s = first + j;
-    const double mm = p.m[s];
-    const double dx = p.x[s] - r[0], dy = p.y[s] - r[1], dz = p.z[s] - r[2];
-    const double drsqd = dx * dx + dy * dy + dz * dz;
-    q[0] += mm * (3.0 * dx * dx - drsqd);
-    q[1] += mm * 3.0 * dx * dy;
-    q[2] += mm * (3.0 * dy * dy - drsqd);
-    q[3] += mm * 3.0 * dz * dx;
-    q[4] += mm * 3.0 * dz * dy;
-  }
-  for (int k = 0; k < 5; k++) q[k] = red_sum8(q[k]);
-  if (!has || sub != 0) return;
-  CellGeom g;
-  finish_geometry(n, bmin, bmax, hmax, theta2, g);
-  t.geom[c] = g;
-  CellBox b, hb;
-  for (int k = 0; k < 3; k++) { b.bbmin[k] = bmin[k]; b.bbmax[k] = bmax[k]; hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
-  t.bb[c] = b;
-  t.hbox[c] = hb;
-  CellMoment mo;
-  for (int k = 0; k < 3; k++) mo.r[k] = r[k];
-  mo.m = m;
-  for (int k = 0; k < 5; k++) mo.q[k] = q[k];
-  mo.pad = 0.0;
-  t.mom[c] = mo;
-}
-
-// The parents, bottom-up: one thread per leaf climbs while it is the second child to
-// arrive at a parent (arrival counters), stocking that parent from its two children.
-__global__ void k_stock_climb(Tree t, double theta2) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= t.nleaf) return;
-  climb_stock(t, t.leaf_cell[s], theta2);
-}
-
 // KDTree::UpdateHmaxValues: hmax and hbox from the solved h; cdistsqd keeps its value.
-// 8 lanes per leaf as in k_stock (minima and maxima only: exact in any order).
 __global__ void k_update_hmax(Tree t, Particles p) {
-  const int sub = threadIdx.x & (kStockLanes - 1);
-  const int leaf = (blockIdx.x * blockDim.x + threadIdx.x) / kStockLanes;
-  const bool has = leaf < t.nleaf;
-  int c = has ? t.leaf_cell[leaf] : 0;
-  const int first = has ? t.cell_first[c] : 0, n = has ? t.cell_n[c] : 0;
-  double hmax = 0.0;
-  double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
-  for (int j = sub; j < n; j += kStockLanes) {
-    const int q = first + j;
-    const double xs[3] = {p.x[q], p.y[q], p.z[q]};
-    const double hh = p.h[q];
-    hmax = fmax(hmax, hh);
-    const double h2 = __dmul_rn(kKernRange, hh);
-    for (int k = 0; k < 3; k++) {
-      hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
-      hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
-    }
-  }
-  hmax = red_max8(hmax);
-  for (int k = 0; k < 3; k++) { hbmin[k] = red_min8(hbmin[k]); hbmax[k] = red_max8(hbmax[k]); }
-  if (!has || sub != 0) return;
-  t.geom[c].hmax = hmax;
-  CellBox hb;
-  for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
-  t.hbox[c] = hb;
-}
-
-// The parents' hmax and hbox, bottom-up as in k_stock_climb.
-__global__ void k_update_hmax_climb(Tree t) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= t.nleaf) return;
   int c = t.leaf_cell[s];
+  {
+    const int first = t.cell_first[c], n = t.cell_n[c];
+    double hmax = 0.0;
+    double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+    for (int j = 0; j < n; j++) {
+      const int q = first + j;
+      const double xs[3] = {p.x[q], p.y[q], p.z[q]};
+      const double hh = p.h[q];
+      hmax = fmax(hmax, hh);
+      const double h2 = __dmul_rn(kKernRange, hh);
+      for (int k = 0; k < 3; k++) {
+        hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
+        hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
+      }
+    }
+    t.geom[c].hmax = hmax;
+    CellBox hb;
+    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
+    t.hbox[c] = hb;
+  }
   int level = t.ltot;
   while (level > 0) {
     const int parent = t.cell_parent[c];
@@ -725,21 +674,21 @@ __global__ void k_update_hmax_climb(Tree t) {
     level--;
     c = parent;
     const int c1 = c + 1, c2 = c2_of(c, level, t.ltot);
-    double hm = 0.0;
-    double hl[3] = {kBig, kBig, kBig}, hu[3] = {-kBig, -kBig, -kBig};
+    double hmax = 0.0;
+    double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
     const int ch[2] = {c1, c2};
-    for (int qq = 0; qq < 2; qq++) {
-      if (t.cell_n[ch[qq]] <= 0) continue;
-      const double* hbp = reinterpret_cast<const double*>(&t.hbox[ch[qq]]);
-      hm = fmax(hm, ldcg(&t.geom[ch[qq]].hmax));
+    for (int q = 0; q < 2; q++) {
+      if (t.cell_n[ch[q]] <= 0) continue;
+      const double* hbp = reinterpret_cast<const double*>(&t.hbox[ch[q]]);
+      hmax = fmax(hmax, ldcg(&t.geom[ch[q]].hmax));
       for (int k = 0; k < 3; k++) {
-        hl[k] = fmin(ldcg(hbp + k), hl[k]);
-        hu[k] = fmax(ldcg(hbp + 3 + k), hu[k]);
+        hbmin[k] = fmin(ldcg(hbp + k), hbmin[k]);
+        hbmax[k] = fmax(ldcg(hbp + 3 + k), hbmax[k]);
       }
     }
-    t.geom[c].hmax = hm;
+    t.geom[c].hmax = hmax;
     CellBox hb;
-    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hl[k]; hb.bbmax[k] = hu[k]; }
+    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
     t.hbox[c] = hb;
   }
 }
@@ -819,15 +768,13 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
   }
   k_gather_leaf_order<<<grid_for(n, 256), 256, 0, st>>>(n, cur.l[0], a.in, a.p, a.id_out, a.slot_of);
   cudaMemsetAsync(a.tree.climb, 0, sizeof(unsigned) * (size_t) a.tree.ncell, st);
-  k_stock<<<(a.tree.nleaf * kStockLanes + 127) / 128, 128, 0, st>>>(a.tree, a.p, a.thetamaxsqd);
-  k_stock_climb<<<(a.tree.nleaf + 127) / 128, 128, 0, st>>>(a.tree, a.thetamaxsqd);
-  return launches + 3;
+  k_stock<<<(a.tree.nleaf + 127) / 128, 128, 0, st>>>(a.tree, a.p, a.thetamaxsqd);
+  return launches + 2;
 }
 
 void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st) {
   cudaMemsetAsync(t.climb, 0, sizeof(unsigned) * (size_t) t.ncell, st);
-  k_update_hmax<<<(t.nleaf * kStockLanes + 127) / 128, 128, 0, st>>>(t, p);
-  k_update_hmax_climb<<<(t.nleaf + 127) / 128, 128, 0, st>>>(t);
+  k_update_hmax<<<(t.nleaf + 127) / 128, 128, 0, st>>>(t, p);
 }
 
 }  // namespace gsph
