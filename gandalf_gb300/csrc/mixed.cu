@@ -111,6 +111,15 @@ __device__ __forceinline__ float gsum_f(float v) {
   for (int o = 1; o < LPG; o <<= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));
   return v;
 }
+// The same sums over groups of a run-time width (a power of two, uniform over the warp).
+__device__ __forceinline__ double gsum_d(double v, int lpg) {
+  for (int o = 1; o < lpg; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+__device__ __forceinline__ float gsum_f(float v, int lpg) {
+  for (int o = 1; o < lpg; o <<= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
 
 __device__ __forceinline__ float fsqrt_pos(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
 
@@ -992,28 +1001,29 @@ __device__ __forceinline__ void load_leaf_geo(const Tree& t, const MixedCells& m
   G.hrangemax = __dmul_rn(kKernRange, g.hmax);
 }
 
-template <int LPG>
+// lpg: lanes per particle (a power of two, uniform over the warp); the particle's lanes
+// are consecutive and the one with sl == 0 writes.
 __device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Particles& p, const DeviceCounters& cnt,
-                                                  bool mine, int sl, int slot, const AccF& A, double gpot0,
+                                                  int lpg, bool mine, int sl, int slot, const AccF& A, double gpot0,
                                                   unsigned long long ndir, unsigned long long dhash, bool grav) {
   // the lanes' partial sums added in float (each holds a few hundred float terms already),
   // the per-particle arithmetic after them in float too; results stored as fp64
   float ah[3], ag[3], gp, du, dv;
   double agd[3], gpd;
-  for (int k = 0; k < 3; k++) ah[k] = gsum_f<LPG>(A.ah[k]);
+  for (int k = 0; k < 3; k++) ah[k] = gsum_f(A.ah[k], lpg);
   if (prm.compensated) {   // the lanes' compensated partials combined in fp64
-    for (int k = 0; k < 3; k++) agd[k] = gsum_d<LPG>((double) A.ag[k] - (double) A.cg[k]);
-    gpd = gsum_d<LPG>((double) A.gpot - (double) A.cg[3]);
+    for (int k = 0; k < 3; k++) agd[k] = gsum_d((double) A.ag[k] - (double) A.cg[k], lpg);
+    gpd = gsum_d((double) A.gpot - (double) A.cg[3], lpg);
   } else {
-    for (int k = 0; k < 3; k++) { ag[k] = gsum_f<LPG>(A.ag[k]); agd[k] = ag[k]; }
-    gp = gsum_f<LPG>(A.gpot);
+    for (int k = 0; k < 3; k++) { ag[k] = gsum_f(A.ag[k], lpg); agd[k] = ag[k]; }
+    gp = gsum_f(A.gpot, lpg);
     gpd = gp;
   }
-  du = gsum_f<LPG>(A.dudt);
-  dv = gsum_f<LPG>(A.divv);
+  du = gsum_f(A.dudt, lpg);
+  dv = gsum_f(A.divv, lpg);
   if (cnt.record) {
     unsigned long long dc = ndir, dh = dhash;
-    for (int o = 1; o < LPG; o <<= 1) { dc += __shfl_xor_sync(kFull, dc, o); dh += __shfl_xor_sync(kFull, dh, o); }
+    for (int o = 1; o < lpg; o <<= 1) { dc += __shfl_xor_sync(kFull, dc, o); dh += __shfl_xor_sync(kFull, dh, o); }
     if (mine && sl == 0) { atomicAdd(&cnt.rec_dir_cnt[slot], dc); atomicAdd(&cnt.rec_dir_hash[slot], dh); }
   }
   if (!(mine && sl == 0)) return;
@@ -1055,13 +1065,33 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
                                                 int capb, int capc, bool give_up, int sel = 0,
                                                 ForceSmem* fs = nullptr) {
   const int lane = threadIdx.x & 31;
-  const int g = lane / LPG, sl = lane % LPG;
+  constexpr int GT = 32 / LPG;   // particles of the leaf (from pfirst) this warp holds
   const int c = t.leaf_cell[leaf];
   const int first = t.cell_first[c], ncell = t.cell_n[c];
-  const int pidx = pfirst + g;
-  const bool mine = pidx < ncell && is_active(p, first + pidx);
   const bool rec = REC && cnt.record;
-  if (SLICES == 1 && !__any_sync(kFull, mine)) return true;   // no active particle in this leaf
+  // Lanes to targets.  SLICES == 1: the warp works for the leaf's active particles only,
+  // nact of them getting 32 / P consecutive lanes each (P the power of two at or above
+  // nact), so that under block timesteps no lane waits on an inactive particle; with every
+  // particle active this is LPG lanes per particle in leaf order.  SLICES > 1: LPG lanes
+  // per particle of the leaf, active or not (the slices' sums are combined per particle).
+  int lpg = LPG, g = lane / LPG, ntg = GT, tk = g;
+  bool mine;
+  if (SLICES == 1) {
+    const unsigned amask =
+        __ballot_sync(kFull, lane < GT && pfirst + lane < ncell && is_active(p, first + pfirst + lane));
+    if (amask == 0u) return true;   // no active particle in this leaf
+    ntg = __popc(amask);
+    int pw = 1;
+    while (pw < ntg) pw <<= 1;
+    lpg = 32 / pw;
+    g = lane / lpg;
+    mine = g < ntg;
+    tk = mine ? nth_bit(amask, g) : 0;
+  } else {
+    mine = pfirst + g < ncell && is_active(p, first + pfirst + g);
+  }
+  const int sl = lane % lpg;
+  const int pidx = pfirst + tk;
   const int slot = first + (pidx < ncell ? pidx : 0);
   int lvn_own = 0;
   TargetF T;
@@ -1078,32 +1108,33 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   // target particle of the warp: positions relative to the leaf centre (hi + lo pairs,
   // accurate to a few ulps of the separation), 8 targets per round held in registers, the
   // per-target sums reduced over the warp afterwards and added to the target's first lane.
-  constexpr int GT = 32 / LPG;
   const float4 lc_hi = mc.geo_hi[c], lc_lo = mc.geo_lo[c];
   auto rel = [&](float4 h, float4 l, float& x, float& y, float& z) {
     x = (h.x - lc_hi.x) + (l.x - lc_lo.x);
     y = (h.y - lc_hi.y) + (l.y - lc_lo.y);
     z = (h.z - lc_hi.z) + (l.z - lc_lo.z);
   };
-  // the warp's targets, broadcast from shared memory: leaf-relative position, w = 1 when active
+  // the warp's targets, broadcast from shared memory: leaf-relative position and, in w,
+  // 1 + the particle's index in the leaf when active, 0 when not; ntg entries (SLICES == 1:
+  // the active particles only, in leaf order)
   constexpr int kTW = SLICES == 1 ? kForceWarps : 8;   // warps per block
   __shared__ float4 s_tgt[kTW][GT];
   float4* tgt = s_tgt[(threadIdx.x >> 5) % kTW];
   {
     float x, y, z;
     rel(T.ph, T.pl, x, y, z);
-    if (sl == 0) tgt[g] = make_float4(x, y, z, mine ? 1.0f : 0.0f);
+    if (sl == 0 && g < ntg) tgt[g] = make_float4(x, y, z, mine ? (float) (1 + tk) : 0.0f);
     __syncwarp();
   }
   auto add_to_targets = [&](float (&acc)[8][4], int u0) {
 #pragma unroll
     for (int u = 0; u < 8; u++) {
-      if (u0 + u >= GT) break;
+      if (u0 + u >= ntg) break;
       if (tgt[u0 + u].w == 0.0f) continue;   // inactive target: nothing was summed (warp-uniform)
 #pragma unroll
       for (int k = 0; k < 4; k++)
         for (int o = 16; o > 0; o >>= 1) acc[u][k] = __fadd_rn(acc[u][k], __shfl_xor_sync(kFull, acc[u][k], o));
-      if (lane == (u0 + u) * LPG) {
+      if (lane == (u0 + u) * lpg) {
         if (prm.compensated) {
           kahan_add(A.ag[0], A.cg[0], acc[u][0]); kahan_add(A.ag[1], A.cg[1], acc[u][1]);
           kahan_add(A.ag[2], A.cg[2], acc[u][2]); kahan_add(A.gpot, A.cg[3], acc[u][3]);
@@ -1117,6 +1148,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   auto consume_c = [&]() {
 #pragma unroll
     for (int u0 = 0; u0 < GT; u0 += 8) {
+      if (u0 >= ntg) break;
       float acc[8][4] = {};
       for (int e = lane; e < L.nc; e += 32) {
         const int cc = L.c[e];
@@ -1127,7 +1159,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         const float q4 = cl.w;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-          if (u0 + u >= GT) continue;
+          if (u0 + u >= ntg) break;
           const float4 tu = tgt[u0 + u];
           if (tu.w == 0.0f) continue;
           // explicit roundings: the same sums in every kernel this leaf code is built into
@@ -1167,6 +1199,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   auto consume_b = [&]() {
 #pragma unroll
     for (int u0 = 0; u0 < GT; u0 += 8) {
+      if (u0 >= ntg) break;
       float acc[8][4] = {};
       for (int e0 = 0; e0 < L.nb; e0 += LPG) {
         const int e = e0 + lane / GT, q = lane % GT;
@@ -1180,7 +1213,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         const float mj = pjh.w;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-          if (u0 + u >= GT) continue;
+          if (u0 + u >= ntg) break;
           const float4 tu = tgt[u0 + u];
           if (tu.w == 0.0f) continue;
           const float dx = __fsub_rn(sx, tu.x), dy = __fsub_rn(sy, tu.y), dz = __fsub_rn(sz, tu.z);
@@ -1191,7 +1224,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           acc[u][2] = __fmaf_rn(dz, inv3, acc[u][2]); acc[u][3] = __fmaf_rn(mj, inv, acc[u][3]);
           ndir_b++;
           if (rec) {
-            const int ts = first + pfirst + u0 + u;
+            const int ts = first + pfirst + (int) tu.w - 1;
             atomicAdd(&cnt.rec_dir_cnt[ts], 1ull);
             atomicAdd(&cnt.rec_dir_hash[ts], mix64((unsigned long long) p.id[j]));
             rec_direct_id(cnt, ts, p.id[j]);
@@ -1201,33 +1234,34 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
       add_to_targets(acc, u0);
     }
   };
+  // near leaves: the particle's lpg lanes take the (entry, particle) pairs of the list in
+  // turn (for lpg <= GT, particle q of every entry goes to lane q mod lpg)
   auto consume_ab = [&]() {
     if (!mine) return;
-    for (int e = 0; e < L.na; e++) {
-      const int node = L.a[e];
-      const int f = t.cell_first[node], nn = t.cell_n[node];
-      for (int q = sl; q < nn; q += LPG) {
-        const int j = f + q;
-        const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
-        const float dx = (pjh.x - T.ph.x) + (pjl.x - T.pl.x);
-        const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
-        const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        if (sph_member(p, T, j, d2, pjl.w, prm, exact)) {
-          hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
-          lvn_pair(p, slot, j, lvn_own);
-          nsph++;
-          if (rec) {
-            const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
-            if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
-          }
-        } else {
-          direct_term_f(dx, dy, dz, pjh.w, A, prm.compensated != 0);
-          ndir++;
-          if (rec) {
-            dhash += mix64((unsigned long long) p.id[j]);
-            rec_direct_id(cnt, slot, p.id[j]);
-          }
+    const int ntot = L.na * GT;
+    for (int idx = sl; idx < ntot; idx += lpg) {
+      const int node = L.a[idx / GT], q = idx % GT;
+      if (q >= t.cell_n[node]) continue;
+      const int j = t.cell_first[node] + q;
+      const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+      const float dx = (pjh.x - T.ph.x) + (pjl.x - T.pl.x);
+      const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
+      const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (sph_member(p, T, j, d2, pjl.w, prm, exact)) {
+        hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
+        lvn_pair(p, slot, j, lvn_own);
+        nsph++;
+        if (rec) {
+          const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
+          if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
+        }
+      } else {
+        direct_term_f(dx, dy, dz, pjh.w, A, prm.compensated != 0);
+        ndir++;
+        if (rec) {
+          dhash += mix64((unsigned long long) p.id[j]);
+          rec_direct_id(cnt, slot, p.id[j]);
         }
       }
     }
@@ -1308,7 +1342,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   const double gpot0 = (double) (T.ph.w * T.hyd.x * (float) m4_wpot(0.0));   // (m / h) wpot(0)
   if (SLICES == 1) {
     if (rec && pfirst == 0 && lane == 0) { cnt.rec_cell_cnt[leaf] = cc; cnt.rec_cell_hash[leaf] = ch; }
-    finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, gpot0, ndir, dhash, true);
+    finish_particle_f(prm, p, cnt, lpg, mine, sl, slot, A, gpot0, ndir, dhash, true);
     return true;
   }
   // sliced: reduce each particle inside the warp, then across slices in slice order
@@ -1491,7 +1525,7 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
   for (int o = 16; o > 0; o >>= 1) { a1 += __shfl_xor_sync(kFull, a1, o); a4 += __shfl_xor_sync(kFull, a4, o); }
   if (lane == 0) { atomicAdd(cnt.hydro_pairs, a1); atomicAdd(cnt.exact_checks, a4); }
   lvn_finish(p, slot, mine, lvn_own);
-  finish_particle_f<LPG>(prm, p, cnt, mine, sl, slot, A, 0.0, 0, 0, false);
+  finish_particle_f(prm, p, cnt, LPG, mine, sl, slot, A, 0.0, 0, 0, false);
 }
 
 template <int LPG>
