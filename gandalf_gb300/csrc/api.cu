@@ -61,7 +61,6 @@ struct gsph_ctx {
   CellGeom* geom = nullptr;
   CellBox *bb = nullptr, *hbox = nullptr;
   CellMoment* mom = nullptr;
-  unsigned* climb = nullptr;
   unsigned long long* key[3] = {};
   int* idx[3] = {};
   int* listb[3] = {};
@@ -71,8 +70,9 @@ struct gsph_ctx {
   int* dens_next = nullptr;               // FP64 h solve: leaf counter of its persistent warps
   double2* dens_comp = nullptr;           // FP64 h solve: per-warp compact lists
   int *radix_hist = nullptr, *radix_tot = nullptr;
-  unsigned char *side = nullptr, *seg_axis = nullptr;
-  int* blocksum = nullptr;
+  unsigned char *side = nullptr, *side2 = nullptr, *seg_axis = nullptr, *seg_axis_next = nullptr;
+  unsigned long long* part_tiles = nullptr;
+  unsigned* part_sync = nullptr;   // ticket, epoch
   unsigned long long* rootkey = nullptr;
   double* ibox = nullptr;
   unsigned long long* counters = nullptr;    // [0] status, [1..5] counts
@@ -288,7 +288,6 @@ int ensure_capacity(gsph_ctx* c, int n) {
     if (rc == GSPH_OK) rc = alloc(c, c->bb, capc);
     if (rc == GSPH_OK) rc = alloc(c, c->hbox, capc);
     if (rc == GSPH_OK) rc = alloc(c, c->mom, capc);
-    if (rc == GSPH_OK) rc = alloc(c, c->climb, capc);
     for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->key[q], capP);
     for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->idx[q], capP);
     for (int q = 0; q < 3 && rc == GSPH_OK; q++) rc = alloc(c, c->listb[q], capn);
@@ -300,8 +299,16 @@ int ensure_capacity(gsph_ctx* c, int n) {
     if (rc == GSPH_OK) rc = alloc(c, c->dens_next, 1);
     if (rc == GSPH_OK && c->cfg.precision != GSPH_PRECISION_MIXED) rc = alloc(c, c->dens_comp, density_fp64_scratch_entries());
     if (rc == GSPH_OK) rc = alloc(c, c->side, capn);
+    if (rc == GSPH_OK) rc = alloc(c, c->side2, capn);
     if (rc == GSPH_OK) rc = alloc(c, c->seg_axis, (capc + 1) / 2);
-    if (rc == GSPH_OK) rc = alloc(c, c->blocksum, 3 * (size_t) partition_blocks(capn) + 3);
+    if (rc == GSPH_OK) rc = alloc(c, c->seg_axis_next, (capc + 1) / 2);
+    if (rc == GSPH_OK) rc = alloc(c, c->part_tiles, 3 * (size_t) partition_blocks(capn));
+    if (rc == GSPH_OK) rc = alloc(c, c->part_sync, 2);
+    // the partition's tile words start invalid (flag 0) and its ticket counter at 0
+    if (rc == GSPH_OK && cudaMemset(c->part_tiles, 0, sizeof(unsigned long long) * 3 * (size_t) partition_blocks(capn)) != cudaSuccess)
+      rc = fail(c, GSPH_ERR_CUDA, "cudaMemset");
+    if (rc == GSPH_OK && cudaMemset(c->part_sync, 0, 2 * sizeof(unsigned)) != cudaSuccess)
+      rc = fail(c, GSPH_ERR_CUDA, "cudaMemset");
     if (rc == GSPH_OK) rc = alloc(c, c->rootkey, 8);
     if (rc == GSPH_OK) rc = alloc(c, c->ibox, 6 * ((size_t) 2 * capc + 3));
     if (rc == GSPH_OK) rc = alloc(c, c->counters, 16);
@@ -411,7 +418,7 @@ Tree make_tree(gsph_ctx* c) {
   t.n = c->n; t.ltot = c->ltot; t.ncell = c->ncell; t.nleaf = c->nleaf;
   t.cell_first = c->cell_first; t.cell_n = c->cell_n; t.cell_level = c->cell_level;
   t.cell_parent = c->cell_parent; t.leaf_cell = c->leaf_cell;
-  t.geom = c->geom; t.bb = c->bb; t.hbox = c->hbox; t.mom = c->mom; t.climb = c->climb;
+  t.geom = c->geom; t.bb = c->bb; t.hbox = c->hbox; t.mom = c->mom;
   return t;
 }
 
@@ -628,6 +635,7 @@ int read_status(gsph_ctx* c) {
   if (st & kStatusHNotConverged) return fail(c, GSPH_ERR_NOT_CONVERGED, "Problem with convergence of h-rho iteration");
   if (st & kStatusStackOverflow) return fail(c, GSPH_ERR_CAPACITY, "tree walk stack overflow");
   if (st & kStatusRetryLimit) return fail(c, GSPH_ERR_CAPACITY, "hmax retry limit reached");
+  if (st & kStatusPartitionWait) return fail(c, GSPH_ERR_CUDA, "tree build: a partition wait gave up");
   return GSPH_OK;
 }
 
@@ -649,7 +657,9 @@ int do_build(gsph_ctx* c) {
   a.radix_hist = c->radix_hist;
   a.radix_tot = c->radix_tot;
   a.deep_inv = c->deep_inv;
-  a.side = c->side; a.seg_axis = c->seg_axis; a.blocksum = c->blocksum; a.rootkey = c->rootkey; a.ibox = c->ibox;
+  a.side[0] = c->side; a.side[1] = c->side2; a.seg_axis = c->seg_axis; a.seg_axis_next = c->seg_axis_next;
+  a.part = PartitionState{c->part_tiles, c->part_sync, c->part_sync + 1, reinterpret_cast<unsigned*>(c->counters)};
+  a.rootkey = c->rootkey; a.ibox = c->ibox;
   a.heap_first = c->heap_first; a.heap_n = c->heap_n; a.heap_ones_before = c->heap_ones;
   a.p = make_particles(c);
   a.id_out = c->id;
@@ -692,8 +702,7 @@ int do_props(gsph_ctx* c) {
   if (rc) return rc;
   GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
   mark(c, 2);
-  launch_update_hmax(t, p, c->stream);
-  c->launches += 1;
+  c->launches += (unsigned) launch_update_hmax(t, p, c->stream);
   if (c->kdk || c->bactive) {   // every particle's thermal properties before the force pass
     launch_kdk_thermal(p, make_params(c), c->stream);
     c->launches += 1;
@@ -1775,9 +1784,9 @@ int batch_body(gsph_batch* b) {
     const Particles p = make_particles(c);
     GSPH_CUDA(cudaMemcpyAsync(c->heavy_count + 2, c->heavy_count, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count, 0, sizeof(int), c->stream));
-    launch_update_hmax(t, p, c->stream);
+    c->launches += (unsigned) launch_update_hmax(t, p, c->stream);
     launch_mixed_prep_hydro(t, p, make_mixed_particles(c), make_mixed_cells(c), c->stream);
-    c->launches += 3;
+    c->launches += 2;
     if (c->record && c->rec_sph_cnt) {
       GSPH_CUDA(cudaMemsetAsync(c->rec_sph_cnt, 0, sizeof(int) * (size_t) c->n, c->stream));
       GSPH_CUDA(cudaMemsetAsync(c->rec_dir_cnt, 0, sizeof(unsigned long long) * (size_t) c->n, c->stream));

@@ -226,6 +226,7 @@ enum StatusBits : unsigned {
   kStatusHNotConverged = 1u << 1,   // h-rho iteration exhausted fixed point + bisection
   kStatusRetryLimit = 1u << 2,      // hmax growth retries exhausted
   kStatusBadInput = 1u << 3,        // non-finite or non-positive mass / h
+  kStatusPartitionWait = 1u << 4,   // a tree-build partition wait gave up (results invalid)
 };
 
 }  // namespace gsph

@@ -100,7 +100,6 @@ struct Tree {
   CellBox* bb;                // tight particle bounding box
   CellBox* hbox;              // bounding box of smoothing volumes
   CellMoment* mom;            // centre of mass, mass, quadrupole
-  unsigned* climb;            // per-cell arrival counters for bottom-up passes
 };
 
 }  // namespace gsph

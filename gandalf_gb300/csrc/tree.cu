@@ -15,8 +15,8 @@
 // marks each particle's side and stable-partitions all three lists with one global scan,
 // which keeps each child's lists sorted; once the segments are small, one block per
 // segment finishes the remaining levels in shared memory.  Particles are never moved
-// until the final gather into leaf order.  Stocking is one launch: each leaf thread stocks
-// its leaf and climbs while it is the second child to arrive at a parent.
+// until the final gather into leaf order.  Stocking runs bottom-up in a few launches, each
+// reducing up to seven levels of complete subtrees in shared memory.
 #include "gsph_state.cuh"
 #include "tree.cuh"
 
@@ -374,6 +374,152 @@ __global__ void __launch_bounds__(1024) k_part_scatter(int l, int n, BuildLists 
   }
 }
 
+// ---- single-pass level partition (the allocating build) ----------------------------------
+// One launch per level in place of count + scan + scatter: each block takes one tile
+// (kScanBlock positions) of one axis list in the order the blocks start (a ticket, so a
+// block only ever waits for blocks already running), counts the tile's second-child marks,
+// publishes the count, obtains the count of all earlier tiles of its list by decoupled
+// look-back, and scatters.  While it scatters, it also writes the next level's side marks of
+// the particles it places into the list of their child's split axis (so the next level needs
+// no marking pass).  Tile words: (epoch << 34) | (flag << 32) | count, flag 1 = count of the
+// tile alone, 2 = count of the tile and every earlier one.  The epoch advances once per
+// launch (the block with the last ticket bumps it and rewinds the ticket counter), so words
+// left by earlier launches are never taken for this one's; a wait that runs past its limit
+// sets kStatusPartitionWait and continues, and the host reports the error.
+constexpr unsigned kLbAggregate = 1u, kLbPrefix = 2u;
+constexpr int kLbSpinLimit = 1 << 22;
+
+// Longest side of a box (the split axis rule of KDTree::DivideTreeCell, :492-498).
+__device__ __forceinline__ int longest_axis(const double* bmin, const double* bmax) {
+  int kd = 0;
+  double rkmax = 0.0;
+  for (int k = 0; k < 3; k++) {
+    const double ext = __dsub_rn(bmax[k], bmin[k]);
+    if (ext > rkmax) { rkmax = ext; kd = k; }
+  }
+  return kd;
+}
+
+// k_split_prepare plus the split axes of the children (the next level's segments).
+__global__ void k_split_prepare_next(int l, BuildLists cur, const double* __restrict__ x,
+                                     const double* __restrict__ y, const double* __restrict__ z,
+                                     const int* __restrict__ heap_first, const int* __restrict__ heap_n,
+                                     double* ibox, unsigned char* seg_axis, unsigned char* seg_axis_next) {
+  const int nseg = 1 << l;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const int hidx = nseg - 1 + s;
+  const int first = heap_first[hidx], cnt = heap_n[hidx];
+  double bmin[3], bmax[3];
+  for (int k = 0; k < 3; k++) { bmin[k] = ibox[6 * hidx + k]; bmax[k] = ibox[6 * hidx + 3 + k]; }
+  const int kd = longest_axis(bmin, bmax);
+  seg_axis[s] = (unsigned char) kd;
+  double rdiv = 0.0;
+  if (cnt > 0) {
+    const int id = cur.l[kd][first + cnt / 2];
+    rdiv = kd == 0 ? x[id] : (kd == 1 ? y[id] : z[id]);
+  }
+  const int c1 = 2 * hidx + 1, c2 = 2 * hidx + 2;
+  double b1[6], b2[6];
+  for (int k = 0; k < 3; k++) {
+    b1[k] = bmin[k]; b1[3 + k] = bmax[k];
+    b2[k] = bmin[k]; b2[3 + k] = bmax[k];
+  }
+  b1[3 + kd] = rdiv;
+  b2[kd] = rdiv;
+  for (int k = 0; k < 6; k++) { ibox[6 * c1 + k] = b1[k]; ibox[6 * c2 + k] = b2[k]; }
+  seg_axis_next[2 * s] = (unsigned char) longest_axis(b1, b1 + 3);
+  seg_axis_next[2 * s + 1] = (unsigned char) longest_axis(b2, b2 + 3);
+}
+
+__device__ __forceinline__ unsigned long long lb_word(unsigned epoch, unsigned flag, unsigned v) {
+  return ((unsigned long long) epoch << 34) | ((unsigned long long) flag << 32) | (unsigned long long) v;
+}
+
+__global__ void __launch_bounds__(1024) k_part_level(int l, int n, BuildLists cur, BuildLists nxt,
+                                                     const unsigned char* __restrict__ side,
+                                                     unsigned char* side_next,
+                                                     const unsigned char* __restrict__ seg_axis_next,
+                                                     const int* __restrict__ heap_ones_before, int nb,
+                                                     PartitionState ps) {
+  __shared__ int ws[33];
+  __shared__ unsigned s_ticket, s_epoch;
+  __shared__ int s_before;
+  if (threadIdx.x == 0) {
+    const unsigned ep = *reinterpret_cast<volatile unsigned*>(ps.epoch);
+    __threadfence();
+    s_ticket = atomicAdd(ps.ticket, 1u);
+    s_epoch = ep & 0x3fffffffu;
+  }
+  __syncthreads();
+  const unsigned ticket = s_ticket, epoch = s_epoch;
+  const int total = 3 * nb;
+  if ((int) ticket >= total) return;   // cannot happen: one ticket per block of the grid
+  // tickets run over the three axes' tiles interleaved, each axis's tiles in order
+  const int a = (int) ticket % 3, b = (int) ticket / 3;
+  unsigned long long* words = ps.tiles + (size_t) a * nb;
+  const int base = b * kScanBlock;
+  const int j0 = base + 2 * threadIdx.x, j1 = j0 + 1;
+  const int* src = pick3(cur.l, a);
+  int* dst = pick3(nxt.l, a);
+  const int id0 = j0 < n ? src[j0] : -1;
+  const int id1 = j1 < n ? src[j1] : -1;
+  const int f0 = id0 >= 0 ? side[id0] : 0;
+  const int f1 = id1 >= 0 ? side[id1] : 0;
+  int count;
+  const int ex = block_exscan(f0 + f1, ws, count);
+  if (threadIdx.x == 0) {
+    if (b == 0) {
+      atomicExch(words, lb_word(epoch, kLbPrefix, (unsigned) count));
+      s_before = 0;
+    } else {
+      atomicExch(words + b, lb_word(epoch, kLbAggregate, (unsigned) count));
+      unsigned before = 0;
+      int i = b - 1, spins = 0;
+      while (i >= 0) {
+        const unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(words + i);
+        const unsigned flag = (unsigned) (w >> 32) & 3u;
+        if ((unsigned) (w >> 34) == epoch && flag != 0u) {
+          before += (unsigned) w;
+          if (flag == kLbPrefix) break;
+          i--;
+          spins = 0;
+          continue;
+        }
+        if (++spins > kLbSpinLimit) {
+          atomicOr(ps.status, (unsigned) kStatusPartitionWait);
+          break;
+        }
+        __nanosleep(32);
+      }
+      atomicExch(words + b, lb_word(epoch, kLbPrefix, before + (unsigned) count));
+      s_before = (int) before;
+    }
+    if ((int) ticket == total - 1) {
+      // every block has its ticket (and has read the epoch before taking it)
+      atomicExch(ps.ticket, 0u);
+      atomicAdd(ps.epoch, 1u);
+    }
+  }
+  __syncthreads();
+  const int ones_before_tile = s_before;
+  const int nseg = 1 << l;
+  auto place = [&](int j, int id, int f, int e) {
+    if (id < 0) return;
+    int first, cnt;
+    const int s = seg_of(j, n, l, first, cnt);
+    const int ones = e - heap_ones_before[nseg - 1 + s];   // ones before j inside the segment
+    const int half = cnt >> 1;
+    int pos, cfirst, ccnt;
+    if (f) { pos = first + half + ones; cfirst = first + half; ccnt = cnt - half; }
+    else { pos = first + (j - first) - ones; cfirst = first; ccnt = half; }
+    dst[pos] = id;
+    if (side_next && seg_axis_next[2 * s + f] == a) side_next[id] = (unsigned char) (pos - cfirst >= (ccnt >> 1));
+  };
+  place(j0, id0, f0, ones_before_tile + ex);
+  place(j1, id1, f1, ones_before_tile + ex + f0);
+}
+
 // ---- the deep levels of a segment in shared memory ---------------------------------------
 // Once every segment of a level holds at most kDeepMax particles, one block finishes its
 // segment's remaining levels in shared memory: the same split axis, median coordinate,
@@ -486,6 +632,29 @@ __global__ void k_gather_leaf_order(int n, const int* __restrict__ perm, InputAr
 }
 
 // ---- stocking (KDTree::StockCellProperties) ------------------------------------------
+// Bottom-up over the complete tree (all 2^ltot leaves on level ltot).  One launch takes the
+// nodes of one level, kStockBlock consecutive nodes per block (a complete subtree's nodes
+// of that level), and reduces up to log2(kStockBlock) levels above them in shared memory;
+// the next launch starts from the level where the last one stopped.  1M particles with
+// Nleafmax 8 (17 levels): leaves -> level 10 -> level 3 -> root, three launches.  Every
+// parent is computed by the lowest threads of its block, so the fp64 arithmetic runs in
+// compact warps, with no arrival counters or fences.
+constexpr int kStockBlock = 128;
+constexpr int kStockLevels = 7;        // log2(kStockBlock)
+
+// What a parent's stock needs of each child (KDTree::StockCellProperties, :958-1059).
+struct StockNode {
+  double bmin[3], bmax[3], hbmin[3], hbmax[3], hmax, m, r[3], q[5];
+  int n;
+};
+
+// Depth-first id of node k (left to right) of level L.
+__device__ __forceinline__ int cell_at(int L, int k, int ltot) {
+  int id = 0;
+  for (int i = 1; i <= L; i++) id += ((k >> (L - i)) & 1) ? (1 << (ltot - i + 1)) : 1;
+  return id;
+}
+
 __device__ void finish_geometry(int n, const double* bmin, const double* bmax, double hmax,
                                 double theta2, CellGeom& g) {
   if (n > 0) {
@@ -505,192 +674,276 @@ __device__ void finish_geometry(int n, const double* bmin, const double* bmax, d
   g.hmax = hmax;
 }
 
-__device__ void stock_leaf(const Tree& t, const Particles& p, int c, double theta2) {
+__device__ void store_cell(const Tree& t, int c, const StockNode& v, const CellGeom& g) {
+  t.geom[c] = g;
+  CellBox b, hb;
+  for (int k = 0; k < 3; k++) {
+    b.bbmin[k] = v.bmin[k]; b.bbmax[k] = v.bmax[k]; hb.bbmin[k] = v.hbmin[k]; hb.bbmax[k] = v.hbmax[k];
+  }
+  t.bb[c] = b;
+  t.hbox[c] = hb;
+  CellMoment mo;
+  for (int k = 0; k < 3; k++) mo.r[k] = v.r[k];
+  mo.m = v.m;
+  for (int k = 0; k < 5; k++) mo.q[k] = v.q[k];
+  mo.pad = 0.0;
+  t.mom[c] = mo;
+}
+
+__device__ StockNode stock_leaf(const Tree& t, const Particles& p, int c, double theta2) {
   const int first = t.cell_first[c], n = t.cell_n[c];
-  double m = 0.0, r[3] = {0.0, 0.0, 0.0}, hmax = 0.0;
-  double bmin[3] = {kBig, kBig, kBig}, bmax[3] = {-kBig, -kBig, -kBig};
-  double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+  StockNode v;
+  v.n = n;
+  v.m = 0.0; v.hmax = 0.0;
+  for (int k = 0; k < 3; k++) {
+    v.r[k] = 0.0; v.bmin[k] = kBig; v.bmax[k] = -kBig; v.hbmin[k] = kBig; v.hbmax[k] = -kBig;
+  }
   for (int j = 0; j < n; j++) {
     const int s = first + j;
     const double xs[3] = {p.x[s], p.y[s], p.z[s]};
     const double hh = p.h[s], mm = p.m[s];
-    hmax = fmax(hmax, hh);
-    m += mm;
+    v.hmax = fmax(v.hmax, hh);
+    v.m += mm;
     const double h2 = __dmul_rn(kKernRange, hh);
     for (int k = 0; k < 3; k++) {
-      r[k] = fma(mm, xs[k], r[k]);
-      bmin[k] = fmin(bmin[k], xs[k]);
-      bmax[k] = fmax(bmax[k], xs[k]);
-      hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
-      hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
+      v.r[k] = fma(mm, xs[k], v.r[k]);
+      v.bmin[k] = fmin(v.bmin[k], xs[k]);
+      v.bmax[k] = fmax(v.bmax[k], xs[k]);
+      v.hbmin[k] = fmin(v.hbmin[k], __dsub_rn(xs[k], h2));
+      v.hbmax[k] = fmax(v.hbmax[k], __dadd_rn(xs[k], h2));
     }
   }
-  if (m > 0.0) {
-    const double im = 1.0 / m;   // one division for the three components
-    for (int k = 0; k < 3; k++) r[k] *= im;
+  if (v.m > 0.0) {
+    const double im = 1.0 / v.m;   // one division for the three components
+    for (int k = 0; k < 3; k++) v.r[k] *= im;
   }
-  CellGeom g;
-  finish_geometry(n, bmin, bmax, hmax, theta2, g);
-  double q[5] = {0, 0, 0, 0, 0};
+  for (int k = 0; k < 5; k++) v.q[k] = 0.0;
   for (int j = 0; j < n; j++) {
     const int s = first + j;
     const double mm = p.m[s];
-    const double dx = p.x[s] - r[0], dy = p.y[s] - r[1], dz = p.z[s] - r[2];
+    const double dx = p.x[s] - v.r[0], dy = p.y[s] - v.r[1], dz = p.z[s] - v.r[2];
     const double drsqd = dx * dx + dy * dy + dz * dz;
-    q[0] += mm * (3.0 * dx * dx - drsqd);
-    q[1] += mm * 3.0 * dx * dy;
-    q[2] += mm * (3.0 * dy * dy - drsqd);
-    q[3] += mm * 3.0 * dz * dx;
-    q[4] += mm * 3.0 * dz * dy;
-  }
-  t.geom[c] = g;
-  CellBox b, hb;
-  for (int k = 0; k < 3; k++) { b.bbmin[k] = bmin[k]; b.bbmax[k] = bmax[k]; hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
-  t.bb[c] = b;
-  t.hbox[c] = hb;
-  CellMoment mo;
-  for (int k = 0; k < 3; k++) mo.r[k] = r[k];
-  mo.m = m;
-  for (int k = 0; k < 5; k++) mo.q[k] = q[k];
-  mo.pad = 0.0;
-  t.mom[c] = mo;
-}
-
-__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
-
-__device__ void stock_parent(const Tree& t, int c, int level, double theta2) {
-  const int c1 = c + 1, c2 = c2_of(c, level, t.ltot);
-  const int n1 = t.cell_n[c1], n2 = t.cell_n[c2];
-  double bmin[3] = {kBig, kBig, kBig}, bmax[3] = {-kBig, -kBig, -kBig};
-  double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
-  double hmax = 0.0;
-  const int ch[2] = {c1, c2};
-  const int chn[2] = {n1, n2};
-  double cm[2], cr[2][3], cq[2][5];
-  for (int q = 0; q < 2; q++) {
-    const int cc = ch[q];
-    const double* bbp = reinterpret_cast<const double*>(&t.bb[cc]);
-    const double* hbp = reinterpret_cast<const double*>(&t.hbox[cc]);
-    const double* gp = reinterpret_cast<const double*>(&t.geom[cc]);
-    const double* mp = reinterpret_cast<const double*>(&t.mom[cc]);
-    if (chn[q] > 0) {
-      for (int k = 0; k < 3; k++) {
-        bmin[k] = fmin(ldcg(bbp + k), bmin[k]);
-        bmax[k] = fmax(ldcg(bbp + 3 + k), bmax[k]);
-        hbmin[k] = fmin(ldcg(hbp + k), hbmin[k]);
-        hbmax[k] = fmax(ldcg(hbp + 3 + k), hbmax[k]);
-      }
-      hmax = fmax(hmax, ldcg(gp + 4));
-    }
-    for (int k = 0; k < 3; k++) cr[q][k] = ldcg(mp + k);
-    cm[q] = ldcg(mp + 3);
-    for (int k = 0; k < 5; k++) cq[q][k] = ldcg(mp + 4 + k);
-  }
-  const int n = n1 + n2;
-  const double m = cm[0] + cm[1];
-  double r[3] = {0.0, 0.0, 0.0};
-  if (m > 0.0) {
-    const double im = 1.0 / m;
-    for (int k = 0; k < 3; k++) r[k] = (cm[0] * cr[0][k] + cm[1] * cr[1][k]) * im;
+    v.q[0] += mm * (3.0 * dx * dx - drsqd);
+    v.q[1] += mm * 3.0 * dx * dy;
+    v.q[2] += mm * (3.0 * dy * dy - drsqd);
+    v.q[3] += mm * 3.0 * dz * dx;
+    v.q[4] += mm * 3.0 * dz * dy;
   }
   CellGeom g;
-  finish_geometry(n, bmin, bmax, hmax, theta2, g);
-  double q[5] = {0, 0, 0, 0, 0};
-  for (int s = 0; s < 2; s++) {
-    if (!(cm[s] > 0.0)) continue;
-    const double dx = cr[s][0] - r[0], dy = cr[s][1] - r[1], dz = cr[s][2] - r[2];
+  finish_geometry(n, v.bmin, v.bmax, v.hmax, theta2, g);
+  store_cell(t, c, v, g);
+  return v;
+}
+
+// A stocked cell read back (the input nodes of the upper launches).
+__device__ StockNode load_node(const Tree& t, int c) {
+  StockNode v;
+  const CellBox b = t.bb[c], hb = t.hbox[c];
+  const CellMoment mo = t.mom[c];
+  for (int k = 0; k < 3; k++) {
+    v.bmin[k] = b.bbmin[k]; v.bmax[k] = b.bbmax[k]; v.hbmin[k] = hb.bbmin[k]; v.hbmax[k] = hb.bbmax[k];
+    v.r[k] = mo.r[k];
+  }
+  v.hmax = t.geom[c].hmax;
+  v.m = mo.m;
+  for (int k = 0; k < 5; k++) v.q[k] = mo.q[k];
+  v.n = t.cell_n[c];
+  return v;
+}
+
+// Parent c from its children a (first) and b (second): boxes and hmax of the non-empty
+// children, centre of mass, and the quadrupole moved to the new centre.
+__device__ StockNode stock_parent(const Tree& t, int c, const StockNode& a, const StockNode& b, double theta2) {
+  StockNode v;
+  v.hmax = 0.0;
+  for (int k = 0; k < 3; k++) { v.bmin[k] = kBig; v.bmax[k] = -kBig; v.hbmin[k] = kBig; v.hbmax[k] = -kBig; }
+  const StockNode* ch[2] = {&a, &b};
+  for (int q = 0; q < 2; q++) {
+    const StockNode& u = *ch[q];
+    if (u.n > 0) {
+      for (int k = 0; k < 3; k++) {
+        v.bmin[k] = fmin(u.bmin[k], v.bmin[k]);
+        v.bmax[k] = fmax(u.bmax[k], v.bmax[k]);
+        v.hbmin[k] = fmin(u.hbmin[k], v.hbmin[k]);
+        v.hbmax[k] = fmax(u.hbmax[k], v.hbmax[k]);
+      }
+      v.hmax = fmax(v.hmax, u.hmax);
+    }
+  }
+  v.n = a.n + b.n;
+  v.m = a.m + b.m;
+  for (int k = 0; k < 3; k++) v.r[k] = 0.0;
+  if (v.m > 0.0) {
+    const double im = 1.0 / v.m;
+    for (int k = 0; k < 3; k++) v.r[k] = (a.m * a.r[k] + b.m * b.r[k]) * im;
+  }
+  for (int k = 0; k < 5; k++) v.q[k] = 0.0;
+  for (int q = 0; q < 2; q++) {
+    const StockNode& u = *ch[q];
+    if (!(u.m > 0.0)) continue;
+    const double dx = u.r[0] - v.r[0], dy = u.r[1] - v.r[1], dz = u.r[2] - v.r[2];
     const double drsqd = dx * dx + dy * dy + dz * dz;
-    for (int k = 0; k < 5; k++) q[k] += cq[s][k];
-    q[0] += cm[s] * (3.0 * dx * dx - drsqd);
-    q[1] += cm[s] * 3.0 * dx * dy;
-    q[2] += cm[s] * (3.0 * dy * dy - drsqd);
-    q[3] += cm[s] * 3.0 * dz * dx;
-    q[4] += cm[s] * 3.0 * dz * dy;
+    for (int k = 0; k < 5; k++) v.q[k] += u.q[k];
+    v.q[0] += u.m * (3.0 * dx * dx - drsqd);
+    v.q[1] += u.m * 3.0 * dx * dy;
+    v.q[2] += u.m * (3.0 * dy * dy - drsqd);
+    v.q[3] += u.m * 3.0 * dz * dx;
+    v.q[4] += u.m * 3.0 * dz * dy;
   }
-  t.geom[c] = g;
-  CellBox b, hb;
-  for (int k = 0; k < 3; k++) { b.bbmin[k] = bmin[k]; b.bbmax[k] = bmax[k]; hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
-  t.bb[c] = b;
-  t.hbox[c] = hb;
-  CellMoment mo;
-  for (int k = 0; k < 3; k++) mo.r[k] = r[k];
-  mo.m = m;
-  for (int k = 0; k < 5; k++) mo.q[k] = q[k];
-  mo.pad = 0.0;
-  t.mom[c] = mo;
+  CellGeom g;
+  finish_geometry(v.n, v.bmin, v.bmax, v.hmax, theta2, g);
+  store_cell(t, c, v, g);
+  return v;
 }
 
-// Bottom-up climb: the second child to finish stocks the parent.
-__global__ void k_stock(Tree t, Particles p, double theta2) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= t.nleaf) return;
-  int c = t.leaf_cell[s];
-  stock_leaf(t, p, c, theta2);
-  int level = t.ltot;
-  while (level > 0) {
-    const int parent = t.cell_parent[c];
-    __threadfence();
-    const unsigned old = atomicAdd(&t.climb[parent], 1u);
-    if (old == 0u) return;
-    __threadfence();
-    level--;
-    c = parent;
-    stock_parent(t, c, level, theta2);
+// Shared-memory copy of the nodes of one level (structure of arrays: no bank conflicts).
+struct StockSmem {
+  double d[21][kStockBlock];
+  int n[kStockBlock], cid[kStockBlock];
+};
+
+__device__ __forceinline__ void put_node(StockSmem& sm, int i, const StockNode& v, int cid) {
+  for (int k = 0; k < 3; k++) {
+    sm.d[k][i] = v.bmin[k]; sm.d[3 + k][i] = v.bmax[k]; sm.d[6 + k][i] = v.hbmin[k]; sm.d[9 + k][i] = v.hbmax[k];
+    sm.d[13 + k][i] = v.r[k];
+  }
+  sm.d[12][i] = v.hmax;
+  sm.d[16][i] = v.m;
+  sm.n[i] = v.n;
+  sm.cid[i] = cid;
+}
+
+__device__ __forceinline__ StockNode get_node(const StockSmem& sm, const double (*q)[kStockBlock], int i) {
+  StockNode v;
+  for (int k = 0; k < 3; k++) {
+    v.bmin[k] = sm.d[k][i]; v.bmax[k] = sm.d[3 + k][i]; v.hbmin[k] = sm.d[6 + k][i]; v.hbmax[k] = sm.d[9 + k][i];
+    v.r[k] = sm.d[13 + k][i];
+  }
+  v.hmax = sm.d[12][i];
+  v.m = sm.d[16][i];
+  for (int k = 0; k < 5; k++) v.q[k] = q[k][i];
+  v.n = sm.n[i];
+  return v;
+}
+
+// Nodes of level Lin (leaves when Lin == ltot) -> stocked cells up to level Lout.
+__global__ void __launch_bounds__(kStockBlock) k_stock(Tree t, Particles p, double theta2, int Lin, int Lout) {
+  __shared__ StockSmem sm;
+  __shared__ double sq[5][kStockBlock];   // the quadrupole terms
+  const int tid = threadIdx.x;
+  const int k = blockIdx.x * blockDim.x + tid;   // node of level Lin
+  StockNode v;
+  int cid;
+  if (Lin == t.ltot) {
+    cid = t.leaf_cell[k];
+    v = stock_leaf(t, p, cid, theta2);
+  } else {
+    cid = cell_at(Lin, k, t.ltot);
+    v = load_node(t, cid);
+  }
+  int w = blockDim.x;   // nodes of the current level held by this block
+  for (int L = Lin; L > Lout; L--) {
+    if (tid < w) {
+      put_node(sm, tid, v, cid);
+      for (int q = 0; q < 5; q++) sq[q][tid] = v.q[q];
+    }
+    __syncthreads();
+    w >>= 1;
+    if (tid < w) {
+      const StockNode a = get_node(sm, sq, 2 * tid), b = get_node(sm, sq, 2 * tid + 1);
+      cid = sm.cid[2 * tid] - 1;   // the first child of c is c + 1
+      v = stock_parent(t, cid, a, b, theta2);
+    }
+    __syncthreads();
   }
 }
 
-// KDTree::UpdateHmaxValues: hmax and hbox from the solved h; cdistsqd keeps its value.
-__global__ void k_update_hmax(Tree t, Particles p) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= t.nleaf) return;
-  int c = t.leaf_cell[s];
-  {
-    const int first = t.cell_first[c], n = t.cell_n[c];
-    double hmax = 0.0;
-    double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
+// ---- hmax update (KDTree::UpdateHmaxValues) --------------------------------------------
+// hmax and hbox from the solved h (cdistsqd keeps its value), the same level scheme.
+struct HmaxSmem {
+  double d[7][kStockBlock];   // hbmin, hbmax, hmax
+  int n[kStockBlock], cid[kStockBlock];
+};
+
+__global__ void __launch_bounds__(kStockBlock) k_update_hmax(Tree t, Particles p, int Lin, int Lout) {
+  __shared__ HmaxSmem sm;
+  const int tid = threadIdx.x;
+  const int k = blockIdx.x * blockDim.x + tid;
+  double hbmin[3], hbmax[3], hmax = 0.0;
+  int cid, n;
+  if (Lin == t.ltot) {
+    cid = t.leaf_cell[k];
+    const int first = t.cell_first[cid];
+    n = t.cell_n[cid];
+    for (int q = 0; q < 3; q++) { hbmin[q] = kBig; hbmax[q] = -kBig; }
     for (int j = 0; j < n; j++) {
-      const int q = first + j;
-      const double xs[3] = {p.x[q], p.y[q], p.z[q]};
-      const double hh = p.h[q];
+      const int s = first + j;
+      const double xs[3] = {p.x[s], p.y[s], p.z[s]};
+      const double hh = p.h[s];
       hmax = fmax(hmax, hh);
       const double h2 = __dmul_rn(kKernRange, hh);
-      for (int k = 0; k < 3; k++) {
-        hbmin[k] = fmin(hbmin[k], __dsub_rn(xs[k], h2));
-        hbmax[k] = fmax(hbmax[k], __dadd_rn(xs[k], h2));
+      for (int q = 0; q < 3; q++) {
+        hbmin[q] = fmin(hbmin[q], __dsub_rn(xs[q], h2));
+        hbmax[q] = fmax(hbmax[q], __dadd_rn(xs[q], h2));
       }
     }
-    t.geom[c].hmax = hmax;
+    t.geom[cid].hmax = hmax;
     CellBox hb;
-    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
-    t.hbox[c] = hb;
+    for (int q = 0; q < 3; q++) { hb.bbmin[q] = hbmin[q]; hb.bbmax[q] = hbmax[q]; }
+    t.hbox[cid] = hb;
+  } else {
+    cid = cell_at(Lin, k, t.ltot);
+    n = t.cell_n[cid];
+    const CellBox hb = t.hbox[cid];
+    for (int q = 0; q < 3; q++) { hbmin[q] = hb.bbmin[q]; hbmax[q] = hb.bbmax[q]; }
+    hmax = t.geom[cid].hmax;
   }
-  int level = t.ltot;
-  while (level > 0) {
-    const int parent = t.cell_parent[c];
-    __threadfence();
-    const unsigned old = atomicAdd(&t.climb[parent], 1u);
-    if (old == 0u) return;
-    __threadfence();
-    level--;
-    c = parent;
-    const int c1 = c + 1, c2 = c2_of(c, level, t.ltot);
-    double hmax = 0.0;
-    double hbmin[3] = {kBig, kBig, kBig}, hbmax[3] = {-kBig, -kBig, -kBig};
-    const int ch[2] = {c1, c2};
-    for (int q = 0; q < 2; q++) {
-      if (t.cell_n[ch[q]] <= 0) continue;
-      const double* hbp = reinterpret_cast<const double*>(&t.hbox[ch[q]]);
-      hmax = fmax(hmax, ldcg(&t.geom[ch[q]].hmax));
-      for (int k = 0; k < 3; k++) {
-        hbmin[k] = fmin(ldcg(hbp + k), hbmin[k]);
-        hbmax[k] = fmax(ldcg(hbp + 3 + k), hbmax[k]);
-      }
+  int w = blockDim.x;
+  for (int L = Lin; L > Lout; L--) {
+    if (tid < w) {
+      for (int q = 0; q < 3; q++) { sm.d[q][tid] = hbmin[q]; sm.d[3 + q][tid] = hbmax[q]; }
+      sm.d[6][tid] = hmax;
+      sm.n[tid] = n;
+      sm.cid[tid] = cid;
     }
-    t.geom[c].hmax = hmax;
-    CellBox hb;
-    for (int k = 0; k < 3; k++) { hb.bbmin[k] = hbmin[k]; hb.bbmax[k] = hbmax[k]; }
-    t.hbox[c] = hb;
+    __syncthreads();
+    w >>= 1;
+    if (tid < w) {
+      hmax = 0.0;
+      for (int q = 0; q < 3; q++) { hbmin[q] = kBig; hbmax[q] = -kBig; }
+      for (int ch = 2 * tid; ch <= 2 * tid + 1; ch++) {
+        if (sm.n[ch] <= 0) continue;
+        hmax = fmax(hmax, sm.d[6][ch]);
+        for (int q = 0; q < 3; q++) {
+          hbmin[q] = fmin(sm.d[q][ch], hbmin[q]);
+          hbmax[q] = fmax(sm.d[3 + q][ch], hbmax[q]);
+        }
+      }
+      n = sm.n[2 * tid] + sm.n[2 * tid + 1];
+      cid = sm.cid[2 * tid] - 1;
+      t.geom[cid].hmax = hmax;
+      CellBox hb;
+      for (int q = 0; q < 3; q++) { hb.bbmin[q] = hbmin[q]; hb.bbmax[q] = hbmax[q]; }
+      t.hbox[cid] = hb;
+    }
+    __syncthreads();
   }
+}
+
+// The level launches of a bottom-up pass: level ltot -> ... -> 0.
+template <class F>
+int for_stock_levels(int ltot, F&& launch) {
+  int launches = 0;
+  for (int Lin = ltot; Lin > 0;) {
+    const int Lout = Lin > kStockLevels ? Lin - kStockLevels : 0;
+    const int nodes = 1 << Lin;
+    const int block = nodes < kStockBlock ? nodes : kStockBlock;
+    launch(nodes / block, block, Lin, Lout);
+    launches++;
+    Lin = Lout;
+  }
+  if (ltot == 0) { launch(1, 1, 0, 0); launches++; }
+  return launches;
 }
 
 int grid_for(int n, int block, int maxblocks = 152 * 16) {
@@ -752,14 +1005,18 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
   if (!a.deep_inv) L0 = a.ltot;
   for (int l = 0; l < L0; l++) {
     const int nseg = 1 << l;
-    k_split_prepare<<<(nseg + 127) / 128, 128, 0, st>>>(l, cur, a.in.x, a.in.y, a.in.z, a.heap_first,
-                                                         a.heap_n, a.ibox, a.seg_axis);
-    k_mark_side<<<grid_for(n, 256), 256, 0, st>>>(l, n, cur, a.seg_axis, a.side);
-    k_part_count<<<dim3(nb, 3), 1024, 0, st>>>(n, cur, a.side, a.blocksum, nb);
-    k_part_scan<<<dim3(1, 3), 1024, 0, st>>>(a.blocksum, nb);
-    k_part_scatter<<<dim3(nb, 3), 1024, 0, st>>>(l, n, cur, nxt, a.side, a.blocksum, nb, a.heap_ones_before);
+    unsigned char* side = a.side[l & 1];
+    k_split_prepare_next<<<(nseg + 127) / 128, 128, 0, st>>>(l, cur, a.in.x, a.in.y, a.in.z, a.heap_first,
+                                                              a.heap_n, a.ibox, a.seg_axis, a.seg_axis_next);
+    launches += 1;
+    if (l == 0) {   // later levels get their marks from the previous level's partition
+      k_mark_side<<<grid_for(n, 256), 256, 0, st>>>(l, n, cur, a.seg_axis, side);
+      launches += 1;
+    }
+    k_part_level<<<3 * nb, 1024, 0, st>>>(l, n, cur, nxt, side, l + 1 < L0 ? a.side[(l + 1) & 1] : nullptr,
+                                          a.seg_axis_next, a.heap_ones_before, nb, a.part);
+    launches += 1;
     BuildLists tmp = cur; cur = nxt; nxt = tmp;
-    launches += 5;
   }
   if (L0 < a.ltot) {
     k_build_deep<<<1 << L0, kDeepThreads, 0, st>>>(L0, a.ltot, cur, a.deep_inv, a.in.x, a.in.y, a.in.z,
@@ -767,14 +1024,17 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
     launches++;
   }
   k_gather_leaf_order<<<grid_for(n, 256), 256, 0, st>>>(n, cur.l[0], a.in, a.p, a.id_out, a.slot_of);
-  cudaMemsetAsync(a.tree.climb, 0, sizeof(unsigned) * (size_t) a.tree.ncell, st);
-  k_stock<<<(a.tree.nleaf + 127) / 128, 128, 0, st>>>(a.tree, a.p, a.thetamaxsqd);
-  return launches + 2;
+  launches += 1;
+  launches += for_stock_levels(a.tree.ltot, [&](int grid, int block, int Lin, int Lout) {
+    k_stock<<<grid, block, 0, st>>>(a.tree, a.p, a.thetamaxsqd, Lin, Lout);
+  });
+  return launches;
 }
 
-void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st) {
-  cudaMemsetAsync(t.climb, 0, sizeof(unsigned) * (size_t) t.ncell, st);
-  k_update_hmax<<<(t.nleaf + 127) / 128, 128, 0, st>>>(t, p);
+int launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st) {
+  return for_stock_levels(t.ltot, [&](int grid, int block, int Lin, int Lout) {
+    k_update_hmax<<<grid, block, 0, st>>>(t, p, Lin, Lout);
+  });
 }
 
 }  // namespace gsph

@@ -24,6 +24,14 @@ struct BuildLists {
   int* l[3];                    // per-axis position lists of particle indices
 };
 
+// Cross-block state of the single-pass level partition (tree.cu k_part_level).
+struct PartitionState {
+  unsigned long long* tiles;    // 3 * partition_blocks(n) tile words
+  unsigned* ticket;             // next tile ticket (0 between launches)
+  unsigned* epoch;              // launch epoch of the tile words
+  unsigned* status;             // kStatusPartitionWait when a look-back wait gave up
+};
+
 struct InputArrays {            // input order, fp64
   const double *x, *y, *z, *vx, *vy, *vz, *m, *u, *h;
 };
@@ -37,9 +45,10 @@ struct BuildArgs {
   int* radix_hist;              // 3 x 256 x radix_tiles(n)
   int* radix_tot;               // 3 x 256
   int* deep_inv;                // n: global -> local id of the shared-memory deep levels
-  unsigned char* side;          // per particle: 0 first child, 1 second child
+  unsigned char* side[2];       // per particle: 0 first child, 1 second child (this level, next level)
   unsigned char* seg_axis;      // per segment of the current level
-  int* blocksum;                // 3 * partition_blocks(n)
+  unsigned char* seg_axis_next; // per segment of the next level
+  PartitionState part;
   unsigned long long* rootkey;  // 6
   double* ibox;                 // inherited boxes, heap-indexed, 6 per cell
   const int* heap_first;        // heap-indexed segment tables (static per N)
@@ -56,6 +65,6 @@ int sort_padded_size(int n);
 int partition_blocks(int n);
 int radix_tiles(int n);
 int launch_build_tree(const BuildArgs& a, cudaStream_t st);   // returns kernels launched
-void launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st);
+int launch_update_hmax(const Tree& t, const Particles& p, cudaStream_t st);   // returns kernels launched
 
 }  // namespace gsph
