@@ -57,6 +57,10 @@ FLOPS = dict(density=45, hydro=60, hydro_grav=127, direct=24, quad=80, mono=23)
 FORCE_TRAFFIC = {
     ("plummer_sphere", 262144, "mixed"): {"bytes": 45.65e6 + 0.55e6 + 5.15e6,
                                           "source": "profiles/forces_density_mixed_plummer262k_dram.md"},
+    # the warp-per-leaf force kernel of a KDK first pass, cold L2 (ncu flushes caches), mean
+    # of three launches
+    ("rotating_cloud", 1048576, "mixed"): {"bytes": 282.0e6,
+                                           "source": "profiles/forces_mixed_rotating_cloud1m_dram.md"},
 }
 
 

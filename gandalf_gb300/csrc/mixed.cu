@@ -161,27 +161,35 @@ struct DensSmem {
 
 // One step of GradhSph::ComputeH's h iteration (src/GradhSph/GradhSph.cpp:206-254) from
 // the kernel sums of the current h (drho = sum m W, dom = sum m h^-1 Womega, dze = sum m
-// Wzeta, before the h^-3 / h^-2 factors): the density, the convergence test against
-// h_fac (m / rho)^(1/3), then a fixed-point step (iterations < 30) or bisection (up to
-// 150).  h_fac (m/rho)^(1/3) = h_fac h w^(-1/3) with w = rho h^3 / m: a float reciprocal
-// cube root refined by one fp64 Newton step (relative error ~1e-14).  Sets done when the
-// particle has finished (converged, left the bracket, aborted with h > hmax_list, or
-// failed to converge).
+// Wzeta, before the h^-3 / h^-2 factors): the convergence test against h_fac (m /
+// rho)^(1/3), then a fixed-point step (iterations < 30) or bisection (up to 150).
+// h_fac (m/rho)^(1/3) = h_fac h w^(-1/3) with w = rho h^3 / m: a float reciprocal cube
+// root refined by one fp64 Newton step (relative error ~1e-14).  Sets done when the
+// particle has finished (converged, left the bracket, aborted with h > hmax_list, or failed
+// to converge).  rho, om and zeta (the density and its terms at this h) are formed only
+// when they are used: on finishing and in the bisection test; rho > 0 is tested as drho > 0
+// (h^-3 > 0).  GB300 runs fp64 at 1/64 of the fp32 rate, so the update keeps to the fp64
+// operations the test and the h sequence need.
 __device__ __forceinline__ void h_update(double drho, double dom, double dze, double inv_m, double inv_hfac,
-                                         double invhsqd, double hmax_list, const SphParams& prm, int iteration,
+                                         double hmax_list, const SphParams& prm, int iteration,
                                          double& hi, double& invh, double& h_lower, double& h_upper,
                                          double& hrho_last, double& rho, double& om, double& zeta, double& mloc,
                                          bool& done, bool& abort_cell, bool& fail) {
-  const double hfac3 = invh * invhsqd;
-  rho = drho * hfac3;
-  om = dom * hfac3;
-  zeta = dze * invhsqd;
+  const double invh0 = invh;
+  auto density = [&]() {
+    const double isq = invh0 * invh0, hfac3 = invh0 * isq;
+    rho = drho * hfac3;
+    om = dom * hfac3;
+    zeta = dze * isq;
+  };
   const double w = drho * inv_m;
   double r = (double) rcbrtf((float) w);
   r = r * (4.0 / 3.0 - (w * (1.0 / 3.0)) * (r * r * r));
   const double hrho = prm.h_fac * hi * r;
   hrho_last = hrho;
-  if (rho > 0.0 && hi > h_lower && fabs(hi - hrho) * invh < prm.h_converge) {
+  // h_lower is 0 until the bisection starts (iteration 31)
+  if (drho > 0.0 && (iteration <= 30 || hi > h_lower) && fabs(hi - hrho) * invh < prm.h_converge) {
+    density();
     done = true;
     return;
   }
@@ -191,9 +199,11 @@ __device__ __forceinline__ void h_update(double drho, double dom, double dze, do
   } else {
     if (iteration == 30) hi = 0.5 * (h_lower + h_upper);
     else if (iteration < 150) {
+      density();
       if (rho < kSmall || hi > hrho) h_upper = hi; else h_lower = hi;
       hi = 0.5 * (h_lower + h_upper);
     } else {
+      density();
       fail = true;
       done = true;
       return;
@@ -203,6 +213,7 @@ __device__ __forceinline__ void h_update(double drho, double dom, double dze, do
   mloc = fmax(mloc, hi);
   if (hi > hmax_list) { abort_cell = true; done = true; }
   else if (!(hi > h_lower && hi < h_upper)) done = true;
+  if (done) density();
 }
 
 // Final per-particle results of the h solve (GradhSph.cpp:262-317): h, rho, hfactor,
@@ -272,6 +283,8 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
   const bool it_mine = remap ? it_g >= 0 : mine;
   const int it_slot = first + (it_g >= 0 && it_g < ncell ? it_g : 0);
   const double it_m = p.m[it_slot], it_h0 = p.h[it_slot];
+  const double it_inv_m = it_sl == 0 ? 1.0 / it_m : 0.0;
+  const double inv_hfac = it_sl == 0 ? 1.0 / prm.h_fac : 0.0;
   const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
   const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot];
   const CellBox bb = t.bb[c];
@@ -449,10 +462,14 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
     const bool use_compact = remap || (!overflow && ccount <= kcap);
 
     // The iteration state (h, its bracket, the h(rho) target) and the convergence test are
-    // fp64, as in the reference (GradhSph.cpp:206-254); the kernel sums are float.
+    // fp64, as in the reference (GradhSph.cpp:206-254); the kernel sums are float.  The
+    // fp64 update runs on the first lane of the particle's group only (an fp64 instruction
+    // occupies GB300's fp64 pipe for every active lane), which passes the float 1/h, 1/h^2
+    // and the done flag to the group's other lanes.
+    const bool lead = it_sl == 0;
+    const int lead_lane = lane - it_sl;
     double hi = it_h0, h_lower = 0.0, h_upper = hmax_list;
-    double invh = 1.0 / hi, hrho_last = hi;
-    const double inv_m = 1.0 / it_m, inv_hfac = 1.0 / prm.h_fac;
+    double invh = lead ? 1.0 / hi : 0.0, hrho_last = hi;
     double rho = 0.0, om = 0.0, zeta = 0.0;
     int iteration = 0;
     bool done = !it_mine, abort_cell = false;
@@ -462,8 +479,13 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
       if (WARPS > 1) any_active = __syncthreads_or(any_active);
       if (!any_active) break;
       iteration++;
-      const double invhsqd = invh * invh;
-      const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
+      float invh_f = 0.0f, invhsqd_f = 0.0f;
+      if (lead) {
+        invh_f = (float) invh;
+        invhsqd_f = (float) (invh * invh);
+      }
+      invh_f = __shfl_sync(kFull, invh_f, lead_lane);
+      invhsqd_f = __shfl_sync(kFull, invhsqd_f, lead_lane);
       float srho = 0.0f, som = 0.0f, sze = 0.0f;
       float crho = 0.0f, com = 0.0f, cze = 0.0f;   // compensation terms (compensated sums)
       const bool comp = prm.compensated != 0;
@@ -536,19 +558,21 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
         drho = fr; dom = fo; dze = fz;
         __syncthreads();
       }
-      if (!done)
-        h_update(drho, dom, dze, inv_m, inv_hfac, invhsqd, hmax_list, prm, iteration, hi,
+      if (!done && lead)
+        h_update(drho, dom, dze, it_inv_m, inv_hfac, hmax_list, prm, iteration, hi,
                  invh, h_lower, h_upper, hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
+      done = __shfl_sync(kFull, done, lead_lane);
     }
     double mw = mloc;
     for (int o = 16; o > 0; o >>= 1) mw = fmax(mw, __shfl_xor_sync(kFull, mw, o));
     bool any_abort = __any_sync(kFull, abort_cell);
     if (WARPS > 1) any_abort = __syncthreads_or(any_abort);
     mcheck = fmax(mcheck, mw);
-    if (!any_abort && it_mine) {
+    if (!any_abort && it_mine && lead) {
       h_out = fmax(hrho_last, h_lower);
       rho_out = rho; om_out = om; zeta_out = zeta;
     }
+    if (!any_abort) h_out = __shfl_sync(kFull, h_out, lead_lane);   // the star term's lanes
     return any_abort ? 1 : 0;
   };
 
@@ -626,16 +650,22 @@ __device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& 
       if (!is_active(p, slot)) continue;
       const float4 pih = mp.pos_hi[slot], pil = mp.pos_lo[slot];
       const double xi = p.x[slot], yi = p.y[slot], zi = p.z[slot], mi = p.m[slot];
+      // the fp64 update on lane 0, which passes h, the float 1/h, 1/h^2 and done to the warp
       double hi = sm.h0[g], h_lower = 0.0, h_upper = hk;
-      double invh = 1.0 / hi, hrho_last = hi;
-      const double inv_m = 1.0 / mi, inv_hfac = 1.0 / prm.h_fac;
+      double invh = lane == 0 ? 1.0 / hi : 0.0, hrho_last = hi;
+      const double inv_m = lane == 0 ? 1.0 / mi : 0.0, inv_hfac = lane == 0 ? 1.0 / prm.h_fac : 0.0;
       double rho = 0.0, om = 0.0, zeta = 0.0;
       bool done = false, abort_cell = false;
       int iteration = 0;
       while (!done) {
         iteration++;
-        const double invhsqd = invh * invh;
-        const float invh_f = (float) invh, invhsqd_f = (float) invhsqd;
+        float invh_f = 0.0f, invhsqd_f = 0.0f;
+        if (lane == 0) {
+          invh_f = (float) invh;
+          invhsqd_f = (float) (invh * invh);
+        }
+        invh_f = __shfl_sync(kFull, invh_f, 0);
+        invhsqd_f = __shfl_sync(kFull, invhsqd_f, 0);
         float srho = 0.0f, som = 0.0f, sze = 0.0f;
         // the particle's search box, rounded outwards, and its periodic images
         const double rr = __dmul_rn(kKernRange * (1.0 + 1.0 / 1024.0), hi);
@@ -722,15 +752,20 @@ __device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& 
           som += __shfl_xor_sync(kFull, som, o);
           sze += __shfl_xor_sync(kFull, sze, o);
         }
-        h_update(srho, som, sze, inv_m, inv_hfac, invhsqd, hk, prm, iteration, hi, invh, h_lower, h_upper,
-                 hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
+        if (lane == 0)
+          h_update(srho, som, sze, inv_m, inv_hfac, hk, prm, iteration, hi, invh, h_lower, h_upper,
+                   hrho_last, rho, om, zeta, mloc, done, abort_cell, fail);
+        hi = __shfl_sync(kFull, hi, 0);
+        done = __shfl_sync(kFull, done, 0);
         if (!stack_ok) done = true;
       }
+      abort_cell = __shfl_sync(kFull, abort_cell, 0);
       abort_any = abort_any || abort_cell;
       // the SPH-star zeta term, the warp's lanes sharing the stars (h is warp-uniform here)
       float zs = 0.0f;
       if (prm.stars.n && !abort_cell) {
-        zs = star_zeta_part_f(prm.stars, pih, pil, (float) fmax(hrho_last, h_lower), lane, 32);
+        const double hfin = __shfl_sync(kFull, fmax(hrho_last, h_lower), 0);
+        zs = star_zeta_part_f(prm.stars, pih, pil, (float) hfin, lane, 32);
         for (int o = 16; o > 0; o >>= 1) zs += __shfl_xor_sync(kFull, zs, o);
       }
       if (!abort_cell && lane == 0)
@@ -1058,12 +1093,14 @@ struct ForceSmem {
 // emitted list entry (sel = its slice), and their partial sums are added in slice order.
 // REC: the list-recording build (counts, hashes and full lists of every pair kind); the
 // production build has none of that code in its pair loops.
+// SLICES == 1 hands the leaf over (returns false) when its near or direct list overflows.
 template <int LPG, int SLICES, bool REC>
 __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& p, const MixedParticles& mp,
                                                 const MixedCells& mc, const SphParams& prm, const DeviceCounters& cnt,
                                                 int leaf, int pfirst, int* stack, int* la, int* lb, int* lc, int capa,
-                                                int capb, int capc, bool give_up, int sel = 0,
+                                                int capb, int capc, int sel = 0,
                                                 ForceSmem* fs = nullptr) {
+  constexpr bool give_up = SLICES == 1;
   const int lane = threadIdx.x & 31;
   constexpr int GT = 32 / LPG;   // particles of the leaf (from pfirst) this warp holds
   const int c = t.leaf_cell[leaf];
@@ -1130,7 +1167,7 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
 #pragma unroll
     for (int u = 0; u < 8; u++) {
       if (u0 + u >= ntg) break;
-      if (tgt[u0 + u].w == 0.0f) continue;   // inactive target: nothing was summed (warp-uniform)
+      if (SLICES > 1 && tgt[u0 + u].w == 0.0f) continue;   // inactive target: nothing was summed (warp-uniform)
 #pragma unroll
       for (int k = 0; k < 4; k++)
         for (int o = 16; o > 0; o >>= 1) acc[u][k] = __fadd_rn(acc[u][k], __shfl_xor_sync(kFull, acc[u][k], o));
@@ -1156,35 +1193,39 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         float cx, cy, cz;
         rel(ch, cl, cx, cy, cz);
         const float4 q = quad ? mc.quad[cc] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float q4 = cl.w;
+        const float q4 = cl.w, qzz = -__fadd_rn(q.x, q.z);
+        const float mc_ = ch.w;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
           if (u0 + u >= ntg) break;
           const float4 tu = tgt[u0 + u];
-          if (tu.w == 0.0f) continue;
-          // explicit roundings: the same sums in every kernel this leaf code is built into
+          if (SLICES > 1 && tu.w == 0.0f) continue;   // (SLICES == 1: the targets are the active particles)
+          // Monopole and quadrupole of the cell (NeighbourSearch.h:423-449) in the form
+          //   a += (-m r^-3 - 2.5 (d.Q.d) r^-7) d + r^-5 Q.d,   gpot += m r^-1 + 0.5 (d.Q.d) r^-5,
+          // accumulated by fused multiply-adds; explicit roundings: the same sums in every
+          // kernel this leaf code is built into
           const float dx = __fsub_rn(tu.x, cx), dy = __fsub_rn(tu.y, cy), dz = __fsub_rn(tu.z, cz);
-          const float r2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), 1.0e-20f);
+          const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, 1.0e-20f)));
           const float inv = rsqrtf(r2);
           const float inv2 = __fmul_rn(inv, inv);
-          const float mon = __fmul_rn(__fmul_rn(ch.w, inv2), inv);
-          float ax = __fmul_rn(-mon, dx), ay = __fmul_rn(-mon, dy), az = __fmul_rn(-mon, dz);
-          float pot = __fmul_rn(ch.w, inv);
+          const float minv3 = __fmul_rn(__fmul_rn(mc_, inv), inv2);
+          float c1 = -minv3;
           if (quad) {
             const float inv5 = __fmul_rn(__fmul_rn(inv2, inv2), inv);
-            const float qzz = -__fadd_rn(q.x, q.z);
             const float qx = __fmaf_rn(q.w, dz, __fmaf_rn(q.y, dy, __fmul_rn(q.x, dx)));
             const float qy = __fmaf_rn(q4, dz, __fmaf_rn(q.z, dy, __fmul_rn(q.y, dx)));
             const float qz = __fmaf_rn(qzz, dz, __fmaf_rn(q4, dy, __fmul_rn(q.w, dx)));
-            const float qscalar = __fmaf_rn(qz, dz, __fmaf_rn(qy, dy, __fmul_rn(qx, dx)));
-            const float qfactor = __fmul_rn(__fmul_rn(__fmul_rn(2.5f, qscalar), inv5), inv2);
-            ax = __fadd_rn(ax, __fmaf_rn(qx, inv5, __fmul_rn(-qfactor, dx)));
-            ay = __fadd_rn(ay, __fmaf_rn(qy, inv5, __fmul_rn(-qfactor, dy)));
-            az = __fadd_rn(az, __fmaf_rn(qz, inv5, __fmul_rn(-qfactor, dz)));
-            pot = __fmaf_rn(__fmul_rn(0.5f, qscalar), inv5, pot);
+            const float qs5 = __fmul_rn(__fmaf_rn(qz, dz, __fmaf_rn(qy, dy, __fmul_rn(qx, dx))), inv5);
+            c1 = -__fmaf_rn(__fmul_rn(2.5f, qs5), inv2, minv3);
+            acc[u][0] = __fmaf_rn(inv5, qx, acc[u][0]);
+            acc[u][1] = __fmaf_rn(inv5, qy, acc[u][1]);
+            acc[u][2] = __fmaf_rn(inv5, qz, acc[u][2]);
+            acc[u][3] = __fmaf_rn(0.5f, qs5, acc[u][3]);
           }
-          acc[u][0] = __fadd_rn(acc[u][0], ax); acc[u][1] = __fadd_rn(acc[u][1], ay);
-          acc[u][2] = __fadd_rn(acc[u][2], az); acc[u][3] = __fadd_rn(acc[u][3], pot);
+          acc[u][0] = __fmaf_rn(c1, dx, acc[u][0]);
+          acc[u][1] = __fmaf_rn(c1, dy, acc[u][1]);
+          acc[u][2] = __fmaf_rn(c1, dz, acc[u][2]);
+          acc[u][3] = __fmaf_rn(mc_, inv, acc[u][3]);
           ncellp++;
         }
         if (u0 == 0 && rec) {
@@ -1215,13 +1256,14 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
         for (int u = 0; u < 8; u++) {
           if (u0 + u >= ntg) break;
           const float4 tu = tgt[u0 + u];
-          if (tu.w == 0.0f) continue;
+          if (SLICES > 1 && tu.w == 0.0f) continue;
           const float dx = __fsub_rn(sx, tu.x), dy = __fsub_rn(sy, tu.y), dz = __fsub_rn(sz, tu.z);
-          const float r2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), 1.0e-20f);
+          const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, 1.0e-20f)));
           const float inv = rsqrtf(r2);
-          const float inv3 = __fmul_rn(__fmul_rn(__fmul_rn(inv, inv), inv), mj);
+          const float minv = __fmul_rn(mj, inv);
+          const float inv3 = __fmul_rn(__fmul_rn(inv, inv), minv);
           acc[u][0] = __fmaf_rn(dx, inv3, acc[u][0]); acc[u][1] = __fmaf_rn(dy, inv3, acc[u][1]);
-          acc[u][2] = __fmaf_rn(dz, inv3, acc[u][2]); acc[u][3] = __fmaf_rn(mj, inv, acc[u][3]);
+          acc[u][2] = __fmaf_rn(dz, inv3, acc[u][2]); acc[u][3] = __fadd_rn(acc[u][3], minv);
           ndir_b++;
           if (rec) {
             const int ts = first + pfirst + (int) tu.w - 1;
@@ -1236,34 +1278,35 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   };
   // near leaves: the particle's lpg lanes take the (entry, particle) pairs of the list in
   // turn (for lpg <= GT, particle q of every entry goes to lane q mod lpg)
+  auto near_pair = [&](int j) {
+    const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
+    const float dx = (pjh.x - T.ph.x) + (pjl.x - T.pl.x);
+    const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
+    const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (sph_member(p, T, j, d2, pjl.w, prm, exact)) {
+      hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
+      lvn_pair(p, slot, j, lvn_own);
+      nsph++;
+      if (rec) {
+        const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
+        if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
+      }
+    } else {
+      direct_term_f(dx, dy, dz, pjh.w, A, prm.compensated != 0);
+      ndir++;
+      if (rec) {
+        dhash += mix64((unsigned long long) p.id[j]);
+        rec_direct_id(cnt, slot, p.id[j]);
+      }
+    }
+  };
   auto consume_ab = [&]() {
     if (!mine) return;
     const int ntot = L.na * GT;
     for (int idx = sl; idx < ntot; idx += lpg) {
-      const int node = L.a[idx / GT], q = idx % GT;
-      if (q >= t.cell_n[node]) continue;
-      const int j = t.cell_first[node] + q;
-      const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
-      const float dx = (pjh.x - T.ph.x) + (pjl.x - T.pl.x);
-      const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
-      const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      if (sph_member(p, T, j, d2, pjl.w, prm, exact)) {
-        hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
-        lvn_pair(p, slot, j, lvn_own);
-        nsph++;
-        if (rec) {
-          const int k = atomicAdd(&cnt.rec_sph_cnt[slot], 1);
-          if (k < cnt.rec_max) cnt.rec_sph_ids[(size_t) slot * cnt.rec_max + k] = j;
-        }
-      } else {
-        direct_term_f(dx, dy, dz, pjh.w, A, prm.compensated != 0);
-        ndir++;
-        if (rec) {
-          dhash += mix64((unsigned long long) p.id[j]);
-          rec_direct_id(cnt, slot, p.id[j]);
-        }
-      }
+      const int node = L.a[idx / GT], qq = idx % GT;
+      if (qq < t.cell_n[node]) near_pair(t.cell_first[node] + qq);
     }
   };
   // the walk, with per-list flushing
@@ -1312,8 +1355,12 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     __syncwarp();
     if (L.nc > capc - 32) { consume_c(); L.nc = 0; __syncwarp(); }
     if (L.na > capa - 32 || L.nb > capb - 32) {
-      if (give_up) { gave_up = true; break; }
-      consume_ab(); consume_b(); L.na = 0; L.nb = 0; __syncwarp();
+      if constexpr (give_up) {
+        gave_up = true;
+        break;
+      } else {
+        consume_ab(); consume_b(); L.na = 0; L.nb = 0; __syncwarp();
+      }
     }
   }
   if (gave_up) {
@@ -1407,7 +1454,7 @@ k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphPar
   if (leaf >= t.nleaf) return;
   const bool ok = all_forces_leaf<LPG, 1, REC>(t, p, mp, mc, prm, cnt, leaf, 0, s_stack[wib], s_a[wib], s_b[wib],
                                                s_c[wib], tuned_depth(prm.near_depth, 64, kFListA), kFListB,
-                                               tuned_depth(prm.cell_depth, 64, kFListC), true);
+                                               tuned_depth(prm.cell_depth, 64, kFListC));
   if (!ok && (threadIdx.x & 31) == 0) {
     const int k = atomicAdd(heavy.count, 1);
     heavy.leaves[k] = leaf;
@@ -1428,7 +1475,7 @@ k_all_forces_mixed_wide(Tree t, Particles p, MixedParticles mp, MixedCells mc, S
   const int nh = *heavy.count;
   for (int k = blockIdx.x; k < nh; k += gridDim.x) {
     all_forces_leaf<LPG, 8, REC>(t, p, mp, mc, prm, cnt, heavy.leaves[k], 0, base, base + kFStack, base + kFStack + kWListA,
-                            base + kFStack + kWListA + kWListB, kWListA, kWListB, kWListC, false, wib, fs);
+                            base + kFStack + kWListA + kWListB, kWListA, kWListB, kWListC, wib, fs);
   }
 }
 
@@ -1646,7 +1693,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_batch_forces(BatchQueue q)
     const int leaf = item - q.leaf_start[s];
     const bool ok = all_forces_leaf<LPG, 1, REC>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, leaf, 0, s_stack[wib], s_a[wib],
                                             s_b[wib], s_c[wib], tuned_depth(d.prm.near_depth, 64, kFListA), kFListB,
-                                            tuned_depth(d.prm.cell_depth, 64, kFListC), true);
+                                            tuned_depth(d.prm.cell_depth, 64, kFListC));
     if (!ok && (threadIdx.x & 31) == 0) {
       const int k = atomicAdd(d.heavy.count, 1);
       d.heavy.leaves[k] = leaf;
@@ -1670,7 +1717,7 @@ __global__ void __launch_bounds__(256) k_batch_forces_wide(BatchQueue q) {
     const SimDesc& d = q.sims[s];
     all_forces_leaf<LPG, 8, REC>(d.t, d.p, d.mp, d.mc, d.prm, d.cnt, d.heavy.leaves[item - q.heavy_start[s]], 0, base,
                             base + kFStack, base + kFStack + kWListA, base + kFStack + kWListA + kWListB, kWListA,
-                            kWListB, kWListC, false, wib, fs);
+                            kWListB, kWListC, wib, fs);
   }
 }
 

@@ -174,59 +174,79 @@ __global__ void __launch_bounds__(1024) k_radix_scan(RadixArgs r) {
   if (threadIdx.x == 0) r.tot[a * 256 + d] = carry;
 }
 
+// Stable scatter of one tile: warp w owns the tile's elements [w * 512, (w + 1) * 512) in
+// rounds of 32 (kept in registers).  Pass 1 counts each digit per warp (warp match: the
+// lowest lane of each equal-digit group adds the group's size), the block turns the counts
+// into per-warp output offsets (digit by digit, warps in order), and pass 2 places each
+// element at its warp's running offset plus its rank among the equal digits of its round.
+// Two block barriers per tile; the element order within a digit is the tile order.
+constexpr int kRadixWarps = 8;
+constexpr int kRadixPerWarp = kRadixTile / kRadixWarps;   // 512
+constexpr int kRadixWarpRounds = kRadixPerWarp / 32;      // 16
+
 __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
-  __shared__ int dbase[256];           // digit start in the output for this tile
-  __shared__ int wcnt[8][256];         // per-warp digit counts of the current round
-  __shared__ int run[256];             // elements of each digit already placed by this tile
+  __shared__ int woff[kRadixWarps][256];   // per-warp digit counts, then output offsets
+  __shared__ int tsum[256];
   const int a = blockIdx.y, b = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  {
-    // exclusive scan of the digit totals (256 values) + this tile's offset within the digit
-    __shared__ int tsum[256];
-    tsum[tid] = r.tot[a * 256 + tid];
-    __syncthreads();
-    for (int o = 1; o < 256; o <<= 1) {
-      const int add = tid >= o ? tsum[tid - o] : 0;
-      __syncthreads();
-      tsum[tid] += add;
-      __syncthreads();
-    }
-    dbase[tid] = tsum[tid] - r.tot[a * 256 + tid] + r.hist[((size_t) a * 256 + tid) * r.ntiles + b];
-    run[tid] = 0;
-  }
+  for (int d = tid; d < kRadixWarps * 256; d += 256) (&woff[0][0])[d] = 0;
   const unsigned long long* key = pick3(r.src_key, a);
   const int* idx = pick3(r.src_idx, a);
   unsigned long long* okey = pick3(r.dst_key, a);
   int* oidx = pick3(r.dst_idx, a);
   const unsigned lt = (1u << lane) - 1u;
-  const int base = b * kRadixTile;
-  for (int q = 0; q < kRadixRounds; q++) {
-    for (int d = tid; d < 8 * 256; d += 256) (&wcnt[0][0])[d] = 0;
+  const int base = b * kRadixTile + w * kRadixPerWarp + lane;
+  unsigned long long k[kRadixWarpRounds];
+  int id[kRadixWarpRounds];
+#pragma unroll
+  for (int q = 0; q < kRadixWarpRounds; q++) {
+    const int i = base + 32 * q;
+    k[q] = i < r.n ? key[i] : 0ull;
+    id[q] = i < r.n ? idx[i] : -1;
+  }
+  // exclusive scan of the digit totals + this tile's offset within each digit
+  tsum[tid] = r.tot[a * 256 + tid];
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    const int add = tid >= o ? tsum[tid - o] : 0;
     __syncthreads();
-    const int i = base + q * 256 + tid;
-    const bool valid = i < r.n;
-    unsigned long long k = 0;
-    int id = 0;
-    unsigned dig = 256u + (unsigned) lane;   // distinct dummy digits for invalid lanes
-    if (valid) { k = key[i]; id = idx[i]; dig = (unsigned) (k >> shift) & 255u; }
+    tsum[tid] += add;
+    __syncthreads();
+  }
+  const int dstart = tsum[tid] - r.tot[a * 256 + tid] + r.hist[((size_t) a * 256 + tid) * r.ntiles + b];
+  // pass 1: per-warp digit counts
+#pragma unroll
+  for (int q = 0; q < kRadixWarpRounds; q++) {
+    const bool valid = id[q] >= 0;
+    const unsigned dig = valid ? (unsigned) (k[q] >> shift) & 255u : 256u + (unsigned) lane;
     const unsigned peers = __match_any_sync(kFull, dig);
-    const int rank = __popc(peers & lt);
-    if (valid && rank == 0) wcnt[w][dig] = __popc(peers);
-    __syncthreads();
+    if (valid && (peers & lt) == 0u) woff[w][dig] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  {
+    int run = dstart;
+    for (int v = 0; v < kRadixWarps; v++) {
+      const int c = woff[v][tid];
+      woff[v][tid] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  // pass 2: placement
+#pragma unroll
+  for (int q = 0; q < kRadixWarpRounds; q++) {
+    const bool valid = id[q] >= 0;
+    const unsigned dig = valid ? (unsigned) (k[q] >> shift) & 255u : 256u + (unsigned) lane;
+    const unsigned peers = __match_any_sync(kFull, dig);
     if (valid) {
-      int before = run[dig];
-      for (int v = 0; v < w; v++) before += wcnt[v][dig];
-      const int pos = dbase[dig] + before + rank;
-      okey[pos] = k;
-      oidx[pos] = id;
+      const int pos = woff[w][dig] + __popc(peers & lt);
+      okey[pos] = k[q];
+      oidx[pos] = id[q];
     }
-    __syncthreads();
-    {
-      int add = 0;
-      for (int v = 0; v < 8; v++) add += wcnt[v][tid];
-      run[tid] += add;
-    }
-    __syncthreads();
+    __syncwarp();
+    if (valid && (peers & lt) == 0u) woff[w][dig] += __popc(peers);
+    __syncwarp();
   }
 }
 
