@@ -860,26 +860,30 @@ struct AccF {
     }                                                                                            \
   } while (0)
 
+// The target's float mirrors; its fp64 position and hrangesqd, which only the rare exact
+// membership re-tests need, are read from the particle arrays there (registers are what
+// limits the force kernels' occupancy).
 struct TargetF {
   float4 ph, pl, vel, hyd, aux;   // see MixedParticles
-  double x, y, z, hrs;            // fp64 copies for exact membership checks
   int slot;
 };
 
 __device__ __forceinline__ void load_target_f(const Particles& p, const MixedParticles& mp, int s, TargetF& T) {
+  (void) p;
   T.ph = mp.pos_hi[s]; T.pl = mp.pos_lo[s]; T.vel = mp.vel[s]; T.hyd = mp.hyd[s]; T.aux = mp.aux[s];
-  T.x = p.x[s]; T.y = p.y[s]; T.z = p.z[s]; T.hrs = p.hrangesqd[s];
   T.slot = s;
 }
 
 // SPH neighbour (1), direct term (0): float test with margin, exact fp64 when ambiguous.
+template <class Count>
 __device__ __forceinline__ int sph_member(const Particles& p, const TargetF& T, int j, float d2, float hrsj,
-                                          const SphParams& prm, unsigned long long& exact) {
+                                          const SphParams& prm, Count& exact) {
   const float thr = fmaxf(T.aux.z, hrsj);
   if (d2 < thr * (1.0f - kMargin)) return 1;
   if (d2 > thr * (1.0f + kMargin)) return 0;
   exact++;
-  double dx = __dsub_rn(p.x[j], T.x), dy = __dsub_rn(p.y[j], T.y), dz = __dsub_rn(p.z[j], T.z);
+  const int i = T.slot;
+  double dx = __dsub_rn(p.x[j], p.x[i]), dy = __dsub_rn(p.y[j], p.y[i]), dz = __dsub_rn(p.z[j], p.z[i]);
   if (prm.periodic) {
     // the reference's image: nearest to the leaf centre, then corrected about the particle
     // (forces.cu k_hydro_fp64); for leaf cells far smaller than the box both give the
@@ -891,7 +895,7 @@ __device__ __forceinline__ int sph_member(const Particles& p, const TargetF& T, 
     }
   }
   const double drsqd = dot3_rn(dx, dy, dz);
-  return (drsqd >= T.hrs && drsqd >= p.hrangesqd[j]) ? 0 : 1;
+  return (drsqd >= p.hrangesqd[i] && drsqd >= p.hrangesqd[j]) ? 0 : 1;
 }
 
 __device__ __forceinline__ float pair_pressure_f(const SphParams& prm, const TargetF& T, float wi, float wj,
@@ -983,11 +987,12 @@ __device__ __forceinline__ void cell_term_f(const MixedCells& mc, int cc, const 
 // float test with margins, exact fp64 re-test when a float value is inside the margin.
 struct LeafGeo {
   float4 hi, lo;                // rcell hi/lo, rmax, hmax
-  double rc[3], rmax, hrangemax;  // fp64
+  int c;                        // the leaf cell (its fp64 geometry is read by the exact re-test)
 };
 
+template <class Count>
 __device__ __forceinline__ int grav_decide(const Tree& t, const MixedCells& mc, const LeafGeo& G, int node, int level,
-                                           float4 mt, unsigned long long& exact) {
+                                           float4 mt, Count& exact) {
   const int on = __float_as_int(mt.y);
   const float4 gh = mc.geo_hi[node], gl = mc.geo_lo[node];
   const float dx = (gh.x - G.hi.x) + (gl.x - G.lo.x);
@@ -1008,13 +1013,13 @@ __device__ __forceinline__ int grav_decide(const Tree& t, const MixedCells& mc, 
   else open_mac = -1;
   if (near < 0 || (near == 0 && open_mac < 0)) {
     exact++;
-    const CellGeom o = t.geom[node];
-    const double ddx = __dsub_rn(o.rcell[0], G.rc[0]);
-    const double ddy = __dsub_rn(o.rcell[1], G.rc[1]);
-    const double ddz = __dsub_rn(o.rcell[2], G.rc[2]);
+    const CellGeom o = t.geom[node], lg = t.geom[G.c];
+    const double ddx = __dsub_rn(o.rcell[0], lg.rcell[0]);
+    const double ddy = __dsub_rn(o.rcell[1], lg.rcell[1]);
+    const double ddz = __dsub_rn(o.rcell[2], lg.rcell[2]);
     const double drsqd = dot3_rn(ddx, ddy, ddz);
-    const double t1 = sq_rn(__dadd_rn(__dadd_rn(o.rmax, G.rmax), G.hrangemax));
-    const double t2 = sq_rn(__dadd_rn(__dadd_rn(G.rmax, o.rmax), __dmul_rn(kKernRange, o.hmax)));
+    const double t1 = sq_rn(__dadd_rn(__dadd_rn(o.rmax, lg.rmax), __dmul_rn(kKernRange, lg.hmax)));
+    const double t2 = sq_rn(__dadd_rn(__dadd_rn(lg.rmax, o.rmax), __dmul_rn(kKernRange, o.hmax)));
     near = (drsqd <= t1 || drsqd <= t2) ? 1 : 0;
     open_mac = drsqd < o.cdistsqd ? 1 : 0;
   }
@@ -1028,12 +1033,10 @@ __device__ __forceinline__ int grav_decide(const Tree& t, const MixedCells& mc, 
 }
 
 __device__ __forceinline__ void load_leaf_geo(const Tree& t, const MixedCells& mc, int c, LeafGeo& G) {
+  (void) t;
   G.hi = mc.geo_hi[c];
   G.lo = mc.geo_lo[c];
-  const CellGeom g = t.geom[c];
-  for (int k = 0; k < 3; k++) G.rc[k] = g.rcell[k];
-  G.rmax = g.rmax;
-  G.hrangemax = __dmul_rn(kKernRange, g.hmax);
+  G.c = c;
 }
 
 // lpg: lanes per particle (a power of two, uniform over the warp); the particle's lanes
@@ -1137,7 +1140,10 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   load_leaf_geo(t, mc, c, G);
   const bool quad = prm.multipole == 1;
   AccF A = {};
-  unsigned long long nsph = 0, ndir = 0, ndir_b = 0, ncellp = 0, exact = 0, dhash = 0, chash = 0, ccount = 0;
+  // per-lane counts of one leaf fit 32 bits; the hashes and cell counts exist only in the
+  // list-recording build
+  unsigned nsph = 0, ndir = 0, ndir_b = 0, ncellp = 0, exact = 0;
+  unsigned long long dhash = 0, chash = 0, ccount = 0;
   bool gave_up = false;
   // lists have separate capacities: WarpLists keeps one, so the flush test is done here
   WarpLists L{la, lb, lc, 0, 0, 0, 1 << 30};
@@ -1441,8 +1447,12 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
   return true;
 }
 
+// Five blocks (20 warps) per SM: the walk and the list loads are latency bound, and at four
+// blocks an SM (128 registers) the 1M rotating-cloud force pass took 10 % longer.  The
+// target's and the leaf's fp64 copies are read only where the exact re-tests need them, so
+// the kernel fits 94 registers (16 bytes of spill).
 template <int LPG, bool REC>
-__global__ void __launch_bounds__(kForceWarps * 32)
+__global__ void __launch_bounds__(kForceWarps * 32, 5)
 k_all_forces_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
                    HeavyList heavy) {
   __shared__ int s_stack[kForceWarps][kFStack];
@@ -1541,7 +1551,7 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
         float d[3] = {(pjh.x - T.ph.x) + (pjl.x - T.pl.x), (pjh.y - T.ph.y) + (pjl.y - T.pl.y),
                       (pjh.z - T.ph.z) + (pjl.z - T.pl.z)};
         if (prm.periodic) {
-          const double xj[3] = {p.x[j], p.y[j], p.z[j]}, xi[3] = {T.x, T.y, T.z};
+          const double xj[3] = {p.x[j], p.y[j], p.z[j]}, xi[3] = {p.x[slot], p.y[slot], p.z[slot]};
           int sh[3] = {0, 0, 0};   // image of j, in box lengths
           for (int k = 0; k < 3; k++) {
             if (fabsf(d[k]) > half[k] * 0.5f) {

@@ -176,17 +176,24 @@ __global__ void __launch_bounds__(1024) k_radix_scan(RadixArgs r) {
 
 // Stable scatter of one tile: warp w owns the tile's elements [w * 512, (w + 1) * 512) in
 // rounds of 32 (kept in registers).  Pass 1 counts each digit per warp (warp match: the
-// lowest lane of each equal-digit group adds the group's size), the block turns the counts
-// into per-warp output offsets (digit by digit, warps in order), and pass 2 places each
-// element at its warp's running offset plus its rank among the equal digits of its round.
-// Two block barriers per tile; the element order within a digit is the tile order.
+// lowest lane of each equal-digit group adds the group's size); the block turns the counts
+// into per-warp offsets inside the tile's digit-sorted order; pass 2 places each element in
+// shared memory at its warp's running offset plus its rank among the equal digits of its
+// round; the tile is then written out in that order, so consecutive threads store
+// consecutive positions of each digit's run (coalesced) instead of one 8-byte key and one
+// 4-byte index per element scattered over 256 runs.  The element order within a digit is
+// the tile order.
 constexpr int kRadixWarps = 8;
 constexpr int kRadixPerWarp = kRadixTile / kRadixWarps;   // 512
 constexpr int kRadixWarpRounds = kRadixPerWarp / 32;      // 16
+constexpr size_t kRadixScatterSmem = (size_t) kRadixTile * (sizeof(unsigned long long) + sizeof(int));
 
 __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
-  __shared__ int woff[kRadixWarps][256];   // per-warp digit counts, then output offsets
-  __shared__ int tsum[256];
+  extern __shared__ unsigned long long s_key[];             // kRadixTile keys, then kRadixTile indices
+  int* s_idx = reinterpret_cast<int*>(s_key + kRadixTile);
+  __shared__ int woff[kRadixWarps][256];   // per-warp digit counts, then offsets in the tile order
+  __shared__ int tsum[256], lsum[256];
+  __shared__ int dglob[256];                // output position of the tile's first element of each digit
   const int a = blockIdx.y, b = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   for (int d = tid; d < kRadixWarps * 256; d += 256) (&woff[0][0])[d] = 0;
@@ -195,7 +202,9 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
   unsigned long long* okey = pick3(r.dst_key, a);
   int* oidx = pick3(r.dst_idx, a);
   const unsigned lt = (1u << lane) - 1u;
-  const int base = b * kRadixTile + w * kRadixPerWarp + lane;
+  const int tile0 = b * kRadixTile;
+  const int ntile = min(kRadixTile, r.n - tile0);
+  const int base = tile0 + w * kRadixPerWarp + lane;
   unsigned long long k[kRadixWarpRounds];
   int id[kRadixWarpRounds];
 #pragma unroll
@@ -204,7 +213,7 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
     k[q] = i < r.n ? key[i] : 0ull;
     id[q] = i < r.n ? idx[i] : -1;
   }
-  // exclusive scan of the digit totals + this tile's offset within each digit
+  // exclusive scan of the digit totals (over all tiles)
   tsum[tid] = r.tot[a * 256 + tid];
   __syncthreads();
   for (int o = 1; o < 256; o <<= 1) {
@@ -224,8 +233,21 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
     __syncwarp();
   }
   __syncthreads();
+  // the tile's digit counts, their exclusive scan (local digit starts), per-warp offsets
+  int cnt = 0;
+  for (int v = 0; v < kRadixWarps; v++) cnt += woff[v][tid];
+  lsum[tid] = cnt;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    const int add = tid >= o ? lsum[tid - o] : 0;
+    __syncthreads();
+    lsum[tid] += add;
+    __syncthreads();
+  }
   {
-    int run = dstart;
+    const int lstart = lsum[tid] - cnt;
+    dglob[tid] = dstart - lstart;
+    int run = lstart;
     for (int v = 0; v < kRadixWarps; v++) {
       const int c = woff[v][tid];
       woff[v][tid] = run;
@@ -233,7 +255,7 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
     }
   }
   __syncthreads();
-  // pass 2: placement
+  // pass 2: placement in the tile's digit-sorted order
 #pragma unroll
   for (int q = 0; q < kRadixWarpRounds; q++) {
     const bool valid = id[q] >= 0;
@@ -241,12 +263,20 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
     const unsigned peers = __match_any_sync(kFull, dig);
     if (valid) {
       const int pos = woff[w][dig] + __popc(peers & lt);
-      okey[pos] = k[q];
-      oidx[pos] = id[q];
+      s_key[pos] = k[q];
+      s_idx[pos] = id[q];
     }
     __syncwarp();
     if (valid && (peers & lt) == 0u) woff[w][dig] += __popc(peers);
     __syncwarp();
+  }
+  __syncthreads();
+  // write-out: position i of the tile order goes to dglob[digit] + i
+  for (int i = tid; i < ntile; i += 256) {
+    const unsigned long long kk = s_key[i];
+    const int pos = dglob[(unsigned) (kk >> shift) & 255u] + i;
+    okey[pos] = kk;
+    oidx[pos] = s_idx[i];
   }
 }
 
@@ -1002,6 +1032,8 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
     r.hist = a.radix_hist;
     r.tot = a.radix_tot;
     const dim3 grid(r.ntiles, 3);
+    // the staged tile (48 KB) is above the default dynamic shared-memory limit
+    cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kRadixScatterSmem);
     for (int pass = 0; pass < 8; pass++) {
       for (int q = 0; q < 3; q++) {
         const bool even = (pass & 1) == 0;
@@ -1012,7 +1044,7 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
       }
       k_radix_hist<<<grid, 256, 0, st>>>(r, 8 * pass);
       k_radix_scan<<<dim3(256, 3), 1024, 0, st>>>(r);
-      k_radix_scatter<<<grid, 256, 0, st>>>(r, 8 * pass);
+      k_radix_scatter<<<grid, 256, kRadixScatterSmem, st>>>(r, 8 * pass);
       launches += 3;
     }
   }
