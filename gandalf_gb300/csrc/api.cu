@@ -101,7 +101,8 @@ struct gsph_ctx {
          *mc_bbmin = nullptr, *mc_bbmax = nullptr, *mc_hbmin = nullptr, *mc_hbmax = nullptr;
   float4* mc_meta = nullptr;
   int* heavy_leaves = nullptr;
-  int* heavy_count = nullptr;
+  int* heavy_count = nullptr;   // [0] current heavy count, [1] wide-tier count, [2] [3] snapshots
+  int* wide_leaves = nullptr;   // leaves of the mixed h solve's wide tier
   int max_leaf = 8;
   // star particles: 8 input arrays (x y z vx vy vz m h) then 7 results (a, adot, gpot)
   int nstar = 0, star_cap = 0;
@@ -322,6 +323,7 @@ int ensure_capacity(gsph_ctx* c, int n) {
       if (rc == GSPH_OK) rc = alloc(c, c->mc_meta, capc);
     }
     if (rc == GSPH_OK) rc = alloc(c, c->heavy_leaves, (capc + 1) / 2);
+    if (rc == GSPH_OK) rc = alloc(c, c->wide_leaves, (capc + 1) / 2);
     if (rc == GSPH_OK) rc = alloc(c, c->heavy_count, 4);
     if (rc != GSPH_OK) { free_all(c); return rc; }
     c->cap = capn;
@@ -691,8 +693,9 @@ int do_props(gsph_ctx* c) {
   if (mixed(c)) {
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count + 2, 0, 2 * sizeof(int), c->stream));
     c->launches += (unsigned) launch_density_mixed(t, p, make_mixed_particles(c), make_mixed_cells(c),
-                                                   make_params(c), make_counters(c), heavy, c->lpg, c->max_leaf,
-                                                   c->stream);
+                                                   make_params(c), make_counters(c), heavy,
+                                                   HeavyList{c->wide_leaves, c->heavy_count + 1}, c->lpg,
+                                                   c->max_leaf, c->stream);
   } else {
     GSPH_CUDA(cudaMemsetAsync(c->heavy_count + 2, 0, 2 * sizeof(int), c->stream));
     launch_density(t, p, make_params(c), make_counters(c), heavy, c->lpg, c->dens_next, c->dens_comp, c->stream);

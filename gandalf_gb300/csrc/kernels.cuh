@@ -53,7 +53,7 @@ struct HeavyList;
 // mixed-precision form (mixed.cu); each returns the number of kernels it launched
 int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
                          const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
-                         int lanes_per_particle, int max_leaf, cudaStream_t st);
+                         const HeavyList& wide, int lanes_per_particle, int max_leaf, cudaStream_t st);
 int launch_all_forces_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
                             const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
                             int lanes_per_particle, int max_leaf, cudaStream_t st);

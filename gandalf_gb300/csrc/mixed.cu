@@ -801,42 +801,54 @@ k_density_mixed_pp(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphPar
 }
 
 constexpr int kDensWarps = 4;
-constexpr int kCompactPerWarp = 1536;   // float2 entries shared by the warp's particle groups
+constexpr int kCompactPerWarp = 1536;   // float2 entries shared by the particle groups of a batch warp
+// The single-simulation h solve in two tiers of the same warp-per-leaf code: every leaf with
+// compact lists of kCompactNormal entries a warp (13 KB of shared memory a warp: 16 warps an
+// SM), the leaves whose lists overflow that with kCompactWide entries (17 KB: 13 warps an
+// SM); leaves that overflow both go to the per-particle heavy-leaf kernel.  The wide tier
+// has the batch kernel's capacity, so a leaf reaches the heavy-leaf kernel in a batch exactly
+// when it does in a single step, and the two give the same sums bit for bit.
+constexpr int kCompactNormal = 1024;
+constexpr int kCompactWide = kCompactPerWarp;
 
-// Per-particle compact list capacity, also the stride between the lists of the particle
-// groups of a warp: congruent to LPG modulo 16 so that the groups' reads of 8-byte entries
-// (lane sl of group g reads entry sl + LPG k) fall in distinct shared-memory banks.
-template <int LPG>
-__host__ __device__ constexpr int compact_stride() {
-  return LPG >= 16 ? kCompactPerWarp / (32 / LPG)
-                   : ((kCompactPerWarp / (32 / LPG) - LPG) / 16) * 16 + LPG;
+// Per-particle compact list capacity of a warp with cap entries, also the stride between
+// the lists of its particle groups: congruent to LPG modulo 16 so that the groups' reads
+// of 8-byte entries (lane sl of group g reads entry sl + LPG k) fall in distinct
+// shared-memory banks.
+__host__ __device__ constexpr int compact_stride(int lpg, int cap) {
+  return lpg >= 16 ? cap / (32 / lpg) : ((cap / (32 / lpg) - lpg) / 16) * 16 + lpg;
 }
 
-size_t dens_smem(int warps) {
-  return (sizeof(float2) * kCompactPerWarp + sizeof(int) * (kDensStack + kDensListNormal)) * warps;
+size_t dens_smem(int warps, int cap = kCompactPerWarp) {
+  return (sizeof(float2) * cap + sizeof(int) * (kDensStack + kDensListNormal)) * warps;
 }
 
 // One warp per block, one leaf per warp: a block's slot frees as soon as its leaf is
 // done (leaf costs vary by an order of magnitude, and warps of a larger block would wait
-// for the slowest).  Shared memory (17 KB a warp) and registers (168 a thread) allow 12
-// resident warps per SM.
+// for the slowest).  At most 128 registers a thread, so that shared memory decides the
+// warps an SM: 16 with kCompactNormal lists.  list == nullptr: leaf = block index (every
+// leaf); otherwise the leaves list[0 .. *list_count) in a block-strided loop.  Leaves whose
+// compact lists overflow cap entries go to out.
 template <int LPG>
-__global__ void __launch_bounds__(32, 12)
+__global__ void __launch_bounds__(32, 16)
 k_density_mixed(Tree t, Particles p, MixedParticles mp, MixedCells mc, SphParams prm, DeviceCounters cnt,
-                HeavyList heavy, bool handover) {
+                HeavyList out, const int* list, const int* list_count, int cap) {
   extern __shared__ float2 s_dyn2[];
   float2* s_compact = s_dyn2;
-  int* s_stack = reinterpret_cast<int*>(s_dyn2 + kCompactPerWarp);
+  int* s_stack = reinterpret_cast<int*>(s_dyn2 + cap);
   int* s_list = s_stack + kDensStack;
-  const int leaf = blockIdx.x;
-  if (leaf >= t.nleaf) return;
-  const int kcap = compact_stride<LPG>();
-  const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack, s_list,
-                                       tuned_depth(prm.gather_depth, 64, kDensListNormal), s_compact, kcap, handover,
-                                       nullptr);
-  if (!ok && (threadIdx.x & 31) == 0) {
-    const int k = atomicAdd(heavy.count, 1);
-    heavy.leaves[k] = leaf;
+  const int kcap = compact_stride(LPG, cap);
+  // every leaf: this block's leaf only (the grid covers the leaves); a list: block-strided
+  const int nl = list ? *list_count : min(t.nleaf, (int) blockIdx.x + 1);
+  for (int k = blockIdx.x; k < nl; k += gridDim.x) {
+    const int leaf = list ? list[k] : k;
+    const bool ok = density_cell<LPG, 1>(t, p, mp, mc, prm, cnt, leaf, s_stack, s_list,
+                                         tuned_depth(prm.gather_depth, 64, kDensListNormal), s_compact, kcap, true,
+                                         nullptr);
+    if (!ok && (threadIdx.x & 31) == 0) {
+      const int q = atomicAdd(out.count, 1);
+      out.leaves[q] = leaf;
+    }
   }
 }
 
@@ -1639,7 +1651,7 @@ __global__ void __launch_bounds__(kDensWarps * 32, 3) k_batch_density(BatchQueue
   int* s_stack = reinterpret_cast<int*>(s_dyn2 + kDensWarps * kCompactPerWarp);
   int* s_list = s_stack + kDensWarps * kDensStack;
   const int wib = threadIdx.x >> 5;
-  const int kcap = compact_stride<LPG>();
+  const int kcap = compact_stride(LPG, kCompactPerWarp);
   const int total = q.leaf_start[q.nsim];
   for (;;) {
     const int item = warp_take(&q.next[0]);
@@ -1688,7 +1700,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_batch_hydro(BatchQueue q) 
 }
 
 template <int LPG, bool REC>
-__global__ void __launch_bounds__(kForceWarps * 32) k_batch_forces(BatchQueue q) {
+__global__ void __launch_bounds__(kForceWarps * 32, 5) k_batch_forces(BatchQueue q) {
   __shared__ int s_stack[kForceWarps][kFStack];
   __shared__ int s_a[kForceWarps][kFListA];
   __shared__ int s_b[kForceWarps][kFListB];
@@ -1783,15 +1795,20 @@ void set_wide_smem(bool batch, size_t smem) {
 
 int launch_density_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
                          const SphParams& prm, const DeviceCounters& cnt, const HeavyList& heavy,
-                         int lanes_per_particle, int max_leaf, cudaStream_t st) {
+                         const HeavyList& wide, int lanes_per_particle, int max_leaf, cudaStream_t st) {
   cudaMemsetAsync(heavy.count, 0, sizeof(int), st);
-  const size_t smem_n = dens_smem(1);
+  cudaMemsetAsync(wide.count, 0, sizeof(int), st);
   (void) max_leaf;
-  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, t.nleaf, 32, smem_n, t, p, mp, mc, prm, cnt, heavy, true)
+  // every leaf, normal lists; overflowing leaves to the wide tier
+  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, t.nleaf, 32, dens_smem(1, kCompactNormal), t, p, mp, mc, prm,
+                 cnt, wide, (const int*) nullptr, (const int*) nullptr, kCompactNormal)
+  // the wide tier's leaves (a persistent grid of 13 warps an SM), overflow to the heavy kernel
+  GSPH_MIXED_LPG(k_density_mixed, lanes_per_particle, 13 * 152, 32, dens_smem(1, kCompactWide), t, p, mp, mc, prm,
+                 cnt, heavy, wide.leaves, wide.count, kCompactWide)
   // 41 KB of shared memory a block: up to 5 blocks an SM; 4 per SM keep the heavy leaves
   // (a few percent of all) spread over every SM
   GSPH_MIXED_LPG(k_density_mixed_pp, lanes_per_particle, 4 * 152, 256, 0, t, p, mp, mc, prm, cnt, heavy)
-  return 2;
+  return 3;
 }
 
 int launch_all_forces_mixed(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
@@ -1843,12 +1860,12 @@ int launch_batch_forces(const BatchQueue& q, bool gravity, int lpg, cudaStream_t
   }
   const size_t smem = sizeof(int) * 8 * (kFStack + kWListA + kWListB + kWListC) + sizeof(ForceSmem);
   if (q.record) {
-    GSPH_MIXED_LPG_REC(k_batch_forces, true, lpg, 152 * 4, kForceWarps * 32, 0, q)
+    GSPH_MIXED_LPG_REC(k_batch_forces, true, lpg, 152 * 5, kForceWarps * 32, 0, q)
     k_batch_heavy_prefix<<<1, 32, 0, st>>>(q);
     set_wide_smem<true>(true, smem);
     GSPH_MIXED_LPG_REC(k_batch_forces_wide, true, lpg, 152 * 2, 256, smem, q)
   } else {
-    GSPH_MIXED_LPG_REC(k_batch_forces, false, lpg, 152 * 4, kForceWarps * 32, 0, q)
+    GSPH_MIXED_LPG_REC(k_batch_forces, false, lpg, 152 * 5, kForceWarps * 32, 0, q)
     k_batch_heavy_prefix<<<1, 32, 0, st>>>(q);
     set_wide_smem<false>(true, smem);
     GSPH_MIXED_LPG_REC(k_batch_forces_wide, false, lpg, 152 * 2, 256, smem, q)
