@@ -116,7 +116,7 @@ struct gsph_ctx {
   KdkParams kp{};
   KdkGlobal* kg = nullptr;
   double* kdk_buf = nullptr;          // r0 v0 a0 (9), u0 dudt0 dt dt_next tlast (5), keep (17): x cap
-  int* kdk_ibuf = nullptr;            // nlast nstep level levelneib: x cap
+  int* kdk_ibuf = nullptr;            // nlast nstep level levelneib bt_list: x cap
   unsigned char* kdk_flags = nullptr;
   unsigned char* leaf_active = nullptr;
   int *leaf_level = nullptr, *leaf_lvn = nullptr;
@@ -1969,7 +1969,7 @@ int ensure_kdk_buffers(gsph_ctx* c) {
   GSPH_CUDA(cudaMalloc(&c->kg, sizeof(KdkGlobal)));
   GSPH_CUDA(cudaMemsetAsync(c->kg, 0, sizeof(KdkGlobal), c->stream));
   GSPH_CUDA(cudaMalloc(&c->kdk_buf, sizeof(double) * (14 + kKeep) * k2));
-  GSPH_CUDA(cudaMalloc(&c->kdk_ibuf, sizeof(int) * 4 * k2));
+  GSPH_CUDA(cudaMalloc(&c->kdk_ibuf, sizeof(int) * 5 * k2));
   GSPH_CUDA(cudaMalloc(&c->kdk_flags, k2));
   GSPH_CUDA(cudaMalloc(&c->leaf_active, k2));
   GSPH_CUDA(cudaMalloc(&c->leaf_level, sizeof(int) * k2));
@@ -1999,7 +1999,7 @@ KdkState make_kdk_state(gsph_ctx* c) {
   s.u0 = b + 9 * k; s.dudt0 = b + 10 * k; s.dt = b + 11 * k; s.dt_next = b + 12 * k; s.tlast = b + 13 * k;
   for (int q = 0; q < kKeep; q++) s.keep[q] = b + (14 + q) * k;
   int* ib = c->kdk_ibuf;
-  s.nlast = ib; s.nstep = ib + k; s.level = ib + 2 * k; s.levelneib = ib + 3 * k;
+  s.nlast = ib; s.nstep = ib + k; s.level = ib + 2 * k; s.levelneib = ib + 3 * k; s.bt_list = ib + 4 * k;
   s.flags = c->kdk_flags;
   return s;
 }
@@ -2183,7 +2183,7 @@ int kdk_step_body(gsph_ctx* c, int step) {
   c->launches += 1;
   launch_kdk_timesteps(s, c->kp, c->kg, c->stream);
   launch_kdk_end(s, c->kp, c->kg, c->stream);
-  c->launches += 5;
+  c->launches += 6;
   return check_launch(c, "kdk step");
 }
 

@@ -203,20 +203,52 @@ __global__ void k_kdk_check_final(KdkGlobal* g) {
 __global__ void k_bt_prepare(KdkGlobal* g) {
   if (threadIdx.x | blockIdx.x) return;
   g->resync = g->n == g->nresync;
+  g->bt_count = 0;
   g->dtmin_bits = dbits(9.9e99);
   g->level_max_new = 0;
   g->nfactor_up = g->nfactor_down = 0;
 }
 
-// Phase A: timesteps of the particles that start a new step (all of them when resyncing).
+// Phase A: the particles that start a new step (all of them when resyncing) go to a list;
+// the levels of the others enter the level_max reduction.  The fp64 timesteps are computed
+// over the list (k_bt_a2): GB300 charges an fp64 instruction per warp whatever its active
+// lanes, and the particles ending a step are scattered over input order, so computing them
+// in place made nearly every warp pay for two divisions, two square roots and a logarithm.
 __global__ void k_bt_a(KdkState s, KdkParams kp, KdkGlobal* g) {
   const bool resync = g->resync;
-  const int n = g->n, level_step = g->level_step;
+  const int n = g->n;
+  const int lane = threadIdx.x & 31;
+  int lmax = 0;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < s.n; base += stride) {
+    const int i = base + lane;
+    bool need = false;
+    if (i < s.n && (resync || kp.nlevels > 1)) {
+      if (resync || n - s.nlast[i] == s.nstep[i]) need = true;
+      else lmax = max(lmax, s.level[i]);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      int at = 0;
+      if (lane == 0) at = atomicAdd(&g->bt_count, __popc(m));
+      at = __shfl_sync(0xffffffffu, at, 0);
+      if (need) s.bt_list[at + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  if (lane == 0 && lmax > 0) atomicMax(&g->level_max_new, lmax);
+}
+
+// Phase A, listed particles: new timesteps and levels (the list order does not matter: each
+// particle's update is its own, and the reductions are a minimum and a maximum).
+__global__ void k_bt_a2(KdkState s, KdkParams kp, KdkGlobal* g) {
+  const bool resync = g->resync;
+  const int n = g->n, level_step = g->level_step, count = g->bt_count;
   const double dt_max = g->dt_max, timestep = g->timestep;
   unsigned long long mbits = dbits(9.9e99);
   int lmax = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x) {
-    if (kp.nlevels == 1 && !resync) continue;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    const int i = s.bt_list[k];
     if (resync) {
       const double dt = particle_timestep(s, kp, i, &g->status);
       s.dt_next[i] = dt;
@@ -224,8 +256,8 @@ __global__ void k_bt_a(KdkState s, KdkParams kp, KdkGlobal* g) {
       if (b < mbits) mbits = b;
       continue;
     }
-    const int dn = n - s.nlast[i];
-    if (dn == s.nstep[i] && s.nstep[i] != pow2i(level_step - s.level[i])) {
+    // n - nlast == nstep here (the listing condition)
+    if (s.nstep[i] != pow2i(level_step - s.level[i])) {
       // timestep reduced by CheckTimesteps (Saitoh & Makino)
       const double dt = particle_timestep(s, kp, i, &g->status);
       const int level = max(timestep_level(dt, dt_max), s.levelneib[i] - kp.level_diff_max);
@@ -235,7 +267,7 @@ __global__ void k_bt_a(KdkState s, KdkParams kp, KdkGlobal* g) {
       s.nstep[i] = pow2i(level_step - s.level[i]);
       s.dt_next[i] = __dmul_rn((double) s.nstep[i], timestep);
       s.flags[i] |= kFlagEndStep;
-    } else if (dn == s.nstep[i]) {
+    } else {
       const int nstep = s.nstep[i], last_level = s.level[i];
       const double dt = particle_timestep(s, kp, i, &g->status);
       const int level = max(timestep_level(dt, dt_max), s.levelneib[i] - kp.level_diff_max);
@@ -467,6 +499,7 @@ void launch_kdk_check(const KdkState& s, const KdkParams& kp, KdkGlobal* g, bool
 void launch_kdk_timesteps(const KdkState& s, const KdkParams& kp, KdkGlobal* g, cudaStream_t st) {
   k_bt_prepare<<<1, 32, 0, st>>>(g);
   k_bt_a<<<grid_for(s.n), 256, 0, st>>>(s, kp, g);
+  k_bt_a2<<<grid_for(s.n), 256, 0, st>>>(s, kp, g);
   k_bt_b<<<1, 32, 0, st>>>(kp, g);
   k_bt_c<<<grid_for(s.n), 256, 0, st>>>(s, kp, g);
 }

@@ -17,6 +17,7 @@ struct KdkGlobal {
   int level_max_new;          // reduction: largest particle level
   int nfactor_up, nfactor_down;
   int resync;                 // the last block-timestep call took the resynchronisation branch
+  int bt_count;               // particles listed for a new timestep (KdkState::bt_list)
   unsigned status;            // KdkStatus bits
   double t, timestep, dt_max, timestep_old;
   unsigned long long dtmin_bits;     // atomicMin over the bits of positive doubles
@@ -47,6 +48,7 @@ struct KdkState {
   double *u0, *dudt0, *dt, *dt_next, *tlast;
   int *nlast, *nstep, *level, *levelneib;
   unsigned char* flags;                        // kFlagActive | kFlagEndStep
+  int* bt_list;                                // particles whose timestep is computed this step
   double* keep[kKeep];
 };
 constexpr unsigned char kFlagActive = 1, kFlagEndStep = 2;

@@ -486,12 +486,15 @@ __device__ __forceinline__ unsigned long long lb_word(unsigned epoch, unsigned f
   return ((unsigned long long) epoch << 34) | ((unsigned long long) flag << 32) | (unsigned long long) v;
 }
 
-__global__ void __launch_bounds__(1024) k_part_level(int l, int n, BuildLists cur, BuildLists nxt,
-                                                     const unsigned char* __restrict__ side,
-                                                     unsigned char* side_next,
-                                                     const unsigned char* __restrict__ seg_axis_next,
-                                                     const int* __restrict__ heap_ones_before, int nb,
-                                                     PartitionState ps) {
+constexpr int kPartThreads = 512, kPartPer = 8;
+constexpr int kPartTile = kPartThreads * kPartPer;   // positions per tile
+
+__global__ void __launch_bounds__(kPartThreads) k_part_level(int l, int n, BuildLists cur, BuildLists nxt,
+                                                             const unsigned char* __restrict__ side,
+                                                             unsigned char* side_next,
+                                                             const unsigned char* __restrict__ seg_axis_next,
+                                                             const int* __restrict__ heap_ones_before, int nb,
+                                                             PartitionState ps) {
   __shared__ int ws[33];
   __shared__ unsigned s_ticket, s_epoch;
   __shared__ int s_before;
@@ -508,66 +511,85 @@ __global__ void __launch_bounds__(1024) k_part_level(int l, int n, BuildLists cu
   // tickets run over the three axes' tiles interleaved, each axis's tiles in order
   const int a = (int) ticket % 3, b = (int) ticket / 3;
   unsigned long long* words = ps.tiles + (size_t) a * nb;
-  const int base = b * kScanBlock;
-  const int j0 = base + 2 * threadIdx.x, j1 = j0 + 1;
   const int* src = pick3(cur.l, a);
   int* dst = pick3(nxt.l, a);
-  const int id0 = j0 < n ? src[j0] : -1;
-  const int id1 = j1 < n ? src[j1] : -1;
-  const int f0 = id0 >= 0 ? side[id0] : 0;
-  const int f1 = id1 >= 0 ? side[id1] : 0;
+  // kPartPer consecutive positions a thread
+  const int j0 = b * kPartTile + threadIdx.x * kPartPer;
+  int ids[kPartPer], f[kPartPer];
+  int mine = 0;
+#pragma unroll
+  for (int q = 0; q < kPartPer; q++) ids[q] = j0 + q < n ? src[j0 + q] : -1;
+#pragma unroll
+  for (int q = 0; q < kPartPer; q++) {
+    f[q] = ids[q] >= 0 ? side[ids[q]] : 0;
+    mine += f[q];
+  }
   int count;
-  const int ex = block_exscan(f0 + f1, ws, count);
-  if (threadIdx.x == 0) {
+  const int ex = block_exscan(mine, ws, count);
+  // decoupled look-back by warp 0: 32 earlier tiles a probe, summed back to the nearest
+  // inclusive prefix
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    unsigned before = 0;
     if (b == 0) {
-      atomicExch(words, lb_word(epoch, kLbPrefix, (unsigned) count));
-      s_before = 0;
+      if (lane == 0) atomicExch(words, lb_word(epoch, kLbPrefix, (unsigned) count));
     } else {
-      atomicExch(words + b, lb_word(epoch, kLbAggregate, (unsigned) count));
-      unsigned before = 0;
+      if (lane == 0) atomicExch(words + b, lb_word(epoch, kLbAggregate, (unsigned) count));
       int i = b - 1, spins = 0;
-      while (i >= 0) {
-        const unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(words + i);
-        const unsigned flag = (unsigned) (w >> 32) & 3u;
-        if ((unsigned) (w >> 34) == epoch && flag != 0u) {
-          before += (unsigned) w;
-          if (flag == kLbPrefix) break;
-          i--;
-          spins = 0;
+      for (;;) {
+        const int k = i - lane;
+        unsigned flag = kLbPrefix, v = 0;   // before tile 0: an empty prefix
+        if (k >= 0) {
+          const unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(words + k);
+          flag = (unsigned) (w >> 34) == epoch ? (unsigned) (w >> 32) & 3u : 0u;
+          v = (unsigned) w;
+        }
+        if (__any_sync(kFull, flag == 0u)) {   // some earlier tile has not published yet
+          if (++spins > kLbSpinLimit) {
+            if (lane == 0) atomicOr(ps.status, (unsigned) kStatusPartitionWait);
+            break;
+          }
+          __nanosleep(32);
           continue;
         }
-        if (++spins > kLbSpinLimit) {
-          atomicOr(ps.status, (unsigned) kStatusPartitionWait);
-          break;
-        }
-        __nanosleep(32);
+        const unsigned pm = __ballot_sync(kFull, flag == kLbPrefix);
+        const int stop = pm ? __ffs(pm) - 1 : 31;   // the nearest inclusive prefix
+        before += __reduce_add_sync(kFull, lane <= stop ? v : 0u);
+        if (pm) break;
+        i -= 32;
+        spins = 0;
       }
-      atomicExch(words + b, lb_word(epoch, kLbPrefix, before + (unsigned) count));
-      s_before = (int) before;
+      if (lane == 0) atomicExch(words + b, lb_word(epoch, kLbPrefix, before + (unsigned) count));
     }
-    if ((int) ticket == total - 1) {
-      // every block has its ticket (and has read the epoch before taking it)
-      atomicExch(ps.ticket, 0u);
-      atomicAdd(ps.epoch, 1u);
+    if (lane == 0) {
+      s_before = (int) before;
+      if ((int) ticket == total - 1) {
+        // every block has its ticket (and has read the epoch before taking it)
+        atomicExch(ps.ticket, 0u);
+        atomicAdd(ps.epoch, 1u);
+      }
     }
   }
   __syncthreads();
-  const int ones_before_tile = s_before;
   const int nseg = 1 << l;
-  auto place = [&](int j, int id, int f, int e) {
-    if (id < 0) return;
-    int first, cnt;
-    const int s = seg_of(j, n, l, first, cnt);
-    const int ones = e - heap_ones_before[nseg - 1 + s];   // ones before j inside the segment
-    const int half = cnt >> 1;
-    int pos, cfirst, ccnt;
-    if (f) { pos = first + half + ones; cfirst = first + half; ccnt = cnt - half; }
-    else { pos = first + (j - first) - ones; cfirst = first; ccnt = half; }
-    dst[pos] = id;
-    if (side_next && seg_axis_next[2 * s + f] == a) side_next[id] = (unsigned char) (pos - cfirst >= (ccnt >> 1));
-  };
-  place(j0, id0, f0, ones_before_tile + ex);
-  place(j1, id1, f1, ones_before_tile + ex + f0);
+  int e = s_before + ex;   // ones before this thread's first position, over the whole list
+#pragma unroll
+  for (int q = 0; q < kPartPer; q++) {
+    const int j = j0 + q, id = ids[q];
+    if (id >= 0) {
+      int first, cnt;
+      const int s2 = seg_of(j, n, l, first, cnt);
+      const int ones = e - heap_ones_before[nseg - 1 + s2];   // ones before j inside the segment
+      const int half = cnt >> 1;
+      int pos, cfirst, ccnt;
+      if (f[q]) { pos = first + half + ones; cfirst = first + half; ccnt = cnt - half; }
+      else { pos = first + (j - first) - ones; cfirst = first; ccnt = half; }
+      dst[pos] = id;
+      if (side_next && seg_axis_next[2 * s2 + f[q]] == a)
+        side_next[id] = (unsigned char) (pos - cfirst >= (ccnt >> 1));
+    }
+    e += f[q];
+  }
 }
 
 // ---- the deep levels of a segment in shared memory ---------------------------------------
@@ -1050,7 +1072,7 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
   }
   BuildLists cur, nxt;
   for (int q = 0; q < 3; q++) { cur.l[q] = a.sort.idx[q]; nxt.l[q] = a.lists_b[q]; }
-  const int nb = partition_blocks(n);
+  const int nbl = (n + kPartTile - 1) / kPartTile;   // tiles of the level partition
   // levels from L0 on run in shared memory, one block per segment of level L0
   int L0 = 0;
   while (L0 < a.ltot && ((n + (1 << L0) - 1) >> L0) > kDeepMax) L0++;
@@ -1065,8 +1087,9 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
       k_mark_side<<<grid_for(n, 256), 256, 0, st>>>(l, n, cur, a.seg_axis, side);
       launches += 1;
     }
-    k_part_level<<<3 * nb, 1024, 0, st>>>(l, n, cur, nxt, side, l + 1 < L0 ? a.side[(l + 1) & 1] : nullptr,
-                                          a.seg_axis_next, a.heap_ones_before, nb, a.part);
+    k_part_level<<<3 * nbl, kPartThreads, 0, st>>>(l, n, cur, nxt, side,
+                                                  l + 1 < L0 ? a.side[(l + 1) & 1] : nullptr, a.seg_axis_next,
+                                                  a.heap_ones_before, nbl, a.part);
     launches += 1;
     BuildLists tmp = cur; cur = nxt; nxt = tmp;
   }
