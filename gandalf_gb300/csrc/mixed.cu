@@ -70,14 +70,16 @@ __global__ void k_prep_build_cells(Tree t, MixedCells mc) {
   }
 }
 
+// The float quotients 1/h, 1/rho and P Omega^-1 / rho^2 are formed from the float values
+// (correctly rounded reciprocals; within an ulp or two of the rounded fp64 quotients): fp64
+// divisions would hold GB300's fp64 pipe for 64 cycles a warp instruction each.
 __global__ void k_prep_hydro_particles(Particles p, MixedParticles mp) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < p.n; s += gridDim.x * blockDim.x) {
-    const double h = p.h[s], rho = p.rho[s];
-    mp.vel[s] = make_float4(__double2float_rn(p.vx[s]), __double2float_rn(p.vy[s]), __double2float_rn(p.vz[s]),
-                            __double2float_rn(h));
-    const double fac = (p.pressure[s] * p.invomega[s]) / (rho * rho);
-    mp.hyd[s] = make_float4(__double2float_rn(1.0 / h), __double2float_rn(fac), __double2float_rn(1.0 / rho),
-                            __double2float_rn(p.sound[s]));
+    const float hf = __double2float_rn(p.h[s]), rf = __double2float_rn(p.rho[s]);
+    mp.vel[s] = make_float4(__double2float_rn(p.vx[s]), __double2float_rn(p.vy[s]), __double2float_rn(p.vz[s]), hf);
+    const float ir = __frcp_rn(rf);
+    const float fac = __double2float_rn(p.pressure[s]) * __double2float_rn(p.invomega[s]) * ir * ir;
+    mp.hyd[s] = make_float4(__frcp_rn(hf), fac, ir, __double2float_rn(p.sound[s]));
     mp.aux[s] = make_float4(__double2float_rn(p.hfactor[s]), __double2float_rn(p.zeta[s]),
                             __double2float_rn(p.hrangesqd[s]), 0.0f);
     mp.pos_lo[s].w = __double2float_rn(p.hrangesqd[s]);   // the neighbour test's candidate load
