@@ -151,27 +151,51 @@ __global__ void __launch_bounds__(256) k_radix_hist(RadixArgs r, int shift) {
 }
 
 // Exclusive prefix over the tiles of one digit; the digit's total goes to tot.
+__device__ __forceinline__ int block_exscan(int v, int* ws, int& total);
+
 __global__ void __launch_bounds__(1024) k_radix_scan(RadixArgs r) {
-  __shared__ int part[1024];
+  __shared__ int ws[33];
   const int a = blockIdx.y, d = blockIdx.x;
   int* h = r.hist + ((size_t) a * 256 + d) * r.ntiles;
   int carry = 0;
   for (int c0 = 0; c0 < r.ntiles; c0 += 1024) {
     const int i = c0 + threadIdx.x;
     const int v = i < r.ntiles ? h[i] : 0;
-    part[threadIdx.x] = v;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-      const int add = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
-      __syncthreads();
-      part[threadIdx.x] += add;
-      __syncthreads();
-    }
-    if (i < r.ntiles) h[i] = carry + part[threadIdx.x] - v;
-    carry += part[1023];
-    __syncthreads();
+    int total;
+    const int ex = block_exscan(v, ws, total);   // warp shuffles, three barriers
+    if (i < r.ntiles) h[i] = carry + ex;
+    carry += total;
   }
   if (threadIdx.x == 0) r.tot[a * 256 + d] = carry;
+}
+
+// Lanes of the warp holding the same 8-bit digit as this lane (valid lanes only): eight
+// ballots, one per digit bit (a warp match waits on the MIO pipe: 24 short-scoreboard
+// stalls per issued instruction in this kernel).
+__device__ __forceinline__ unsigned digit_peers(unsigned dig, bool valid) {
+  unsigned peers = __ballot_sync(kFull, valid);
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    const bool on = (dig >> b) & 1u;
+    const unsigned m = __ballot_sync(kFull, on);
+    peers &= on ? m : ~m;
+  }
+  return peers;
+}
+
+// Inclusive scan of one int per thread over a 256-thread block (warp shuffles, two barriers).
+__device__ __forceinline__ int scan256_inclusive(int v, int* wsum) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, v, o);
+    if (lane >= o) v += y;
+  }
+  if (lane == 31) wsum[w] = v;
+  __syncthreads();
+  int add = 0;
+  for (int q = 0; q < w; q++) add += wsum[q];
+  __syncthreads();
+  return v + add;
 }
 
 // Stable scatter of one tile: warp w owns the tile's elements [w * 512, (w + 1) * 512) in
@@ -192,7 +216,7 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
   extern __shared__ unsigned long long s_key[];             // kRadixTile keys, then kRadixTile indices
   int* s_idx = reinterpret_cast<int*>(s_key + kRadixTile);
   __shared__ int woff[kRadixWarps][256];   // per-warp digit counts, then offsets in the tile order
-  __shared__ int tsum[256], lsum[256];
+  __shared__ int wsum[kRadixWarps];
   __shared__ int dglob[256];                // output position of the tile's first element of each digit
   const int a = blockIdx.y, b = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -205,30 +229,16 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
   const int tile0 = b * kRadixTile;
   const int ntile = min(kRadixTile, r.n - tile0);
   const int base = tile0 + w * kRadixPerWarp + lane;
-  unsigned long long k[kRadixWarpRounds];
-  int id[kRadixWarpRounds];
-#pragma unroll
+  // exclusive scan of the digit totals (over all tiles)
+  const int tot = r.tot[a * 256 + tid];
+  const int dstart = scan256_inclusive(tot, wsum) - tot + r.hist[((size_t) a * 256 + tid) * r.ntiles + b];
+  // pass 1: per-warp digit counts (the keys are read again in pass 2, from L2)
+#pragma unroll 2
   for (int q = 0; q < kRadixWarpRounds; q++) {
     const int i = base + 32 * q;
-    k[q] = i < r.n ? key[i] : 0ull;
-    id[q] = i < r.n ? idx[i] : -1;
-  }
-  // exclusive scan of the digit totals (over all tiles)
-  tsum[tid] = r.tot[a * 256 + tid];
-  __syncthreads();
-  for (int o = 1; o < 256; o <<= 1) {
-    const int add = tid >= o ? tsum[tid - o] : 0;
-    __syncthreads();
-    tsum[tid] += add;
-    __syncthreads();
-  }
-  const int dstart = tsum[tid] - r.tot[a * 256 + tid] + r.hist[((size_t) a * 256 + tid) * r.ntiles + b];
-  // pass 1: per-warp digit counts
-#pragma unroll
-  for (int q = 0; q < kRadixWarpRounds; q++) {
-    const bool valid = id[q] >= 0;
-    const unsigned dig = valid ? (unsigned) (k[q] >> shift) & 255u : 256u + (unsigned) lane;
-    const unsigned peers = __match_any_sync(kFull, dig);
+    const bool valid = i < r.n;
+    const unsigned dig = valid ? (unsigned) (key[i] >> shift) & 255u : 0u;
+    const unsigned peers = digit_peers(dig, valid);
     if (valid && (peers & lt) == 0u) woff[w][dig] += __popc(peers);
     __syncwarp();
   }
@@ -236,16 +246,8 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
   // the tile's digit counts, their exclusive scan (local digit starts), per-warp offsets
   int cnt = 0;
   for (int v = 0; v < kRadixWarps; v++) cnt += woff[v][tid];
-  lsum[tid] = cnt;
-  __syncthreads();
-  for (int o = 1; o < 256; o <<= 1) {
-    const int add = tid >= o ? lsum[tid - o] : 0;
-    __syncthreads();
-    lsum[tid] += add;
-    __syncthreads();
-  }
   {
-    const int lstart = lsum[tid] - cnt;
+    const int lstart = scan256_inclusive(cnt, wsum) - cnt;
     dglob[tid] = dstart - lstart;
     int run = lstart;
     for (int v = 0; v < kRadixWarps; v++) {
@@ -258,13 +260,15 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
   // pass 2: placement in the tile's digit-sorted order
 #pragma unroll
   for (int q = 0; q < kRadixWarpRounds; q++) {
-    const bool valid = id[q] >= 0;
-    const unsigned dig = valid ? (unsigned) (k[q] >> shift) & 255u : 256u + (unsigned) lane;
-    const unsigned peers = __match_any_sync(kFull, dig);
+    const int i = base + 32 * q;
+    const bool valid = i < r.n;
+    const unsigned long long kk = valid ? key[i] : 0ull;
+    const unsigned dig = (unsigned) (kk >> shift) & 255u;
+    const unsigned peers = digit_peers(dig, valid);
     if (valid) {
       const int pos = woff[w][dig] + __popc(peers & lt);
-      s_key[pos] = k[q];
-      s_idx[pos] = id[q];
+      s_key[pos] = kk;
+      s_idx[pos] = idx[i];
     }
     __syncwarp();
     if (valid && (peers & lt) == 0u) woff[w][dig] += __popc(peers);
@@ -277,6 +281,40 @@ __global__ void __launch_bounds__(256) k_radix_scatter(RadixArgs r, int shift) {
     const int pos = dglob[(unsigned) (kk >> shift) & 255u] + i;
     okey[pos] = kk;
     oidx[pos] = s_idx[i];
+  }
+}
+
+// The radix passes sort on the top kRadixSkipBits.. bits of the keys only (six byte passes
+// instead of eight); elements whose keys agree in those bits keep their index order, and
+// this pass puts each run of such elements into (full key, index) order.  For coordinates
+// the runs are rare (a few per axis among a million random positions) and short; equal full
+// keys (lattice positions) are already in index order and cost one comparison each.
+constexpr int kRadixSkipBits = 16;
+
+__global__ void k_radix_fixup(SortArrays s, int n) {
+  const int a = blockIdx.y;
+  unsigned long long* key = pick3(s.key, a);
+  int* idx = pick3(s.idx, a);
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const unsigned long long hj = key[j] >> kRadixSkipBits;
+    // a run starts at j when it differs from its left neighbour and equals its right one
+    if (j > 0 && (key[j - 1] >> kRadixSkipBits) == hj) continue;
+    if (j + 1 >= n || (key[j + 1] >> kRadixSkipBits) != hj) continue;
+    int end = j + 1;
+    while (end < n && (key[end] >> kRadixSkipBits) == hj) end++;
+    // insertion sort of [j, end) by (key, index)
+    for (int q = j + 1; q < end; q++) {
+      const unsigned long long kq = key[q];
+      const int iq = idx[q];
+      int r = q - 1;
+      while (r >= j && key_gt(key[r], idx[r], kq, iq)) {
+        key[r + 1] = key[r];
+        idx[r + 1] = idx[r];
+        r--;
+      }
+      key[r + 1] = kq;
+      idx[r + 1] = iq;
+    }
   }
 }
 
@@ -1064,7 +1102,9 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
     const dim3 grid(r.ntiles, 3);
     // the staged tile (48 KB) is above the default dynamic shared-memory limit
     cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kRadixScatterSmem);
-    for (int pass = 0; pass < 8; pass++) {
+    constexpr int kPasses = (64 - kRadixSkipBits) / 8;   // an even count: ends in the sort arrays
+    static_assert(kPasses % 2 == 0, "the radix passes must end in the sort arrays");
+    for (int pass = 0; pass < kPasses; pass++) {
       for (int q = 0; q < 3; q++) {
         const bool even = (pass & 1) == 0;
         r.src_key[q] = even ? a.sort.key[q] : a.key2[q];
@@ -1072,11 +1112,14 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
         r.dst_key[q] = even ? a.key2[q] : a.sort.key[q];
         r.dst_idx[q] = even ? a.lists_b[q] : a.sort.idx[q];
       }
-      k_radix_hist<<<grid, 256, 0, st>>>(r, 8 * pass);
+      const int shift = kRadixSkipBits + 8 * pass;
+      k_radix_hist<<<grid, 256, 0, st>>>(r, shift);
       k_radix_scan<<<dim3(256, 3), 1024, 0, st>>>(r);
-      k_radix_scatter<<<grid, 256, kRadixScatterSmem, st>>>(r, 8 * pass);
+      k_radix_scatter<<<grid, 256, kRadixScatterSmem, st>>>(r, shift);
       launches += 3;
     }
+    k_radix_fixup<<<dim3(grid_for(n, 256), 3), 256, 0, st>>>(a.sort, n);
+    launches += 1;
   }
   BuildLists cur, nxt;
   for (int q = 0; q < 3; q++) { cur.l[q] = a.sort.idx[q]; nxt.l[q] = a.lists_b[q]; }

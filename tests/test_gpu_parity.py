@@ -94,6 +94,24 @@ def test_gpu_plummer_vs_oracle(n):
     compare_with_oracle(c, c["params"], gravity=True)
 
 
+def test_gpu_tree_near_tie_coordinates_vs_oracle():
+    """x and y of groups of particles agree in all but the lowest mantissa bits (the
+    presort orders the top 48 bits of the coordinate keys by radix passes and then puts
+    each run of equal top bits into full-key order): tree, lists and values against the
+    oracle.  Offsets within a group are distinct, so no two coordinates are equal."""
+    c = ics_mod.plummer_sphere(4099, seed=321)
+    rng = np.random.default_rng(5)
+    for k in ("x", "y"):
+        g = np.linspace(-1.0, 1.0, 64)[rng.integers(0, 64, len(c[k]))]
+        off = np.zeros(len(g), dtype=np.int64)
+        for v in np.unique(g):
+            sel = np.flatnonzero(g == v)
+            off[sel] = rng.permutation(len(sel))
+        c[k] = (g.view(np.int64) + off).view(np.float64)
+        assert len(np.unique(c[k])) == len(g)
+    compare_with_oracle(c, c["params"], gravity=True)
+
+
 @pytest.mark.parametrize("n", [5, 9, 100])
 def test_gpu_tiny_open_sets(n):
     """Tiny sets: a single-leaf tree and leaves with one particle."""
