@@ -266,6 +266,8 @@ void make_shape(int n, int ltot, Shape& s) {
 int ensure_capacity(gsph_ctx* c, int n) {
   const int ltot = tree_levels(n, c->cfg.nleafmax);
   if (ltot > 23) return fail(c, GSPH_ERR_UNSUPPORTED, "tree deeper than 23 levels");
+  if (c->cfg.precision == GSPH_PRECISION_MIXED && n > mixed_max_particles())
+    return fail(c, GSPH_ERR_UNSUPPORTED, "the mixed form takes at most 2^27 particles");
   const int ncell = 2 * (1 << ltot) - 1;
   const int P = sort_padded_size(n);
   bool fresh = false;
@@ -396,6 +398,9 @@ SphParams make_params(const gsph_ctx* c) {
   p.eos = cfg.eos; p.periodic = cfg.periodic; p.multipole = cfg.multipole; p.self_gravity = cfg.self_gravity;
   p.compensated = cfg.precision == GSPH_PRECISION_MIXED && cfg.compensated ? 1 : 0;
   p.near_depth = c->near_depth; p.cell_depth = c->cell_depth; p.gather_depth = c->gather_depth;
+  p.alpha_visc_f = (float) cfg.alpha_visc;
+  p.ab_visc_f = (float) (cfg.beta_visc * cfg.alpha_visc);
+  p.gm1_f = (float) (cfg.gamma_eos - 1.0);
   return p;
 }
 

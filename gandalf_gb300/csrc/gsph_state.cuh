@@ -27,6 +27,10 @@ struct SphParams {
   // multipole-list depth consumed per flush, and the density gather-list depth before a
   // leaf goes to the per-particle kernel.
   int near_depth, cell_depth, gather_depth;
+  // float roundings of alpha_visc, beta_visc * alpha_visc and gamma - 1 for the mixed pair
+  // loops, formed on the host: on the device each would be an fp64 multiply or conversion
+  // per pair, and GB300 charges an fp64 instruction per warp at 1/64 of the fp32 rate
+  float alpha_visc_f, ab_visc_f, gm1_f;
   StarSet stars;    // n = 0: no stars
 };
 

@@ -30,6 +30,18 @@ constexpr float kMargin = 6.103515625e-05f;   // 2^-14 relative
 constexpr int kNodeBits = 25;
 constexpr int kNoShift = 13;
 
+// A leaf of the force walk's near and direct-sum lists as one word: its first slot and
+// particle count, (first << 5) | (n - 1), taken from the walk's own cell load, so that the
+// list consumers read no cell arrays (leaves hold 1..32 particles; the mixed form takes up
+// to 2^27 particles).
+constexpr int kLeafCountBits = 5;
+constexpr int kMixedMaxParticles = 1 << (32 - kLeafCountBits);
+__device__ __forceinline__ unsigned pack_leaf(int first, int n) {
+  return ((unsigned) first << kLeafCountBits) | (unsigned) (n - 1);
+}
+__device__ __forceinline__ int leaf_first(unsigned w) { return (int) (w >> kLeafCountBits); }
+__device__ __forceinline__ int leaf_count(unsigned w) { return (int) (w & ((1u << kLeafCountBits) - 1u)) + 1; }
+
 // ---- preparation --------------------------------------------------------------------
 __device__ __forceinline__ void split2(double v, float& hi, float& lo) {
   hi = __double2float_rn(v);
@@ -57,7 +69,7 @@ __global__ void k_prep_build_cells(Tree t, MixedCells mc) {
     mc.geo_hi[c] = make_float4(h[0], h[1], h[2], __double2float_rn(g.rmax));
     mc.geo_lo[c] = make_float4(l[0], l[1], l[2], __double2float_rn(g.hmax));
     mc.meta[c] = make_float4(__double2float_rn(g.cdistsqd), __int_as_float(t.cell_n[c]),
-                             __int_as_float((int) t.cell_level[c]), 0.0f);
+                             __int_as_float((int) t.cell_level[c]), __int_as_float(t.cell_first[c]));
     for (int k = 0; k < 3; k++) split2(m.r[k], h[k], l[k]);
     mc.com_hi[c] = make_float4(h[0], h[1], h[2], __double2float_rn(m.m));
     mc.com_lo[c] = make_float4(l[0], l[1], l[2], __double2float_rn(m.q[4]));
@@ -918,8 +930,8 @@ __device__ __forceinline__ float pair_pressure_f(const SphParams& prm, const Tar
   float paux = T.hyd.y * wi + facj * wj;
   if (dvdr < 0.0f) {
     const float winvrho = 0.25f * (wi + wj) * (T.hyd.z + invrhoj);
-    const float vsignal = T.hyd.w + soundj - (float) (prm.beta_visc * prm.alpha_visc) * dvdr;
-    const float av = (float) prm.alpha_visc * vsignal * dvdr * winvrho;
+    const float vsignal = T.hyd.w + soundj - prm.ab_visc_f * dvdr;
+    const float av = prm.alpha_visc_f * vsignal * dvdr * winvrho;
     paux -= av;
     dudt -= 0.5f * mj * av * dvdr;
   }
@@ -1082,7 +1094,7 @@ __device__ __forceinline__ void finish_particle_f(const SphParams& prm, const Pa
   const float rho = (float) p.rho[slot];
   const float invrho = __frcp_rn(rho);
   const float divv = dv * invrho;
-  const float P = (float) (prm.gamma_eos - 1.0) * rho * (float) p.u[slot];
+  const float P = prm.gm1_f * rho * (float) p.u[slot];
   p.div_v[slot] = (double) divv;
   p.dudt[slot] = (double) (du - P * divv * invrho * (float) p.invomega[slot]);
   p.ax[slot] = (double) ah[0] + agd[0];
@@ -1202,11 +1214,18 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
       }
     }
   };
+  // targets of the round u0..u0+7 that take terms (the pair counts are kept per source)
+  auto round_targets = [&](int u0) {
+    unsigned nu = 0;
+    for (int u = 0; u < 8 && u0 + u < ntg; u++) nu += (SLICES == 1 || tgt[u0 + u].w != 0.0f) ? 1u : 0u;
+    return nu;
+  };
   auto consume_c = [&]() {
 #pragma unroll
     for (int u0 = 0; u0 < GT; u0 += 8) {
       if (u0 >= ntg) break;
       float acc[8][4] = {};
+      const unsigned nu = round_targets(u0);
       for (int e = lane; e < L.nc; e += 32) {
         const int cc = L.c[e];
         const float4 ch = mc.com_hi[cc], cl = mc.com_lo[cc];
@@ -1246,8 +1265,8 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           acc[u][1] = __fmaf_rn(c1, dy, acc[u][1]);
           acc[u][2] = __fmaf_rn(c1, dz, acc[u][2]);
           acc[u][3] = __fmaf_rn(mc_, inv, acc[u][3]);
-          ncellp++;
         }
+        ncellp += nu;
         if (u0 == 0 && rec) {
           chash += mix64((unsigned long long) cc);
           ccount++;
@@ -1262,16 +1281,18 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     for (int u0 = 0; u0 < GT; u0 += 8) {
       if (u0 >= ntg) break;
       float acc[8][4] = {};
+      const unsigned nu = round_targets(u0);
       for (int e0 = 0; e0 < L.nb; e0 += LPG) {
         const int e = e0 + lane / GT, q = lane % GT;
         if (e >= L.nb) continue;
-        const int node = L.b[e];
-        if (q >= t.cell_n[node]) continue;
-        const int j = t.cell_first[node] + q;
+        const unsigned lw = (unsigned) L.b[e];
+        if (q >= leaf_count(lw)) continue;
+        const int j = leaf_first(lw) + q;
         const float4 pjh = mp.pos_hi[j], pjl = mp.pos_lo[j];
         float sx, sy, sz;
         rel(pjh, pjl, sx, sy, sz);
         const float mj = pjh.w;
+        ndir_b += nu;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
           if (u0 + u >= ntg) break;
@@ -1284,7 +1305,6 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
           const float inv3 = __fmul_rn(__fmul_rn(inv, inv), minv);
           acc[u][0] = __fmaf_rn(dx, inv3, acc[u][0]); acc[u][1] = __fmaf_rn(dy, inv3, acc[u][1]);
           acc[u][2] = __fmaf_rn(dz, inv3, acc[u][2]); acc[u][3] = __fadd_rn(acc[u][3], minv);
-          ndir_b++;
           if (rec) {
             const int ts = first + pfirst + (int) tu.w - 1;
             atomicAdd(&cnt.rec_dir_cnt[ts], 1ull);
@@ -1325,8 +1345,9 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     if (!mine) return;
     const int ntot = L.na * GT;
     for (int idx = sl; idx < ntot; idx += lpg) {
-      const int node = L.a[idx / GT], qq = idx % GT;
-      if (qq < t.cell_n[node]) near_pair(t.cell_first[node] + qq);
+      const unsigned lw = (unsigned) L.a[idx / GT];
+      const int qq = idx % GT;
+      if (qq < leaf_count(lw)) near_pair(leaf_first(lw) + qq);
     }
   };
   // the walk, with per-list flushing
@@ -1343,10 +1364,12 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     top -= take;
     __syncwarp();
     int act = kSkip, level = 0;
+    unsigned lw = 0;   // the leaf's list word (near and direct-sum entries)
     if (node >= 0) {
       const float4 mt = mc.meta[node];
       level = __float_as_int(mt.z);
       act = grav_decide(t, mc, G, node, level, mt, exact);
+      lw = pack_leaf(__float_as_int(mt.w), __float_as_int(mt.y));
     }
     const unsigned mo = __ballot_sync(kFull, act == kOpen);
     const int nopen = __popc(mo);
@@ -1368,8 +1391,8 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     const unsigned ma = __ballot_sync(kFull, ka);
     const unsigned mb = __ballot_sync(kFull, kb);
     const unsigned mcm = __ballot_sync(kFull, kc);
-    if (ka) L.a[L.na + __popc(ma & lt)] = node;
-    if (kb) L.b[L.nb + __popc(mb & lt)] = node;
+    if (ka) L.a[L.na + __popc(ma & lt)] = (int) lw;
+    if (kb) L.b[L.nb + __popc(mb & lt)] = (int) lw;
     if (kc) L.c[L.nc + __popc(mcm & lt)] = node;
     L.na += __popc(ma); L.nb += __popc(mb); L.nc += __popc(mcm);
     __syncwarp();
@@ -1748,6 +1771,8 @@ __global__ void __launch_bounds__(256) k_batch_forces_wide(BatchQueue q) {
 int grid1(int n) { return n < 1 ? 1 : (n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8; }
 
 }  // namespace
+
+int mixed_max_particles() { return kMixedMaxParticles; }
 
 void launch_mixed_prep_build(const Tree& t, const Particles& p, const MixedParticles& mp, const MixedCells& mc,
                              cudaStream_t st) {

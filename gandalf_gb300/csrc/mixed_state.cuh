@@ -23,7 +23,7 @@ struct MixedParticles {
 struct MixedCells {
   float4* geo_hi;   // rcell_hi xyz, rmax
   float4* geo_lo;   // rcell_lo xyz, hmax (after the h solve)
-  float4* meta;     // cdistsqd, cell_n and level (int bits), 0: one load per walk decision
+  float4* meta;     // cdistsqd, cell_n, level and cell_first (int bits): one load per walk decision
   float4* com_hi;   // com_hi xyz, m
   float4* com_lo;   // com_lo xyz, q4
   float4* quad;     // q0 q1 q2 q3
@@ -38,6 +38,8 @@ struct HeavyList {
   int* leaves;      // leaf indices
   int* count;       // device counter
 };
+
+int mixed_max_particles();   // the most particles the mixed form's list words address
 
 void launch_mixed_prep_build(const Tree& t, const Particles& p, const MixedParticles& mp,
                              const MixedCells& mc, cudaStream_t st);
