@@ -42,6 +42,12 @@ __device__ __forceinline__ unsigned pack_leaf(int first, int n) {
 __device__ __forceinline__ int leaf_first(unsigned w) { return (int) (w >> kLeafCountBits); }
 __device__ __forceinline__ int leaf_count(unsigned w) { return (int) (w & ((1u << kLeafCountBits) - 1u)) + 1; }
 
+// The w lane of a cell's float bounding-box maximum: (cell_first << 5) | level (at most 23
+// levels), so that a walk decision's box loads also give the list word of an emitted leaf.
+constexpr int kLevelBits = 5;
+__device__ __forceinline__ int box_level(float w) { return __float_as_int(w) & ((1 << kLevelBits) - 1); }
+__device__ __forceinline__ int box_first(float w) { return (int) ((unsigned) __float_as_int(w) >> kLevelBits); }
+
 // ---- preparation --------------------------------------------------------------------
 __device__ __forceinline__ void split2(double v, float& hi, float& lo) {
   hi = __double2float_rn(v);
@@ -78,7 +84,8 @@ __global__ void k_prep_build_cells(Tree t, MixedCells mc) {
     mc.bbmin[c] = make_float4(__double2float_rd(b.bbmin[0]), __double2float_rd(b.bbmin[1]),
                               __double2float_rd(b.bbmin[2]), __int_as_float(t.cell_n[c]));
     mc.bbmax[c] = make_float4(__double2float_ru(b.bbmax[0]), __double2float_ru(b.bbmax[1]),
-                              __double2float_ru(b.bbmax[2]), __int_as_float((int) t.cell_level[c]));
+                              __double2float_ru(b.bbmax[2]),
+                              __int_as_float((int) (((unsigned) t.cell_first[c] << kLevelBits) | t.cell_level[c])));
   }
 }
 
@@ -337,21 +344,38 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
               bmin[k] = __double2float_rd(gmin[k] - s);
               bmax[k] = __double2float_ru(gmax[k] - s);
             }
-            // cell count and level ride in the float box's w lanes: two loads a decision
+            // cell count, level and first slot ride in the float box's w lanes: two loads a
+            // decision, and an emitted leaf's list word (open boxes: the leaf itself; periodic
+            // boxes: node and image code, the slots read from the cell arrays)
+            unsigned lw = 0;
             auto decide = [&](int node, int& level) -> int {
               const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];
-              level = __float_as_int(b1.w);
+              level = box_level(b1.w);
               if (__float_as_int(b0.w) == 0) return kSkip;
               if (!fbox_overlap(bmin, bmax, b0, b1)) return kSkip;
+              lw = pack_leaf(box_first(b1.w), __float_as_int(b0.w));
               return level == t.ltot ? kEmitA : kOpen;
             };
-            auto tag = [&](int node, int) { return node | (code << kNodeBits); };
+            auto tag = [&](int node, int) { return prm.periodic ? node | (code << kNodeBits) : (int) lw; };
             stack_ok = stack_ok && warp_walk_lv(0, t.ltot, stack, kDensStack, L, decide, tag, flush);
           }
     };
     walk_all([&]() { overflow = true; });
     if (give_up && __any_sync(kFull, overflow)) return 2;
     const int ncached = L.na;
+    // a gather-list entry: the leaf's first slot and count, and the periodic image code
+    auto entry = [&](int tagv, int& f, int& nn, int& code) {
+      if (prm.periodic) {
+        const int node = tagv & ((1 << kNodeBits) - 1);
+        code = tagv >> kNodeBits;
+        f = t.cell_first[node];
+        nn = t.cell_n[node];
+      } else {
+        f = leaf_first((unsigned) tagv);
+        nn = leaf_count((unsigned) tagv);
+        code = kNoShift;
+      }
+    };
 
     // The candidate's separation from this particle in float (false: that periodic
     // image does not exist, ghost semantics as in the fp64 form).
@@ -436,10 +460,9 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
           bool valid = false;
           float4 ch = make_float4(0.f, 0.f, 0.f, 0.f), cl = ch;
           if (e < ncached) {
-            const int tagv = list[e];
-            const int node = tagv & ((1 << kNodeBits) - 1);
-            const int code = tagv >> kNodeBits;
-            if (q < t.cell_n[node]) valid = cand_pos(t.cell_first[node] + q, code, ch, cl);
+            int f, nn, code;
+            entry(list[e], f, nn, code);
+            if (q < nn) valid = cand_pos(f + q, code, ch, cl);
           }
           const float cx = (ch.x - lch.x) + (cl.x - lcl.x);
           const float cy = (ch.y - lch.y) + (cl.y - lcl.y);
@@ -524,10 +547,8 @@ __device__ __forceinline__ bool density_cell(const Tree& t, const Particles& p, 
       auto consume = [&](int count) {
         if (done) return;
         for (int e = 0; e < count; e++) {
-          const int tagv = list[e];
-          const int node = tagv & ((1 << kNodeBits) - 1);
-          const int code = tagv >> kNodeBits;
-          const int f = t.cell_first[node], nn = t.cell_n[node];
+          int f, nn, code;
+          entry(list[e], f, nn, code);
           for (int q = sl; q < nn; q += LPG) {
             float d2, mj;
             if (cand(f + q, code, d2, mj)) add(d2, mj);
@@ -750,8 +771,8 @@ __device__ __forceinline__ void density_pp_leaf(const Tree& t, const Particles& 
                 bmax[q] = __double2float_ru(gmax[q] - sft);
               }
               auto decide = [&](int node, int& level) -> int {
-                const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];   // w: cell_n, level
-                level = __float_as_int(b1.w);
+                const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];   // w: cell_n, first << 5 | level
+                level = box_level(b1.w);
                 if (__float_as_int(b0.w) == 0) return kSkip;
                 if (!fbox_overlap(bmin, bmax, b0, b1)) return kSkip;
                 return level == t.ltot ? kEmitA : kOpen;
@@ -1569,8 +1590,8 @@ __device__ __forceinline__ void hydro_leaf(const Tree& t, const Particles& p, co
     return true;
   };
   auto decide = [&](int node, int& level) -> int {
-    const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];   // w: cell_n, level
-    level = __float_as_int(b1.w);
+    const float4 b0 = mc.bbmin[node], b1 = mc.bbmax[node];   // w: cell_n, first << 5 | level
+    level = box_level(b1.w);
     if (__float_as_int(b0.w) == 0) return kSkip;
     if (!(pbox(bmin_f, bmax_f, mc.hbmin[node], mc.hbmax[node]) || pbox(hmin_f, hmax_f, b0, b1)))
       return kSkip;

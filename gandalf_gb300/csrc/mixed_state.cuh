@@ -27,8 +27,8 @@ struct MixedCells {
   float4* com_hi;   // com_hi xyz, m
   float4* com_lo;   // com_lo xyz, q4
   float4* quad;     // q0 q1 q2 q3
-  float4* bbmin;    // bounding box rounded outwards
-  float4* bbmax;
+  float4* bbmin;    // bounding box rounded outwards; w: cell_n (int bits)
+  float4* bbmax;    // w: (cell_first << 5) | level (int bits)
   float4* hbmin;    // smoothing-volume box rounded outwards
   float4* hbmax;
 };
