@@ -973,9 +973,8 @@ __device__ __forceinline__ void hydro_pair_f(const SphParams& prm, const MixedPa
   A.ah[0] += mj * ux * paux; A.ah[1] += mj * uy * paux; A.ah[2] += mj * uz * paux;
 }
 
-__device__ __forceinline__ void hydro_grav_pair_f(const SphParams& prm, const MixedParticles& mp, const TargetF& T,
-                                                  int j, float dx, float dy, float dz, float d2, float mj, AccF& A) {
-  const float4 vj = mp.vel[j], hj = mp.hyd[j], xj = mp.aux[j];
+__device__ __forceinline__ void hydro_grav_pair_f(const SphParams& prm, const TargetF& T, float4 vj, float4 hj,
+                                                  float4 xj, float dx, float dy, float dz, float d2, float mj, AccF& A) {
   const float r2 = d2 + 1.0e-20f;
   const float invdrmag = rsqrtf(r2);
   const float drmag = r2 * invdrmag;
@@ -1345,8 +1344,9 @@ __device__ __forceinline__ bool all_forces_leaf(const Tree& t, const Particles& 
     const float dy = (pjh.y - T.ph.y) + (pjl.y - T.pl.y);
     const float dz = (pjh.z - T.ph.z) + (pjl.z - T.pl.z);
     const float d2 = dx * dx + dy * dy + dz * dz;
+    const float4 vj = mp.vel[j], hj = mp.hyd[j], xj = mp.aux[j];
     if (sph_member(p, T, j, d2, pjl.w, prm, exact)) {
-      hydro_grav_pair_f(prm, mp, T, j, dx, dy, dz, d2, pjh.w, A);
+      hydro_grav_pair_f(prm, T, vj, hj, xj, dx, dy, dz, d2, pjh.w, A);
       lvn_pair(p, slot, j, lvn_own);
       nsph++;
       if (rec) {
