@@ -636,8 +636,19 @@ __global__ void __launch_bounds__(kPartThreads) k_part_level(int l, int n, Build
 // child boxes, side marks and stable partitions as the level passes, on 16-bit local ids
 // (a particle's position in the segment's x list), with one launch instead of five per
 // level.  The block writes the segment's final first list (leaf order) back in place.
-constexpr int kDeepMax = 1024;
-constexpr int kDeepThreads = 512;
+constexpr int kDeepMax = 4096;
+constexpr int kDeepThreads = 1024;
+constexpr int kDeepPer = kDeepMax / kDeepThreads;   // list positions a thread scans
+
+// 86 KB: above the static shared-memory limit, so it is dynamic (one or two blocks an SM)
+struct DeepSmem {
+  unsigned short l[2][3][kDeepMax];
+  int glob[kDeepMax];
+  int scan[kDeepMax];
+  unsigned char side[kDeepMax];
+  unsigned char kd[kDeepMax / 2];
+  int ws[33];
+};
 
 __global__ void __launch_bounds__(kDeepThreads) k_build_deep(int L0, int ltot, BuildLists cur, int* inv,
                                                             const double* __restrict__ x,
@@ -645,12 +656,14 @@ __global__ void __launch_bounds__(kDeepThreads) k_build_deep(int L0, int ltot, B
                                                             const double* __restrict__ z,
                                                             const int* __restrict__ heap_first,
                                                             const int* __restrict__ heap_n, double* ibox) {
-  __shared__ unsigned short s_l[2][3][kDeepMax];
-  __shared__ int s_glob[kDeepMax];
-  __shared__ int s_scan[kDeepMax];
-  __shared__ unsigned char s_side[kDeepMax];
-  __shared__ unsigned char s_kd[kDeepMax / 2];
-  __shared__ int ws[33];
+  extern __shared__ __align__(16) unsigned char s_deep_raw[];
+  DeepSmem& sm = *reinterpret_cast<DeepSmem*>(s_deep_raw);
+  auto& s_l = sm.l;
+  int* s_glob = sm.glob;
+  int* s_scan = sm.scan;
+  unsigned char* s_side = sm.side;
+  unsigned char* s_kd = sm.kd;
+  int* ws = sm.ws;
   const int tid = threadIdx.x;
   const int s0 = blockIdx.x;
   const int h0 = (1 << L0) - 1 + s0;
@@ -704,22 +717,30 @@ __global__ void __launch_bounds__(kDeepThreads) k_build_deep(int L0, int ltot, B
     __syncthreads();
     // stable partition of the three lists inside each sub-segment (k_part_scatter)
     for (int a = 0; a < 3; a++) {
-      const int q0 = 2 * tid, q1 = q0 + 1;
-      const int f0 = q0 < cnt ? s_side[s_l[cb][a][q0]] : 0;
-      const int f1 = q1 < cnt ? s_side[s_l[cb][a][q1]] : 0;
+      // positions q0 .. q0 + kDeepPer - 1 of the list, consecutive per thread
+      const int q0 = kDeepPer * tid;
+      int fl[kDeepPer], sum = 0;
+#pragma unroll
+      for (int r = 0; r < kDeepPer; r++) {
+        fl[r] = q0 + r < cnt ? s_side[s_l[cb][a][q0 + r]] : 0;
+        sum += fl[r];
+      }
       int total;
-      const int ex = block_exscan(f0 + f1, ws, total);
-      if (q0 < cnt) s_scan[q0] = ex;
-      if (q1 < cnt) s_scan[q1] = ex + f0;
+      int run = block_exscan(sum, ws, total);
+#pragma unroll
+      for (int r = 0; r < kDeepPer; r++) {
+        if (q0 + r < cnt) s_scan[q0 + r] = run;
+        run += fl[r];
+      }
       __syncthreads();
-      const int qq[2] = {q0, q1}, ff[2] = {f0, f1};
-      for (int r = 0; r < 2; r++) {
-        const int q = qq[r];
+#pragma unroll
+      for (int r = 0; r < kDeepPer; r++) {
+        const int q = q0 + r;
         if (q >= cnt) continue;
         int f, c;
         seg_of(q, cnt, d, f, c);
         const int ones = s_scan[q] - s_scan[f];   // ones before q inside its sub-segment
-        const int pos = ff[r] ? f + (c >> 1) + ones : f + (q - f) - ones;
+        const int pos = fl[r] ? f + (c >> 1) + ones : f + (q - f) - ones;
         s_l[cb ^ 1][a][pos] = s_l[cb][a][q];
       }
       __syncthreads();
@@ -1145,7 +1166,8 @@ int launch_build_tree(const BuildArgs& a, cudaStream_t st) {
     BuildLists tmp = cur; cur = nxt; nxt = tmp;
   }
   if (L0 < a.ltot) {
-    k_build_deep<<<1 << L0, kDeepThreads, 0, st>>>(L0, a.ltot, cur, a.deep_inv, a.in.x, a.in.y, a.in.z,
+    cudaFuncSetAttribute(k_build_deep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(DeepSmem));
+    k_build_deep<<<1 << L0, kDeepThreads, sizeof(DeepSmem), st>>>(L0, a.ltot, cur, a.deep_inv, a.in.x, a.in.y, a.in.z,
                                                    a.heap_first, a.heap_n, a.ibox);
     launches++;
   }
