@@ -59,7 +59,7 @@ FORCE_TRAFFIC = {
                                           "source": "profiles/forces_density_mixed_plummer262k_dram.md"},
     # the warp-per-leaf force kernel of a KDK first pass, cold L2 (ncu flushes caches), mean
     # of three launches
-    ("rotating_cloud", 1048576, "mixed"): {"bytes": 282.0e6,
+    ("rotating_cloud", 1048576, "mixed"): {"bytes": 244.0e6,
                                            "source": "profiles/forces_mixed_rotating_cloud1m_dram.md"},
 }
 
