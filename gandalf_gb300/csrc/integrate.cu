@@ -19,9 +19,23 @@ constexpr double kInvLogTwo = 1.44269504088896;  // invlogetwo, src/Headers/Cons
 
 __device__ __forceinline__ int pow2i(int k) { return k >= 0 ? (1 << k) : 0; }   // (int) pow(2, k)
 
-// ComputeTimestepLevel (src/Headers/InlineFuncs.h:550-557)
+// ComputeTimestepLevel (src/Headers/InlineFuncs.h:550-557): (int) (invlogetwo log q) + 1,
+// q = dt_max / dt.  For q = M 2^E with 0 <= E < 64 and the mantissa M in [1 + 2^-40,
+// 2 - 2^-40], log2 q lies at least 6.5e-13 inside (E, E + 1), while invlogetwo log q is
+// within 1.8e-13 of log2 q (invlogetwo is 2.4e-15 relative below 1/ln 2, the logarithm and
+// the product within an ulp each, |log2 q| < 64): the truncation is E, and the level E + 1
+// is read from the exponent bits.  The fp64 logarithm (GB300: fp64 at 1/64 of the fp32
+// rate) is taken only for the other quotients.
 __device__ __forceinline__ int timestep_level(double dt, double dt_max) {
-  const int l = (int) __dmul_rn(kInvLogTwo, log(__ddiv_rn(dt_max, dt))) + 1;
+  const double q = __ddiv_rn(dt_max, dt);
+  const long long b = __double_as_longlong(q);
+  const int ebits = (int) ((b >> 52) & 0x7ff);
+  const long long mant = b & ((1ll << 52) - 1);
+  int l;
+  if (b > 0 && ebits >= 1023 && ebits < 1023 + 64 && mant >= (1ll << 12) && mant <= (1ll << 52) - (1ll << 12))
+    l = ebits - 1023 + 1;
+  else
+    l = (int) __dmul_rn(kInvLogTwo, log(q)) + 1;
   return l > 0 ? l : 0;
 }
 
