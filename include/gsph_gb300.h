@@ -59,7 +59,8 @@ typedef struct gsph_config {
   int32_t eos;           /* "gas_eos": energy_eqn or isothermal */
   int32_t multipole;     /* "multipole": monopole or quadrupole (geometric MAC) */
   int32_t periodic;      /* 1: periodic in x, y and z ("boundary_lhs/rhs" = periodic) */
-  int32_t precision;     /* GSPH_PRECISION_FP64 or GSPH_PRECISION_MIXED */
+  int32_t precision;     /* GSPH_PRECISION_FP64 or GSPH_PRECISION_MIXED (at most 2^27
+                            particles: larger sets return GSPH_ERR_UNSUPPORTED) */
   double h_fac;          /* "h_fac" */
   double h_converge;     /* "h_converge" */
   double alpha_visc;     /* "alpha_visc" (avisc = mon97) */
