@@ -233,3 +233,36 @@ def test_gravity_lists_as_full_sets(precision):
     for leaf, cells in zip(leaves, cl):
         np.testing.assert_array_equal(np.sort(cells), ref_cells[int(leaf)])
     assert sum(len(x) for x in dl) > 0 and sum(len(x) for x in cl) > 0
+
+
+@pytest.mark.parametrize("nleafmax", [1, 32])
+def test_mixed_lists_at_extreme_leaf_sizes(nleafmax):
+    """The mixed form's near and direct-sum lists hold each leaf as one word (first slot and
+    count): at one particle a leaf and at 32 (one lane a particle) the lists are the
+    oracle's as full sets, the oracle run on the mixed form's own smoothing lengths."""
+    c = ics_mod.plummer_sphere(3000, seed=3100 + nleafmax)
+    params = dict(c["params"], nleafmax=nleafmax)
+    t = GradhSphTree(params, precision="mixed")
+    t.set_particles(c)
+    t.set_recording(True, 1024)
+    t.set_list_recording(8192, 8192)
+    t.step()
+    got = t.results()
+    dl = t.direct_lists()
+    leaves, _, _ = t.cell_summary()
+    cl = t.cell_lists()
+    nb = t.sph_neighbours()
+    t.close()
+    given = {k: got[k] for k in ("h", "rho", "invomega", "zeta", "pressure", "sound")}
+    r = oracle.run(c, params, lists=True, given=given)
+    assert same_lists(nb, r["hydro_neib"]) == []
+    assert same_lists(dl, r["grav_direct"]) == []
+    ref_cells = {int(l): np.sort(g) for l, g in zip(r["gcell_leaf"], r["gcell_lists"])}
+    mine = {int(l): np.sort(g) for l, g in zip(leaves, cl)}
+    # the complete tree's empty leaves (no particle, so no walk) appear on this side only
+    assert set(ref_cells) <= set(mine)
+    for leaf, cells in mine.items():
+        if leaf in ref_cells:
+            np.testing.assert_array_equal(cells, ref_cells[leaf])
+        else:
+            assert len(cells) == 0
